@@ -1,0 +1,109 @@
+"""Regenerate the golden fixtures in this folder from the MATLAB reference's own data.
+
+The reference (project-asgard/DG-SparseGrid) cannot run here (no MATLAB or Octave), so its
+committed gold files are the executable-free pins for the oracle.  This script reads them
+once, in the container that has the reference checked out, and packs the subset the
+``apply_A`` hot path needs into small ``.npz`` files that travel with the tests:
+
+* ``two_scale_rel.npz``   -- H0/G0/scale_co/phi_co of ``two_scale/two_scale_rel_{1..8}.mat``
+                             (the multiwavelet filters ``OperatorTwoScale_wavelet2.m:18-26`` loads)
+* ``element_table.npz``   -- ``gold/generated-inputs/element_table/{table,ids}_{1,2,3}d_{SG,FG}.dat``
+                             and ``1d_index_*.dat`` (``gold/gold_hash_table.m:11-80``)
+* ``connectivity.npz``    -- ``connect_1_{2,3,8}.dat``, ``connect_n_2_3_FG_*.dat``,
+                             ``connect_n_3_4_SG_*.dat`` (``gold/gold_connect.m:19-57``)
+* ``permutations.npz``    -- ``gold/generated-inputs/permutations/*`` (``gold/gold_permute.m``)
+* ``quadrature.npz``      -- ``gold/generated-inputs/quadrature/*`` (``gold/gold_quadrature.m``)
+* ``transformations.npz`` -- ``operator_two_scale_*.dat``, ``multiwavelet_*.dat``, ``combine_dim_*.dat``
+* ``time_advance.npz``    -- RK3 trajectories ``continuity{1,2,3}_*_t{0..4}.dat``
+                             (``gold/gold_time_advance.m:252-364``)
+
+Run:  python tests/golden/make_golden.py [reference_root]
+"""
+import glob
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def read_octave_text(path):
+    """Parse the ``write_octave_like_output.m`` format: '#' header lines, then rows."""
+    rows = None
+    cols = None
+    data = []
+    with open(path) as fh:
+        for line in fh:
+            if line.startswith("#"):
+                m = re.match(r"#\s*rows:\s*(\d+)", line)
+                if m:
+                    rows = int(m.group(1))
+                m = re.match(r"#\s*columns:\s*(\d+)", line)
+                if m:
+                    cols = int(m.group(1))
+                continue
+            s = line.strip()
+            if s:
+                data.extend(float(v) for v in s.split())
+    arr = np.array(data, dtype=np.float64)
+    if rows is not None and cols is not None:
+        if rows * cols == 0:
+            return np.zeros((rows, cols))
+        arr = arr.reshape(rows, cols)
+    return arr
+
+
+def main(ref_root):
+    gold = os.path.join(ref_root, "gold", "generated-inputs")
+
+    # ---- two-scale filters -------------------------------------------------------------
+    import scipy.io as sio
+
+    ts = {}
+    for deg in range(1, 9):
+        m = sio.loadmat(os.path.join(ref_root, "two_scale", "two_scale_rel_%d.mat" % deg))
+        for key in ("H0", "G0", "scale_co", "phi_co"):
+            ts["%s_%d" % (key, deg)] = np.asarray(m[key], dtype=np.float64)
+    np.savez_compressed(os.path.join(HERE, "two_scale_rel.npz"), **ts)
+
+    def pack(subdir, pattern, outname, keyfn=None):
+        out = {}
+        for path in sorted(glob.glob(os.path.join(gold, subdir, pattern))):
+            name = os.path.basename(path)[:-4]
+            key = keyfn(name) if keyfn else name
+            out[key] = read_octave_text(path)
+        np.savez_compressed(os.path.join(HERE, outname), **out)
+        return len(out)
+
+    n = 0
+    n += pack("element_table", "*.dat", "element_table.npz")
+    out = {}
+    for pat in ("connect_1_*.dat", "connect_n_2_3_FG_*.dat", "connect_n_3_4_SG_*.dat"):
+        for path in sorted(glob.glob(os.path.join(gold, "connectivity", pat))):
+            out[os.path.basename(path)[:-4]] = read_octave_text(path)
+    np.savez_compressed(os.path.join(HERE, "connectivity.npz"), **out)
+    n += len(out)
+    n += pack("permutations", "*.dat", "permutations.npz")
+    n += pack("quadrature", "*.dat", "quadrature.npz")
+    out = {}
+    for pat in ("operator_two_scale_*.dat", "multiwavelet_*.dat", "combine_dim_*.dat"):
+        for path in sorted(glob.glob(os.path.join(gold, "transformations", pat))):
+            out[os.path.basename(path)[:-4]] = read_octave_text(path)
+    np.savez_compressed(os.path.join(HERE, "transformations.npz"), **out)
+    n += len(out)
+    out = {}
+    for stem in ("continuity1_sg_l2_d2", "continuity1_sg_l4_d3", "continuity1_fg_l2_d2",
+                 "continuity2_sg_l2_d2", "continuity2_sg_l4_d3", "continuity2_fg_l2_d2",
+                 "continuity3_sg_l2_d2", "continuity3_sg_l4_d3"):
+        for t in range(5):
+            path = os.path.join(gold, "time_advance", "%s_t%d.dat" % (stem, t))
+            out["%s_t%d" % (stem, t)] = read_octave_text(path).reshape(-1)
+    np.savez_compressed(os.path.join(HERE, "time_advance.npz"), **out)
+    n += len(out)
+    print("packed %d gold arrays into %s" % (n, HERE))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
