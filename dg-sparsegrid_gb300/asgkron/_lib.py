@@ -1,0 +1,119 @@
+"""ctypes binding of libasgkron.so (the C ABI declared in include/asgkron.h).
+
+The library must have been built (``asgkron._build.build()`` or ``__graft_entry__.build()``);
+loading fails loudly otherwise -- there is no CPU fallback for any entry point.
+"""
+import ctypes as C
+import os
+
+from . import _build
+
+ASG_OK = 0
+ASG_ERR_INVALID = 1
+ASG_ERR_UNSUPPORTED = 2
+ASG_ERR_CUDA = 3
+ASG_ERR_NOMEM = 4
+ASG_ERR_TIMEOUT = 5
+ASG_ERR_CAPACITY = 6
+_NAMES = {1: "ASG_ERR_INVALID", 2: "ASG_ERR_UNSUPPORTED", 3: "ASG_ERR_CUDA", 4: "ASG_ERR_NOMEM",
+          5: "ASG_ERR_TIMEOUT", 6: "ASG_ERR_CAPACITY"}
+
+ASG_STRUCT_NONE = 0
+ASG_STRUCT_DETECT = 1
+ASG_GRID_SG = 0
+ASG_GRID_FG = 1
+KERNEL_CHAIN_WARP, KERNEL_CHAIN_CTA, KERNEL_SINGLE_MODE = 0, 1, 2
+
+
+class AsgError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("%s: %s" % (_NAMES.get(status, status), msg))
+        self.status = status
+
+
+class PlanDesc(C.Structure):
+    _fields_ = [
+        ("num_dims", C.c_int),
+        ("deg", C.c_int),
+        ("num_terms", C.c_int),
+        ("num_elems", C.c_int),
+        ("index_base", C.c_int),
+        ("idx1d", C.POINTER(C.c_int)),
+        ("row_ptr", C.POINTER(C.c_longlong)),
+        ("cols", C.POINTER(C.c_int)),
+        ("ops", C.POINTER(C.POINTER(C.c_double))),
+        ("op_ld", C.POINTER(C.c_int)),
+        ("structure", C.c_int),
+        ("drop_tol", C.c_double),
+    ]
+
+
+class PlanStats(C.Structure):
+    _fields_ = [
+        ("num_pairs", C.c_longlong),
+        ("num_entries", C.c_longlong),
+        ("dof", C.c_longlong),
+        ("flops_reference", C.c_double),
+        ("flops_executed", C.c_double),
+        ("op_bytes_f64", C.c_longlong),
+        ("kernel_kind", C.c_int),
+        ("active_modes_max", C.c_int),
+    ]
+
+
+# name -> (restype, argtypes); every symbol include/asgkron.h declares
+SIGNATURES = {
+    "asg_version": (C.c_char_p, []),
+    "asg_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
+    "asg_plan_create": (C.c_int, [C.POINTER(PlanDesc), C.POINTER(C.c_void_p)]),
+    "asg_plan_destroy": (C.c_int, [C.c_void_p]),
+    "asg_plan_stats_get": (C.c_int, [C.c_void_p, C.POINTER(PlanStats)]),
+    "asg_plan_update_ops": (C.c_int, [C.c_void_p, C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.c_int)]),
+    "asg_plan_set_kernel": (C.c_int, [C.c_void_p, C.c_int]),
+    "asg_apply_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "asg_apply_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "asg_apply_host_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "asg_apply_host_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "asg_hash_table_sparse_nd": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.c_int, C.c_int, C.POINTER(C.c_int),
+                                           C.POINTER(C.c_int), C.POINTER(C.c_ulonglong), C.c_longlong,
+                                           C.POINTER(C.c_longlong)]),
+    "asg_hash_table_nd": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_longlong,
+                                    C.POINTER(C.c_longlong)]),
+    "asg_element_idx1d": (C.c_int, [C.c_int, C.c_longlong, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                    C.POINTER(C.c_int)]),
+    "asg_connect_nd": (C.c_int, [C.c_int, C.c_longlong, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int, C.c_int,
+                                 C.c_int, C.POINTER(C.c_longlong), C.POINTER(C.c_int), C.c_longlong,
+                                 C.POINTER(C.c_longlong)]),
+}
+
+_LIB = None
+
+
+def lib():
+    """The loaded library (built on first use if the sources are newer)."""
+    global _LIB
+    if _LIB is None:
+        path = _build.LIB_PATH
+        if not os.path.exists(path):
+            _build.build()
+        if not os.path.exists(path):
+            raise ImportError("libasgkron.so is missing; run __graft_entry__.build()")
+        L = C.CDLL(path)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def last_error():
+    buf = C.create_string_buffer(1024)
+    lib().asg_last_error(buf, 1024)
+    return buf.value.decode(errors="replace")
+
+
+def check(status):
+    if status != ASG_OK:
+        raise AsgError(status, last_error())
+    return status

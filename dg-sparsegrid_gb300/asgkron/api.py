@@ -1,0 +1,212 @@
+"""Host-side mirror of the reference's operator-application interface.
+
+``Plan`` wraps one ``asg_plan`` (operators + element 1-D indices + pair list) and applies
+``y = A*f`` on the GPU, either on device tensors (torch CUDA tensors are used only as
+device memory and stream handles) or on host arrays.  ``apply_A`` keeps the MATLAB
+signature of apply_A.m:1 and caches plans the way a MEX gateway would keep a persistent
+handle.
+"""
+import ctypes as C
+
+import numpy as np
+
+from ._lib import (ASG_STRUCT_DETECT, ASG_STRUCT_NONE, PlanDesc, PlanStats, check, lib)
+
+# |entry| <= DEFAULT_DROP_TOL * max|op| is treated as an exact zero by the structure
+# analysis.  The wavelet-space mass factors differ from the identity by ~1e-15 relative
+# (rotation round-off), which this threshold absorbs; the induced change of y is far
+# below the 1e-12 FP64 parity bound.
+DEFAULT_DROP_TOL = 1e-13
+
+
+def _as_term_mats(term_mats):
+    out = []
+    for row in term_mats:
+        out.append([np.asfortranarray(np.asarray(m, dtype=np.float64)) for m in row])
+    return out
+
+
+class Plan:
+    """y = A f for fixed operators, element indices and pair list.
+
+    term_mats: T lists of d dense 1-D operators (pde.terms{t}.terms_1D{d}.mat).
+    idx1d:     [N, d] 1-D indices (A_data.element_local_index_D), base ``index_base``.
+    pairs:     None (all pairs, the apply_A default) or (row_ptr, cols) CSR.
+    structure: "none" (reference work model) or "detect" (skip zero blocks, identity
+               factors as copies; ``drop_tol`` relative threshold).
+    """
+
+    def __init__(self, term_mats, idx1d, pairs=None, structure="detect", drop_tol=DEFAULT_DROP_TOL, index_base=1):
+        mats = _as_term_mats(term_mats)
+        idx = np.ascontiguousarray(np.asarray(idx1d, dtype=np.int32))
+        if idx.ndim != 2:
+            raise ValueError("idx1d must be [num_elems, num_dims]")
+        N, D = idx.shape
+        T = len(mats)
+        if T == 0 or any(len(r) != D for r in mats):
+            raise ValueError("term_mats must hold num_terms lists of num_dims operators")
+        deg = None
+        self.term_mats = mats
+        self.N, self.D, self.T = N, D, T
+        self._keep = [mats, idx]
+        ptrs = (C.POINTER(C.c_double) * (T * D))()
+        lds = (C.c_int * (T * D))()
+        for t in range(T):
+            for d in range(D):
+                m = mats[t][d]
+                if m.ndim != 2 or m.shape[0] != m.shape[1]:
+                    raise ValueError("operator (term %d, dim %d) must be square" % (t, d))
+                ptrs[t * D + d] = m.ctypes.data_as(C.POINTER(C.c_double))
+                lds[t * D + d] = m.shape[0]
+        self._ptrs, self._lds = ptrs, lds
+        desc = PlanDesc()
+        desc.num_dims = D
+        desc.num_terms = T
+        desc.num_elems = N
+        desc.index_base = int(index_base)
+        desc.idx1d = idx.ctypes.data_as(C.POINTER(C.c_int))
+        if pairs is not None:
+            rp = np.ascontiguousarray(np.asarray(pairs[0], dtype=np.int64))
+            cl = np.ascontiguousarray(np.asarray(pairs[1], dtype=np.int32))
+            if cl.size == 0:
+                cl = np.zeros(1, dtype=np.int32)
+            self._keep += [rp, cl]
+            desc.row_ptr = rp.ctypes.data_as(C.POINTER(C.c_longlong))
+            desc.cols = cl.ctypes.data_as(C.POINTER(C.c_int))
+        desc.ops = ptrs
+        desc.op_ld = lds
+        desc.structure = ASG_STRUCT_DETECT if structure == "detect" else ASG_STRUCT_NONE
+        desc.drop_tol = float(drop_tol) if structure == "detect" else 0.0
+        self.deg = deg
+        self._desc = desc
+        self._handle = C.c_void_p()
+
+    def _create(self, deg):
+        self._desc.deg = int(deg)
+        self.deg = int(deg)
+        check(lib().asg_plan_create(C.byref(self._desc), C.byref(self._handle)))
+        self.B = self.deg ** self.D
+        self.dof = self.N * self.B
+
+    @classmethod
+    def create(cls, term_mats, idx1d, deg, **kw):
+        p = cls(term_mats, idx1d, **kw)
+        p._create(deg)
+        return p
+
+    # ---------------------------------------------------------------------------------
+    @property
+    def handle(self):
+        return self._handle.value
+
+    def stats(self):
+        s = PlanStats()
+        check(lib().asg_plan_stats_get(self._handle, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in PlanStats._fields_}
+
+    def set_kernel(self, kind):
+        check(lib().asg_plan_set_kernel(self._handle, int(kind)))
+
+    def update_ops(self, term_mats):
+        mats = _as_term_mats(term_mats)
+        ptrs = (C.POINTER(C.c_double) * (self.T * self.D))()
+        lds = (C.c_int * (self.T * self.D))()
+        for t in range(self.T):
+            for d in range(self.D):
+                ptrs[t * self.D + d] = mats[t][d].ctypes.data_as(C.POINTER(C.c_double))
+                lds[t * self.D + d] = mats[t][d].shape[0]
+        check(lib().asg_plan_update_ops(self._handle, ptrs, lds))
+        self.term_mats = mats
+        self._keep[0] = mats
+
+    def apply(self, f, y=None, stream=None):
+        """Device apply on CUDA tensors (float64 or float32); returns y."""
+        import torch
+
+        if not (f.is_cuda and f.is_contiguous() and f.numel() == self.dof):
+            raise ValueError("f must be a contiguous CUDA tensor with %d values" % self.dof)
+        if y is None:
+            y = torch.empty_like(f)
+        if y.dtype != f.dtype or not y.is_cuda or y.numel() != self.dof or not y.is_contiguous():
+            raise ValueError("y must match f")
+        s = stream if stream is not None else torch.cuda.current_stream(f.device)
+        sp = C.c_void_p(s.cuda_stream)
+        if f.dtype == torch.float64:
+            check(lib().asg_apply_f64(self._handle, C.c_void_p(f.data_ptr()), C.c_void_p(y.data_ptr()), sp))
+        elif f.dtype == torch.float32:
+            check(lib().asg_apply_f32(self._handle, C.c_void_p(f.data_ptr()), C.c_void_p(y.data_ptr()), sp))
+        else:
+            raise TypeError("f must be float64 or float32")
+        return y
+
+    def apply_host(self, f, out=None):
+        """Host apply (copies in/out inside the library); numpy float64 or float32."""
+        f = np.ascontiguousarray(f)
+        if f.size != self.dof:
+            raise ValueError("f must hold %d values" % self.dof)
+        if out is None:
+            out = np.empty_like(f)
+        if f.dtype == np.float64:
+            check(lib().asg_apply_host_f64(self._handle, f.ctypes.data, out.ctypes.data))
+        elif f.dtype == np.float32:
+            check(lib().asg_apply_host_f32(self._handle, f.ctypes.data, out.ctypes.data))
+        else:
+            raise TypeError("f must be float64 or float32")
+        return out
+
+    def close(self):
+        if self._handle:
+            lib().asg_plan_destroy(self._handle)
+            self._handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# -------------------------------------------------------------------------------------
+# MATLAB-signature mirror: [ftmp, A, ALHS] = apply_A(pde, opts, A_data, f, deg, Vmax, Emax, imex_flag)
+# -------------------------------------------------------------------------------------
+_PLAN_CACHE = {}
+
+
+def clear_plan_cache():
+    for p in _PLAN_CACHE.values():
+        p.close()
+    _PLAN_CACHE.clear()
+
+
+def _get(obj, name, default=None):
+    if isinstance(obj, dict):
+        return obj.get(name, default)
+    return getattr(obj, name, default)
+
+
+def apply_A(pde, opts, A_data, f, deg, Vmax=None, Emax=None, imex_flag="N"):
+    """Mirror of apply_A.m:1-252 (explicit path): returns ftmp = A*f as float64 numpy.
+
+    pde.terms[t].terms_1D[d].mat and pde.terms[t].imex select the terms (apply_A.m:19-28);
+    opts.use_connectivity selects pde.connectivity (1-based lists) over all pairs
+    (apply_A.m:44-52).  Plans are cached per operator/index set like a MEX persistent
+    handle; call clear_plan_cache() after mutating operators in place."""
+    terms = [t for t in _get(pde, "terms") if _get(t, "imex", "N") == imex_flag]
+    if not terms:
+        return np.zeros(np.asarray(f).size)
+    mats = [[_get(sd, "mat") for sd in _get(t, "terms_1D")] for t in terms]
+    idx = np.stack([np.asarray(v).reshape(-1) for v in _get(A_data, "element_local_index_D")], axis=1)
+    pairs = None
+    if _get(opts, "use_connectivity", False):
+        conn = _get(pde, "connectivity")
+        lens = np.array([len(c) for c in conn], dtype=np.int64)
+        rp = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
+        cl = np.concatenate([np.asarray(c, dtype=np.int64).reshape(-1) for c in conn]).astype(np.int32)
+        pairs = (rp, cl)
+    key = (tuple((id(m), m.shape) for row in mats for m in row), idx.tobytes(), int(deg),
+           None if pairs is None else (pairs[0].tobytes(), pairs[1].tobytes()))
+    plan = _PLAN_CACHE.get(key)
+    if plan is None:
+        plan = Plan.create(mats, idx, deg, pairs=pairs, structure="detect", index_base=1)
+        _PLAN_CACHE[key] = plan
+    return plan.apply_host(np.asarray(f, dtype=np.float64).reshape(-1))

@@ -1,0 +1,135 @@
+"""The PDEs of the benchmark configurations, as term/source specifications.
+
+Each follows the reference's pdes/*.m file it names: domains, per-dimension partial terms
+(an empty slot is a mass term, MD_TERM.m:23-28), separable sources and initial conditions.
+``lev`` overrides every dimension's level, as PDE.m:69 (set_levels) does with opts.lev.
+"""
+import numpy as np
+
+from . import grid as _grid
+from .operators import combine_dimensions, div_term, grad_term, mass_term, project_1d, term_matrix
+
+
+class PDE:
+    def __init__(self, name, bounds, lev, terms, sources=(), ic=(), dt_rule=None):
+        self.name = name
+        self.bounds = list(bounds)
+        d = len(self.bounds)
+        self.levels = [int(lev)] * d if np.isscalar(lev) else [int(v) for v in lev]
+        self.terms = [[(sd if sd is not None else [mass_term()]) for sd in t] for t in terms]
+        self.sources = list(sources)
+        self.ic = list(ic)
+        self.dt_rule = dt_rule
+
+    @property
+    def num_dims(self):
+        return len(self.bounds)
+
+    @property
+    def num_terms(self):
+        return len(self.terms)
+
+    def dt(self, cfl):
+        return self.dt_rule(self, cfl)
+
+    def element_table(self, max_lev=None, grid_type="SG"):
+        ml = max_lev if max_lev is not None else max(8, max(self.levels))
+        return _grid.hash_table_sparse_nD(self.levels, ml, grid_type)
+
+    def term_mats(self, deg, construction_level=None):
+        """pde.terms{t}.terms_1D{d}.mat for every term (get_coeff_mats.m:29-50)."""
+        cache = {}
+        out = []
+        for t in self.terms:
+            row = []
+            for d, pts in enumerate(t):
+                lo, hi = self.bounds[d]
+                lev = self.levels[d] if construction_level is None else construction_level
+                key = (d, lev, tuple((p.kind, p.LF, p.bcl, p.bcr, id(p.g)) for p in pts))
+                if key not in cache:
+                    cache[key] = term_matrix(deg, lo, hi, lev, pts)
+                row.append(cache[key])
+            out.append(row)
+        return out
+
+    def _md(self, deg, funcs, idx1d, t):
+        out = np.zeros(idx1d.shape[0] * deg ** self.num_dims)
+        for fs in funcs:
+            vecs = [project_1d(deg, self.levels[d], self.bounds[d][0], self.bounds[d][1], fs[d], t)
+                    for d in range(self.num_dims)]
+            out += combine_dimensions(deg, vecs, fs[-1](t), idx1d)
+        return out
+
+    def source_vector(self, deg, idx1d, t):
+        """source_vector.m / md_eval_function.m (separable sources, no mass solve)."""
+        return self._md(deg, self.sources, idx1d, t)
+
+    def source_parts(self, deg, idx1d):
+        """Spatial parts of the sources (one vector per source) and their time factors,
+        so s(t) = sum_s c_s(t) * v_s can be formed on the device each stage."""
+        vs = []
+        for fs in self.sources:
+            vecs = [project_1d(deg, self.levels[d], self.bounds[d][0], self.bounds[d][1], fs[d], 0.0)
+                    for d in range(self.num_dims)]
+            vs.append(combine_dimensions(deg, vecs, 1.0, idx1d))
+        return vs, [fs[-1] for fs in self.sources]
+
+    def initial_condition(self, deg, idx1d, t=0.0):
+        return self._md(deg, self.ic, idx1d, t)
+
+
+def _neg(v):
+    return lambda x: 0 * x - v
+
+
+def continuity2(lev, LF=-1.0):
+    """pdes/continuity2.m: x in [-1,1], y in [-2,2]; d/dx and d/dy with g=-1, periodic."""
+    pi = np.pi
+    terms = [[[div_term(_neg(1.0), LF, "P", "P")], [mass_term()]], [None, [div_term(_neg(1.0), LF, "P", "P")]]]
+    sources = [
+        [lambda x, t: np.cos(pi * x), lambda y, t: np.sin(2 * pi * y), lambda t: 2 * np.cos(2 * t)],
+        [lambda x, t: np.cos(pi * x), lambda y, t: np.cos(2 * pi * y), lambda t: 2 * pi * np.sin(2 * t)],
+        [lambda x, t: np.sin(pi * x), lambda y, t: np.sin(2 * pi * y), lambda t: -pi * np.sin(2 * t)],
+    ]
+    ic = [[lambda x, t: np.cos(pi * x), lambda y, t: np.sin(2 * pi * y), lambda t: np.sin(2 * t)]]
+    return PDE("continuity2", [(-1.0, 1.0), (-2.0, 2.0)], lev, terms, sources, ic,
+               lambda p, cfl: (p.bounds[0][1] - p.bounds[0][0]) / 2 ** p.levels[0] * cfl)
+
+
+def continuity3(lev, LF=-1.0):
+    """pdes/continuity3.m: [-1,1] x [-2,2] x [-3,3]; one d/dx_k term per dimension, g=-1."""
+    pi = np.pi
+    terms = [[[div_term(_neg(1.0), LF, "P", "P")] if k == d else None for d in range(3)] for k in range(3)]
+    sources = [
+        [lambda x, t: np.cos(pi * x), lambda y, t: np.sin(2 * pi * y), lambda z, t: np.cos(2 * pi * z / 3),
+         lambda t: 2 * np.cos(2 * t)],
+        [lambda x, t: np.cos(pi * x), lambda y, t: np.cos(2 * pi * y), lambda z, t: np.cos(2 * pi * z / 3),
+         lambda t: 2 * pi * np.sin(2 * t)],
+        [lambda x, t: np.sin(pi * x), lambda y, t: np.sin(2 * pi * y), lambda z, t: np.cos(2 * pi * z / 3),
+         lambda t: -pi * np.sin(2 * t)],
+        [lambda x, t: np.cos(pi * x), lambda y, t: np.sin(2 * pi * y), lambda z, t: np.sin(2 * pi * z / 3),
+         lambda t: -2.0 / 3.0 * pi * np.sin(2 * t)],
+    ]
+    ic = [[lambda x, t: 0 * x] * 3 + [lambda t: 1.0]]
+    return PDE("continuity3", [(-1.0, 1.0), (-2.0, 2.0), (-3.0, 3.0)], lev, terms, sources, ic,
+               lambda p, cfl: (p.bounds[0][1] - p.bounds[0][0]) / 2 ** p.levels[0] * cfl)
+
+
+def continuity6(lev, LF=-1.0):
+    """pdes/continuity6.m: six dimensions, d/dx_k with speeds (1,1,3,4,3,2), periodic."""
+    bounds = [(-1.0, 1.0), (-2.0, 2.0), (-3.0, 3.0), (-10.0, 10.0), (-20.0, 20.0), (-30.0, 30.0)]
+    speeds = [1.0, 1.0, 3.0, 4.0, 3.0, 2.0]
+    terms = [[[div_term(_neg(speeds[k]), LF, "P", "P")] if k == d else None for d in range(6)] for k in range(6)]
+    return PDE("continuity6", bounds, lev, terms, (), (),
+               lambda p, cfl: (p.bounds[0][1] - p.bounds[0][0]) / 2 ** p.levels[0] * cfl)
+
+
+def diffusion2(lev):
+    """pdes/diffusion2.m: LDG d2/dx2 + d2/dy2 on [0,1]^2: DIV(+1, N, N) then GRAD(-1, D, D)."""
+    one = lambda x: 0 * x + 1
+    ldg = [div_term(one, 1.0, "N", "N"), grad_term(one, -1.0, "D", "D")]
+    terms = [[ldg, [mass_term(), mass_term()]], [[mass_term(), mass_term()], ldg]]
+    pi = np.pi
+    ic = [[lambda x, t: np.sin(pi * x), lambda y, t: np.sin(pi * y), lambda t: 1.0]]
+    return PDE("diffusion2", [(0.0, 1.0), (0.0, 1.0)], lev, terms, (), ic,
+               lambda p, cfl: cfl * (1.0 / 2 ** p.levels[0]) ** 2)

@@ -1,0 +1,449 @@
+// Operator application y = A*f over the sparse-grid element pairs (apply_A.m:102-236).
+//
+// Row-stationary: a team of threads (one warp, or one CTA for large element blocks) owns an
+// output element i, walks its work entries (column element j, term t), applies the term's
+// Kronecker factors A_{t,m}[I_m(i), J_m(j)] to f_j as a chain of mode products (fastest
+// dimension first, as kronmult{d}.m's method-1 recursion does), and accumulates in
+// registers.  Each y block is written exactly once: no atomics, bitwise deterministic.
+// FP32 accumulation across the column reduction is Kahan-compensated.
+#include <cstdio>
+
+#include "asg_internal.h"
+
+namespace asg {
+namespace {
+
+template <typename T>
+__device__ __forceinline__ void acc_add(T& s, T& c, T v, bool kahan) {
+  if (kahan) {
+    const T yv = v - c;
+    const T t = s + yv;
+    c = (t - s) - yv;
+    s = t;
+  } else {
+    s += v;
+  }
+}
+
+// P contiguous values with the widest aligned vector access the element type allows.
+template <typename T, int P>
+struct Row {
+  T v[P];
+  __device__ __forceinline__ void load(const T* p) {
+#pragma unroll
+    for (int i = 0; i < P; ++i) v[i] = p[i];
+  }
+  __device__ __forceinline__ void store(T* p) const {
+#pragma unroll
+    for (int i = 0; i < P; ++i) p[i] = v[i];
+  }
+};
+template <>
+struct Row<float, 4> {
+  float v[4];
+  __device__ __forceinline__ void load(const float* p) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+  }
+  __device__ __forceinline__ void store(float* p) const {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  }
+};
+template <>
+struct Row<float, 2> {
+  float v[2];
+  __device__ __forceinline__ void load(const float* p) {
+    const float2 q = *reinterpret_cast<const float2*>(p);
+    v[0] = q.x; v[1] = q.y;
+  }
+  __device__ __forceinline__ void store(float* p) const { *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]); }
+};
+template <>
+struct Row<double, 4> {
+  double v[4];
+  __device__ __forceinline__ void load(const double* p) {
+    const double2 a = reinterpret_cast<const double2*>(p)[0];
+    const double2 b = reinterpret_cast<const double2*>(p)[1];
+    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+  }
+  __device__ __forceinline__ void store(double* p) const {
+    reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
+    reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
+  }
+};
+template <>
+struct Row<double, 2> {
+  double v[2];
+  __device__ __forceinline__ void load(const double* p) {
+    const double2 a = *reinterpret_cast<const double2*>(p);
+    v[0] = a.x; v[1] = a.y;
+  }
+  __device__ __forceinline__ void store(double* p) const { *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]); }
+};
+
+// Cooperative copy of n values (16-byte vectors when both ends allow it).
+template <typename T>
+__device__ __forceinline__ void team_copy(T* dst, const T* src, int n, int rank, int size) {
+  constexpr int V = 16 / sizeof(T);
+  if ((n % V) == 0 && ((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0) {
+    const int4* s4 = reinterpret_cast<const int4*>(src);
+    int4* d4 = reinterpret_cast<int4*>(dst);
+    for (int k = rank; k < n / V; k += size) d4[k] = s4[k];
+  } else {
+    for (int k = rank; k < n; k += size) dst[k] = src[k];
+  }
+}
+
+// One mode product of the chain on an element block held in shared memory:
+// out[.., a, ..] = sum_b A[a][b] * in[.., b, ..] along dimension m (stride s).
+template <typename T, int P>
+__device__ __forceinline__ void mode_pass(const T* __restrict__ in, T* __restrict__ out, const T* A, int B, int s,
+                                          int rank, int size) {
+  const int nf = B / P;
+  for (int fi = rank; fi < nf; fi += size) {
+    const int hi = fi / s;
+    const int lo = fi - hi * s;
+    const int base = hi * s * P + lo;
+    T x[P];
+#pragma unroll
+    for (int b = 0; b < P; ++b) x[b] = in[base + b * s];
+#pragma unroll
+    for (int a = 0; a < P; ++a) {
+      T sum = A[a * P] * x[0];
+#pragma unroll
+      for (int b = 1; b < P; ++b) sum = fma(A[a * P + b], x[b], sum);
+      out[base + a * s] = sum;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Chain kernel, one warp per output element (element blocks of at most 256 values).
+// ---------------------------------------------------------------------------------------
+template <typename T, int P, bool KAHAN>
+__global__ void __launch_bounds__(128) k_chain_warp(ApplyArgs<T> a) {
+  constexpr int MAXE = 8;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int wpb = blockDim.x >> 5;
+  const int B = a.B, D = a.D;
+  const int Bpad = (B + 3) & ~3;
+  T* buf0 = reinterpret_cast<T*>(smem_raw) + static_cast<size_t>(warp) * 2 * Bpad;
+  T* buf1 = buf0 + Bpad;
+  for (int row = blockIdx.x * wpb + warp; row < a.N; row += gridDim.x * wpb) {
+    T acc[MAXE], cmp[MAXE];
+#pragma unroll
+    for (int k = 0; k < MAXE; ++k) acc[k] = cmp[k] = T(0);
+    int ii[kMaxDims];
+    for (int m = 0; m < D; ++m) ii[m] = a.idx1d[row * D + m];
+    const long long q1 = a.row_ptr[row + 1];
+    for (long long q = a.row_ptr[row]; q < q1; ++q) {
+      const int e = a.ent[q];
+      const int j = e >> 4;
+      const int t = e & 15;
+      const unsigned act = a.active[t];
+      team_copy(buf0, a.f + static_cast<size_t>(j) * B, B, lane, 32);
+      __syncwarp();
+      T* in = buf0;
+      T* out = buf1;
+      for (int m = D - 1; m >= 0; --m) {
+        if (!((act >> m) & 1u)) continue;
+        const int tm = t * D + m;
+        const T* Ag = a.ops + a.op_off[tm] +
+                      (static_cast<long long>(ii[m]) * a.op_nb[tm] + a.idx1d[j * D + m]) * (P * P);
+        T A[P * P];
+#pragma unroll
+        for (int r = 0; r < P * P; ++r) A[r] = Ag[r];
+        mode_pass<T, P>(in, out, A, B, a.stride[m], lane, 32);
+        __syncwarp();
+        T* tmp = in;
+        in = out;
+        out = tmp;
+      }
+#pragma unroll
+      for (int k = 0; k < MAXE; ++k) {
+        const int idx = lane + 32 * k;
+        if (idx < B) acc_add(acc[k], cmp[k], in[idx], KAHAN);
+      }
+      __syncwarp();
+    }
+    T* yr = a.y + static_cast<size_t>(row) * B;
+#pragma unroll
+    for (int k = 0; k < MAXE; ++k) {
+      const int idx = lane + 32 * k;
+      if (idx < B) yr[idx] = acc[k];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Chain kernel, one CTA per output element (element blocks up to 4096 values).
+// ---------------------------------------------------------------------------------------
+template <typename T, int P, bool KAHAN, int NT>
+__global__ void __launch_bounds__(NT) k_chain_cta(ApplyArgs<T> a) {
+  constexpr int MAXE = kMaxBlock / NT;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int tid = threadIdx.x;
+  const int B = a.B, D = a.D;
+  const int Bpad = (B + 3) & ~3;
+  T* buf0 = reinterpret_cast<T*>(smem_raw);
+  T* buf1 = buf0 + Bpad;
+  T* blk = buf1 + Bpad;  // D*P*P operator blocks of the current entry
+  for (int row = blockIdx.x; row < a.N; row += gridDim.x) {
+    T acc[MAXE], cmp[MAXE];
+#pragma unroll
+    for (int k = 0; k < MAXE; ++k) acc[k] = cmp[k] = T(0);
+    const long long q1 = a.row_ptr[row + 1];
+    for (long long q = a.row_ptr[row]; q < q1; ++q) {
+      const int e = a.ent[q];
+      const int j = e >> 4;
+      const int t = e & 15;
+      const unsigned act = a.active[t];
+      team_copy(buf0, a.f + static_cast<size_t>(j) * B, B, tid, NT);
+      for (int idx = tid; idx < D * P * P; idx += NT) {
+        const int m = idx / (P * P);
+        if ((act >> m) & 1u) {
+          const int tm = t * D + m;
+          blk[idx] = a.ops[a.op_off[tm] +
+                           (static_cast<long long>(a.idx1d[row * D + m]) * a.op_nb[tm] + a.idx1d[j * D + m]) * (P * P) +
+                           (idx - m * P * P)];
+        }
+      }
+      __syncthreads();
+      T* in = buf0;
+      T* out = buf1;
+      for (int m = D - 1; m >= 0; --m) {
+        if (!((act >> m) & 1u)) continue;
+        T A[P * P];
+#pragma unroll
+        for (int r = 0; r < P * P; ++r) A[r] = blk[m * P * P + r];
+        mode_pass<T, P>(in, out, A, B, a.stride[m], tid, NT);
+        __syncthreads();
+        T* tmp = in;
+        in = out;
+        out = tmp;
+      }
+#pragma unroll
+      for (int k = 0; k < MAXE; ++k) {
+        const int idx = tid + NT * k;
+        if (idx < B) acc_add(acc[k], cmp[k], in[idx], KAHAN);
+      }
+      __syncthreads();
+    }
+    T* yr = a.y + static_cast<size_t>(row) * B;
+#pragma unroll
+    for (int k = 0; k < MAXE; ++k) {
+      const int idx = tid + NT * k;
+      if (idx < B) yr[idx] = acc[k];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------
+// Single-mode fiber kernel.  Used when every term has exactly one non-identity factor
+// (I x .. x D_k x .. x I, the shape of every advection/diffusion term once the mass
+// factors are the identity) and the block is large (deg^d >= 32*deg^2).
+//
+// The CTA has B/P^2 threads; thread t owns the P x P output tile over dimensions (d-2, d-1)
+// starting at t*P^2 (its "natural" tile).  Entries of a row are sorted by term.  For a term
+// acting on dimension m the thread reads, straight from global memory, the P fibers along m
+// that hit a P x P tile over (m, d-1) and contracts them with the P x P block in registers:
+// 4-wide vector loads, P^3 FMAs per tile.  Terms on dimensions d-2 and d-1 land directly on
+// the natural tile; the others are summed per term and moved to the natural tile through
+// one shared-memory transpose.
+// ---------------------------------------------------------------------------------------
+template <typename T, int P, bool KAHAN>
+__global__ void __launch_bounds__(256) k_single_mode(ApplyArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* scratch = reinterpret_cast<T*>(smem_raw);  // B values
+  const int tid = threadIdx.x;
+  const int B = a.B, D = a.D;
+  const int row = blockIdx.x;
+  if (row >= a.N) return;
+  T nat[P][P], natc[P][P], g[P][P], gc[P][P];
+#pragma unroll
+  for (int r = 0; r < P; ++r)
+#pragma unroll
+    for (int c = 0; c < P; ++c) nat[r][c] = natc[r][c] = g[r][c] = gc[r][c] = T(0);
+
+  int cur_m = -1;
+  int base_g = 0, s_g = 0;
+  const long long q0 = a.row_ptr[row], q1 = a.row_ptr[row + 1];
+  for (long long q = q0; q <= q1; ++q) {
+    int m = -1, j = 0, t = 0;
+    if (q < q1) {
+      const int e = a.ent[q];
+      j = e >> 4;
+      t = e & 15;
+      m = __ffs(a.active[t]) - 1;
+    }
+    if (m != cur_m) {
+      if (cur_m >= 0 && cur_m < D - 2) {
+        // flush the per-term sum through shared memory onto the natural tiles
+#pragma unroll
+        for (int r = 0; r < P; ++r) {
+          Row<T, P> rr;
+#pragma unroll
+          for (int c = 0; c < P; ++c) rr.v[c] = g[r][c];
+          rr.store(scratch + base_g + r * s_g);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < P; ++r) {
+          Row<T, P> rr;
+          rr.load(scratch + tid * P * P + r * P);
+#pragma unroll
+          for (int c = 0; c < P; ++c) acc_add(nat[r][c], natc[r][c], rr.v[c], KAHAN);
+        }
+        __syncthreads();
+      }
+      cur_m = m;
+    }
+    if (m < 0) break;
+    {
+#pragma unroll
+      for (int r = 0; r < P; ++r)
+#pragma unroll
+        for (int c = 0; c < P; ++c) g[r][c] = gc[r][c] = T(0);
+      if (m < D - 1) {
+        int pw = 1;
+        for (int k = 0; k < D - 2 - m; ++k) pw *= P;
+        const int lo = tid % pw, hi = tid / pw;
+        s_g = a.stride[m];
+        base_g = hi * s_g * P + lo * P;
+      } else {
+        s_g = P;
+        base_g = tid * P * P;
+      }
+    }
+    // P x P block of operator (t, m) at (I_m(row), J_m(j))
+    const int tm = t * D + m;
+    const T* Ag = a.ops + a.op_off[tm] +
+                  (static_cast<long long>(a.idx1d[row * D + m]) * a.op_nb[tm] + a.idx1d[j * D + m]) * (P * P);
+    T A[P][P];
+#pragma unroll
+    for (int r = 0; r < P; ++r) {
+      Row<T, P> rr;
+      rr.load(Ag + r * P);
+#pragma unroll
+      for (int c = 0; c < P; ++c) A[r][c] = rr.v[c];
+    }
+    const T* fj = a.f + static_cast<size_t>(j) * B + base_g;
+    T x[P][P];
+#pragma unroll
+    for (int r = 0; r < P; ++r) {
+      Row<T, P> rr;
+      rr.load(fj + r * s_g);
+#pragma unroll
+      for (int c = 0; c < P; ++c) x[r][c] = rr.v[c];
+    }
+    if (m == D - 1) {
+      // contraction along the contiguous index: out[r][a] = sum_b A[a][b] x[r][b]
+#pragma unroll
+      for (int r = 0; r < P; ++r)
+#pragma unroll
+        for (int aa = 0; aa < P; ++aa) {
+          T s = A[aa][0] * x[r][0];
+#pragma unroll
+          for (int b = 1; b < P; ++b) s = fma(A[aa][b], x[r][b], s);
+          acc_add(nat[r][aa], natc[r][aa], s, KAHAN);
+        }
+    } else {
+      // contraction across rows: out[a][c] = sum_b A[a][b] x[b][c]
+#pragma unroll
+      for (int aa = 0; aa < P; ++aa)
+#pragma unroll
+        for (int c = 0; c < P; ++c) {
+          T s = A[aa][0] * x[0][c];
+#pragma unroll
+          for (int b = 1; b < P; ++b) s = fma(A[aa][b], x[b][c], s);
+          if (m == D - 2)
+            acc_add(nat[aa][c], natc[aa][c], s, KAHAN);
+          else
+            acc_add(g[aa][c], gc[aa][c], s, KAHAN);
+        }
+    }
+  }
+  T* yr = a.y + static_cast<size_t>(row) * B + tid * P * P;
+#pragma unroll
+  for (int r = 0; r < P; ++r) {
+    Row<T, P> rr;
+#pragma unroll
+    for (int c = 0; c < P; ++c) rr.v[c] = nat[r][c];
+    rr.store(yr + r * P);
+  }
+}
+
+// Opt a kernel into more than 48 KB of dynamic shared memory (once per instantiation; the
+// limit set is the largest this kernel can request, so later plans need no new call).
+template <typename K>
+cudaError_t ensure_smem(K kernel, size_t bytes, size_t max_bytes, bool& done) {
+  if (bytes <= 48 * 1024 || done) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(max_bytes));
+  if (e == cudaSuccess) done = true;
+  return e;
+}
+
+template <typename T, int P>
+cudaError_t launch_p(const ApplyArgs<T>& a, int kind, cudaStream_t s) {
+  constexpr bool K = sizeof(T) == 4;
+  const int Bpad = (a.B + 3) & ~3;
+  if (kind == KK_CHAIN_WARP) {
+    const int wpb = 4;
+    const size_t sm = static_cast<size_t>(wpb) * 2 * Bpad * sizeof(T);
+    auto kern = k_chain_warp<T, P, K>;
+    static bool done = false;
+    cudaError_t e = ensure_smem(kern, sm, static_cast<size_t>(wpb) * 2 * 256 * sizeof(T), done);
+    if (e != cudaSuccess) return e;
+    const int grid = (a.N + wpb - 1) / wpb;
+    kern<<<grid, wpb * 32, sm, s>>>(a);
+    return cudaGetLastError();
+  }
+  if (kind == KK_CHAIN_CTA) {
+    constexpr int NT = 256;
+    const size_t sm = (static_cast<size_t>(2) * Bpad + a.D * P * P) * sizeof(T);
+    auto kern = k_chain_cta<T, P, K, NT>;
+    static bool done = false;
+    cudaError_t e = ensure_smem(kern, sm, (static_cast<size_t>(2) * kMaxBlock + kMaxDims * P * P) * sizeof(T), done);
+    if (e != cudaSuccess) return e;
+    kern<<<a.N, NT, sm, s>>>(a);
+    return cudaGetLastError();
+  }
+  if constexpr (P == 3 || P == 4) {
+    if (kind == KK_SINGLE_MODE) {
+      const int nt = a.B / (P * P);
+      const size_t sm = static_cast<size_t>(a.B) * sizeof(T);
+      auto kern = k_single_mode<T, P, K>;
+      static bool done = false;
+      cudaError_t e = ensure_smem(kern, sm, static_cast<size_t>(kMaxBlock) * sizeof(T), done);
+      if (e != cudaSuccess) return e;
+      kern<<<a.N, nt, sm, s>>>(a);
+      return cudaGetLastError();
+    }
+  }
+  return cudaErrorInvalidValue;
+}
+
+}  // namespace
+
+template <typename T>
+cudaError_t launch_apply(const ApplyArgs<T>& a, int P, int kind, cudaStream_t s) {
+  if (a.N == 0) return cudaSuccess;
+  switch (P) {
+    case 1: return launch_p<T, 1>(a, kind, s);
+    case 2: return launch_p<T, 2>(a, kind, s);
+    case 3: return launch_p<T, 3>(a, kind, s);
+    case 4: return launch_p<T, 4>(a, kind, s);
+    case 5: return launch_p<T, 5>(a, kind, s);
+    case 6: return launch_p<T, 6>(a, kind, s);
+    case 7: return launch_p<T, 7>(a, kind, s);
+    case 8: return launch_p<T, 8>(a, kind, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template cudaError_t launch_apply<double>(const ApplyArgs<double>&, int, int, cudaStream_t);
+template cudaError_t launch_apply<float>(const ApplyArgs<float>&, int, int, cudaStream_t);
+
+}  // namespace asg

@@ -1,0 +1,86 @@
+// Internal declarations shared by the asgkron translation units (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "asgkron.h"
+
+namespace asg {
+
+constexpr int kMaxDims = 6;    // kron_multd.m dispatches d<=6 to kronmult{d}; larger d is rejected
+constexpr int kMaxTerms = 16;  // work entries pack the term id into 4 bits
+constexpr int kMaxBlock = 4096;  // deg^d of one element block handled on chip
+
+// Records a message for asg_last_error() and returns the status.
+asg_status fail(asg_status st, const char* fmt, ...);
+asg_status cuda_fail(cudaError_t e, const char* what);
+
+#define ASG_CUDA(call)                                   \
+  do {                                                   \
+    cudaError_t _e = (call);                             \
+    if (_e != cudaSuccess) return ::asg::cuda_fail(_e, #call); \
+  } while (0)
+
+// Arguments of the operator-application kernels.  One work entry is one
+// (column element, term) product contributing to a row element; entries of a row are
+// contiguous (CSR by row), packed as (col << 4) | term.
+template <typename T>
+struct ApplyArgs {
+  const T* f;
+  T* y;
+  const T* ops;              // block-major packed 1-D operators
+  const long long* op_off;   // [T*D] element offset of packed operator (t,d); -1 when not packed
+  const int* op_nb;          // [T*D] 1-D blocks per side of packed operator (t,d)
+  const int* idx1d;          // [N*D] 0-based 1-D index of each element per dimension
+  const long long* row_ptr;  // [N+1]
+  const int* ent;            // packed entries
+  const unsigned* active;    // [T] bit m set <=> operator (t,m) is applied (else identity)
+  int N, D, B, nterms;
+  int stride[kMaxDims];      // deg^(D-1-m): element-block stride of dimension m
+};
+
+template <typename T>
+cudaError_t launch_apply(const ApplyArgs<T>& a, int P, int kernel_kind, cudaStream_t s);
+
+enum KernelKind { KK_CHAIN_WARP = 0, KK_CHAIN_CTA = 1, KK_SINGLE_MODE = 2 };
+
+}  // namespace asg
+
+// The plan object behind the opaque C handle.
+struct asg_plan {
+  int D = 0, P = 0, T = 0, N = 0, B = 0;
+  int structure = 0;
+  double drop_tol = 0.0;
+  int kernel_kind = 0;
+  // host-side metadata
+  std::vector<int> idx1d;            // N*D, 0-based
+  std::vector<int> op_nb;            // T*D
+  std::vector<unsigned> active;      // T
+  std::vector<long long> op_off;     // T*D
+  std::vector<long long> row_ptr;    // N+1
+  std::vector<int> ent;              // entries
+  std::vector<long long> tr_row_ptr; // transposed work list (by column) for the adjoint
+  std::vector<int> tr_ent;           // packed (row << 4) | term
+  long long packed_elems = 0;
+  long long pairs = 0;
+  double flops_dense = 0, flops_exec = 0;
+  // device-side copies
+  int* d_idx1d = nullptr;
+  int* d_op_nb = nullptr;
+  unsigned* d_active = nullptr;
+  long long* d_op_off = nullptr;
+  long long* d_row_ptr = nullptr;
+  int* d_ent = nullptr;
+  long long* d_tr_row_ptr = nullptr;
+  int* d_tr_ent = nullptr;
+  double* d_ops64 = nullptr;
+  float* d_ops32 = nullptr;
+  // host-pointer apply path (staging owned by the plan)
+  void* d_io = nullptr;
+  size_t d_io_bytes = 0;
+  cudaStream_t stream = nullptr;
+};

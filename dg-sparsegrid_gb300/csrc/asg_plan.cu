@@ -1,0 +1,427 @@
+// Plan creation, structure analysis, work-list construction and the apply entry points of
+// the C ABI.  Host-side code (compiled by nvcc for the runtime API); the kernels live in
+// asg_apply.cu.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <new>
+#include <vector>
+
+#include "asg_internal.h"
+
+namespace asg {
+
+static thread_local char g_err[1024] = "";
+
+asg_status fail(asg_status st, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return st;
+}
+
+asg_status cuda_fail(cudaError_t e, const char* what) {
+  return fail(ASG_ERR_CUDA, "%s: %s (%s)", what, cudaGetErrorName(e), cudaGetErrorString(e));
+}
+
+namespace {
+
+template <typename X>
+asg_status upload(X** dst, const std::vector<X>& src) {
+  if (src.empty()) return ASG_OK;
+  ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(dst), src.size() * sizeof(X)));
+  ASG_CUDA(cudaMemcpy(*dst, src.data(), src.size() * sizeof(X), cudaMemcpyHostToDevice));
+  return ASG_OK;
+}
+
+void free_device(asg_plan* p) {
+  cudaFree(p->d_idx1d);
+  cudaFree(p->d_op_nb);
+  cudaFree(p->d_active);
+  cudaFree(p->d_op_off);
+  cudaFree(p->d_row_ptr);
+  cudaFree(p->d_ent);
+  cudaFree(p->d_tr_row_ptr);
+  cudaFree(p->d_tr_ent);
+  cudaFree(p->d_ops64);
+  cudaFree(p->d_ops32);
+  cudaFree(p->d_io);
+  if (p->stream) cudaStreamDestroy(p->stream);
+}
+
+// Pack operator (t,m) into block-major order: block (a,b) holds the P x P sub-matrix
+// rows a*P.., cols b*P.. row-major, so one (row, column) element pair reads P*P
+// contiguous values.
+void pack_op(const double* op, int ld, int nb, int P, double* dst) {
+  for (int a = 0; a < nb; ++a)
+    for (int b = 0; b < nb; ++b) {
+      double* blk = dst + (static_cast<long long>(a) * nb + b) * P * P;
+      for (int r = 0; r < P; ++r)
+        for (int c = 0; c < P; ++c)
+          blk[r * P + c] = op[static_cast<long long>(b * P + c) * ld + (a * P + r)];
+    }
+}
+
+asg_status pack_and_upload(asg_plan* p, const double* const* ops, const int* op_ld) {
+  std::vector<double> h64(static_cast<size_t>(p->packed_elems));
+  for (int t = 0; t < p->T; ++t)
+    for (int m = 0; m < p->D; ++m) {
+      const int tm = t * p->D + m;
+      if (p->op_off[tm] < 0) continue;
+      pack_op(ops[tm], op_ld[tm], p->op_nb[tm], p->P, h64.data() + p->op_off[tm]);
+    }
+  std::vector<float> h32(h64.size());
+  for (size_t i = 0; i < h64.size(); ++i) h32[i] = static_cast<float>(h64[i]);
+  if (!p->d_ops64 && !h64.empty()) {
+    ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_ops64), h64.size() * sizeof(double)));
+    ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_ops32), h32.size() * sizeof(float)));
+  }
+  if (!h64.empty()) {
+    ASG_CUDA(cudaMemcpy(p->d_ops64, h64.data(), h64.size() * sizeof(double), cudaMemcpyHostToDevice));
+    ASG_CUDA(cudaMemcpy(p->d_ops32, h32.data(), h32.size() * sizeof(float), cudaMemcpyHostToDevice));
+  }
+  return ASG_OK;
+}
+
+template <typename T>
+ApplyArgs<T> make_args(const asg_plan* p, const T* f, T* y, const T* ops) {
+  ApplyArgs<T> a{};
+  a.f = f;
+  a.y = y;
+  a.ops = ops;
+  a.op_off = p->d_op_off;
+  a.op_nb = p->d_op_nb;
+  a.idx1d = p->d_idx1d;
+  a.row_ptr = p->d_row_ptr;
+  a.ent = p->d_ent;
+  a.active = p->d_active;
+  a.N = p->N;
+  a.D = p->D;
+  a.B = p->B;
+  a.nterms = p->T;
+  int s = 1;
+  for (int m = p->D - 1; m >= 0; --m) {
+    a.stride[m] = s;
+    s *= p->P;
+  }
+  return a;
+}
+
+asg_status check_ptr(const void* ptr, const char* name) {
+  if (!ptr) return fail(ASG_ERR_INVALID, "%s is NULL", name);
+  if (reinterpret_cast<uintptr_t>(ptr) & 15) return fail(ASG_ERR_INVALID, "%s must be 16-byte aligned", name);
+  return ASG_OK;
+}
+
+template <typename T>
+asg_status apply_dev(asg_plan* p, const T* f, T* y, void* stream) {
+  if (!p) return fail(ASG_ERR_INVALID, "apply: NULL plan");
+  asg_status st = check_ptr(f, "f");
+  if (st) return st;
+  st = check_ptr(y, "y");
+  if (st) return st;
+  if (f == y) return fail(ASG_ERR_INVALID, "apply: f and y must not alias");
+  const T* ops = sizeof(T) == 8 ? reinterpret_cast<const T*>(p->d_ops64) : reinterpret_cast<const T*>(p->d_ops32);
+  ApplyArgs<T> a = make_args<T>(p, f, y, ops);
+  cudaError_t e = launch_apply<T>(a, p->P, p->kernel_kind, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "apply kernel launch");
+  return ASG_OK;
+}
+
+template <typename T>
+asg_status apply_host(asg_plan* p, const T* hf, T* hy) {
+  if (!p) return fail(ASG_ERR_INVALID, "apply_host: NULL plan");
+  if (!hf || !hy) return fail(ASG_ERR_INVALID, "apply_host: NULL host buffer");
+  const size_t n = static_cast<size_t>(p->N) * p->B;
+  const size_t need = 2 * n * sizeof(T) + 256;
+  if (!p->stream) ASG_CUDA(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+  if (p->d_io_bytes < need) {
+    cudaFree(p->d_io);
+    p->d_io = nullptr;
+    p->d_io_bytes = 0;
+    ASG_CUDA(cudaMalloc(&p->d_io, need));
+    p->d_io_bytes = need;
+  }
+  T* df = static_cast<T*>(p->d_io);
+  T* dy = reinterpret_cast<T*>(reinterpret_cast<char*>(p->d_io) + ((n * sizeof(T) + 255) / 256) * 256);
+  ASG_CUDA(cudaMemcpyAsync(df, hf, n * sizeof(T), cudaMemcpyHostToDevice, p->stream));
+  asg_status st = apply_dev<T>(p, df, dy, p->stream);
+  if (st) return st;
+  ASG_CUDA(cudaMemcpyAsync(hy, dy, n * sizeof(T), cudaMemcpyDeviceToHost, p->stream));
+  ASG_CUDA(cudaStreamSynchronize(p->stream));
+  return ASG_OK;
+}
+
+}  // namespace
+}  // namespace asg
+
+using asg::fail;
+
+extern "C" {
+
+const char* asg_version(void) { return "asgkron 0.1 (sm_103a)"; }
+
+asg_status asg_last_error(char* buf, size_t len) {
+  if (!buf || len == 0) return ASG_ERR_INVALID;
+  snprintf(buf, len, "%s", asg::g_err);
+  return ASG_OK;
+}
+
+asg_status asg_plan_create(const asg_plan_desc* desc, asg_plan** out) {
+  if (!desc || !out) return fail(ASG_ERR_INVALID, "plan_create: NULL argument");
+  *out = nullptr;
+  const int D = desc->num_dims, P = desc->deg, T = desc->num_terms, N = desc->num_elems;
+  if (D < 1 || D > asg::kMaxDims)
+    return fail(D < 1 ? ASG_ERR_INVALID : ASG_ERR_UNSUPPORTED, "kron_multd: invalid nkron=%d (1..%d supported)", D,
+                asg::kMaxDims);
+  if (P < 1 || P > 8) return fail(P < 1 ? ASG_ERR_INVALID : ASG_ERR_UNSUPPORTED, "deg=%d outside 1..8", P);
+  if (T < 1 || T > asg::kMaxTerms)
+    return fail(T < 1 ? ASG_ERR_INVALID : ASG_ERR_UNSUPPORTED, "num_terms=%d outside 1..%d", T, asg::kMaxTerms);
+  if (N < 0 || N >= (1 << 27)) return fail(ASG_ERR_UNSUPPORTED, "num_elems=%d outside 0..2^27-1", N);
+  long long B = 1;
+  for (int k = 0; k < D; ++k) B *= P;
+  if (B > asg::kMaxBlock) return fail(ASG_ERR_UNSUPPORTED, "deg^d=%lld exceeds %d", B, asg::kMaxBlock);
+  if (desc->index_base != 0 && desc->index_base != 1) return fail(ASG_ERR_INVALID, "index_base must be 0 or 1");
+  if (desc->structure != ASG_STRUCT_NONE && desc->structure != ASG_STRUCT_DETECT)
+    return fail(ASG_ERR_INVALID, "unknown structure mode %d", desc->structure);
+  if (!(desc->drop_tol >= 0.0) || desc->drop_tol > 1e-3) return fail(ASG_ERR_INVALID, "drop_tol must be in [0, 1e-3]");
+  if (N > 0 && (!desc->idx1d || !desc->ops || !desc->op_ld)) return fail(ASG_ERR_INVALID, "plan_create: NULL array");
+  const int base = desc->index_base;
+
+  asg_plan* p = new (std::nothrow) asg_plan;
+  if (!p) return fail(ASG_ERR_NOMEM, "plan_create: out of host memory");
+  p->D = D;
+  p->P = P;
+  p->T = T;
+  p->N = N;
+  p->B = static_cast<int>(B);
+  p->structure = desc->structure;
+  p->drop_tol = desc->drop_tol;
+
+  auto bail = [&](asg_status st) {
+    asg::free_device(p);
+    delete p;
+    return st;
+  };
+
+  // ---- 1-D indices ------------------------------------------------------------------
+  p->idx1d.resize(static_cast<size_t>(N) * D);
+  std::vector<int> nb_dim(D, 0);
+  for (long long i = 0; i < static_cast<long long>(N) * D; ++i) {
+    const int v = desc->idx1d[i] - base;
+    if (v < 0) return bail(fail(ASG_ERR_INVALID, "idx1d[%lld]=%d below index base %d", i, desc->idx1d[i], base));
+    p->idx1d[i] = v;
+    nb_dim[i % D] = std::max(nb_dim[i % D], v + 1);
+  }
+  // ---- operators: validate, analyse structure ----------------------------------------
+  p->op_nb.assign(static_cast<size_t>(T) * D, 0);
+  p->op_off.assign(static_cast<size_t>(T) * D, -1);
+  p->active.assign(T, 0u);
+  std::vector<std::vector<uint8_t>> zero_blk(static_cast<size_t>(T) * D);
+  const bool detect = desc->structure == ASG_STRUCT_DETECT;
+  for (int t = 0; t < T; ++t)
+    for (int m = 0; m < D; ++m) {
+      const int tm = t * D + m;
+      const int nb = nb_dim[m];
+      p->op_nb[tm] = nb;
+      if (N == 0) continue;
+      const double* op = desc->ops[tm];
+      const int ld = desc->op_ld[tm];
+      if (!op) return bail(fail(ASG_ERR_INVALID, "operator (term %d, dim %d) is NULL", t, m));
+      if (ld < nb * P)
+        return bail(fail(ASG_ERR_INVALID, "operator (term %d, dim %d): ld=%d < deg*max(idx1d)=%d", t, m, ld, nb * P));
+      const int n = nb * P;
+      double maxabs = 0.0;
+      for (int c = 0; c < n; ++c)
+        for (int r = 0; r < n; ++r) {
+          const double v = op[static_cast<long long>(c) * ld + r];
+          if (!std::isfinite(v))
+            return bail(fail(ASG_ERR_INVALID, "operator (term %d, dim %d) has a non-finite entry at (%d,%d)", t, m, r, c));
+          maxabs = std::max(maxabs, std::fabs(v));
+        }
+      bool ident = false;
+      if (detect) {
+        const double thr = desc->drop_tol * maxabs;
+        ident = true;
+        for (int c = 0; c < n && ident; ++c)
+          for (int r = 0; r < n; ++r)
+            if (std::fabs(op[static_cast<long long>(c) * ld + r] - (r == c ? 1.0 : 0.0)) > thr) {
+              ident = false;
+              break;
+            }
+        if (!ident) {
+          auto& zb = zero_blk[tm];
+          zb.assign(static_cast<size_t>(nb) * nb, 1);
+          for (int c = 0; c < n; ++c)
+            for (int r = 0; r < n; ++r)
+              if (std::fabs(op[static_cast<long long>(c) * ld + r]) > thr) zb[static_cast<size_t>(r / P) * nb + c / P] = 0;
+        }
+      }
+      if (!ident) p->active[t] |= 1u << m;
+    }
+  // ---- pair list ----------------------------------------------------------------------
+  const bool all_pairs = desc->row_ptr == nullptr;
+  if (!all_pairs) {
+    if (desc->row_ptr[0] != 0) return bail(fail(ASG_ERR_INVALID, "row_ptr[0] must be 0"));
+    for (int i = 0; i < N; ++i)
+      if (desc->row_ptr[i + 1] < desc->row_ptr[i]) return bail(fail(ASG_ERR_INVALID, "row_ptr not monotone at %d", i));
+    if (desc->row_ptr[N] > 0 && !desc->cols) return bail(fail(ASG_ERR_INVALID, "cols is NULL"));
+    for (long long q = 0; q < desc->row_ptr[N]; ++q) {
+      const int j = desc->cols[q] - base;
+      if (j < 0 || j >= N) return bail(fail(ASG_ERR_INVALID, "cols[%lld]=%d outside the element table", q, desc->cols[q]));
+    }
+    p->pairs = desc->row_ptr[N];
+  } else {
+    p->pairs = static_cast<long long>(N) * N;
+  }
+  // ---- work entries ---------------------------------------------------------------------
+  p->row_ptr.assign(N + 1, 0);
+  std::vector<int>& ent = p->ent;
+  auto blk_zero = [&](int t, int m, int i, int j) {
+    const auto& zb = zero_blk[t * D + m];
+    return !zb.empty() && zb[static_cast<size_t>(p->idx1d[i * D + m]) * p->op_nb[t * D + m] + p->idx1d[j * D + m]];
+  };
+  auto keep = [&](int t, int i, int j) {
+    for (int m = 0; m < D; ++m) {
+      if ((p->active[t] >> m) & 1u) {
+        if (blk_zero(t, m, i, j)) return false;
+      } else if (p->idx1d[i * D + m] != p->idx1d[j * D + m]) {
+        return false;
+      }
+    }
+    return true;
+  };
+  if (!detect) {
+    for (int t = 0; t < T; ++t) p->active[t] = (1u << D) - 1u;
+    for (int i = 0; i < N; ++i) {
+      const long long q0 = all_pairs ? 0 : desc->row_ptr[i];
+      const long long q1 = all_pairs ? N : desc->row_ptr[i + 1];
+      for (long long q = q0; q < q1; ++q) {
+        const int j = all_pairs ? static_cast<int>(q) : desc->cols[q] - base;
+        for (int t = 0; t < T; ++t) ent.push_back((j << 4) | t);
+      }
+      p->row_ptr[i + 1] = static_cast<long long>(ent.size());
+    }
+  } else {
+    // group candidate columns by the 1-D indices of the term's identity dimensions
+    std::vector<std::map<std::vector<int>, std::vector<int>>> groups(T);
+    if (all_pairs) {
+      for (int t = 0; t < T; ++t)
+        for (int e = 0; e < N; ++e) {
+          std::vector<int> key;
+          for (int m = 0; m < D; ++m)
+            if (!((p->active[t] >> m) & 1u)) key.push_back(p->idx1d[e * D + m]);
+          groups[t][key].push_back(e);
+        }
+    }
+    for (int i = 0; i < N; ++i) {
+      for (int t = 0; t < T; ++t) {
+        if (all_pairs) {
+          std::vector<int> key;
+          for (int m = 0; m < D; ++m)
+            if (!((p->active[t] >> m) & 1u)) key.push_back(p->idx1d[i * D + m]);
+          for (int j : groups[t][key])
+            if (keep(t, i, j)) ent.push_back((j << 4) | t);
+        } else {
+          for (long long q = desc->row_ptr[i]; q < desc->row_ptr[i + 1]; ++q) {
+            const int j = desc->cols[q] - base;
+            if (keep(t, i, j)) ent.push_back((j << 4) | t);
+          }
+        }
+      }
+      p->row_ptr[i + 1] = static_cast<long long>(ent.size());
+    }
+  }
+  // ---- flop model and kernel choice --------------------------------------------------
+  double pd1 = 1.0;
+  for (int k = 0; k <= D; ++k) pd1 *= P;
+  p->flops_dense = static_cast<double>(p->pairs) * T * D * 2.0 * pd1;
+  p->flops_exec = 0.0;
+  int amax = 0;
+  for (int i = 0; i < N; ++i)
+    for (long long q = p->row_ptr[i]; q < p->row_ptr[i + 1]; ++q)
+      p->flops_exec += 2.0 * pd1 * __builtin_popcount(p->active[ent[q] & 15]);
+  bool single = detect && (P == 3 || P == 4) && B >= 32LL * P * P;
+  for (int t = 0; t < T; ++t) {
+    const int na = __builtin_popcount(p->active[t]);
+    amax = std::max(amax, na);
+    if (na != 1) single = false;
+  }
+  p->kernel_kind = single ? asg::KK_SINGLE_MODE : (B <= 256 ? asg::KK_CHAIN_WARP : asg::KK_CHAIN_CTA);
+  // ---- pack operators -------------------------------------------------------------
+  long long off = 0;
+  for (int t = 0; t < T; ++t)
+    for (int m = 0; m < D; ++m) {
+      const int tm = t * D + m;
+      if (N == 0 || !((p->active[t] >> m) & 1u)) continue;
+      p->op_off[tm] = off;
+      off += static_cast<long long>(p->op_nb[tm]) * p->op_nb[tm] * P * P;
+    }
+  p->packed_elems = off;
+  asg_status st;
+  if ((st = asg::pack_and_upload(p, desc->ops, desc->op_ld))) return bail(st);
+  if ((st = asg::upload(&p->d_idx1d, p->idx1d))) return bail(st);
+  if ((st = asg::upload(&p->d_op_nb, p->op_nb))) return bail(st);
+  if ((st = asg::upload(&p->d_active, p->active))) return bail(st);
+  if ((st = asg::upload(&p->d_op_off, p->op_off))) return bail(st);
+  if ((st = asg::upload(&p->d_row_ptr, p->row_ptr))) return bail(st);
+  if ((st = asg::upload(&p->d_ent, p->ent))) return bail(st);
+  (void)amax;
+  *out = p;
+  return ASG_OK;
+}
+
+asg_status asg_plan_destroy(asg_plan* plan) {
+  if (!plan) return ASG_OK;
+  asg::free_device(plan);
+  delete plan;
+  return ASG_OK;
+}
+
+asg_status asg_plan_stats_get(const asg_plan* p, asg_plan_stats* s) {
+  if (!p || !s) return fail(ASG_ERR_INVALID, "plan_stats_get: NULL argument");
+  s->num_pairs = p->pairs;
+  s->num_entries = static_cast<long long>(p->ent.size());
+  s->dof = static_cast<long long>(p->N) * p->B;
+  s->flops_reference = p->flops_dense;
+  s->flops_executed = p->flops_exec;
+  s->op_bytes_f64 = p->packed_elems * 8;
+  s->kernel_kind = p->kernel_kind;
+  int amax = 0;
+  for (unsigned a : p->active) amax = std::max(amax, __builtin_popcount(a));
+  s->active_modes_max = amax;
+  return ASG_OK;
+}
+
+asg_status asg_plan_update_ops(asg_plan* p, const double* const* ops, const int* op_ld) {
+  if (!p || !ops || !op_ld) return fail(ASG_ERR_INVALID, "plan_update_ops: NULL argument");
+  for (int tm = 0; tm < p->T * p->D; ++tm) {
+    if (p->op_off[tm] < 0) continue;
+    if (!ops[tm]) return fail(ASG_ERR_INVALID, "plan_update_ops: operator %d is NULL", tm);
+    if (op_ld[tm] < p->op_nb[tm] * p->P) return fail(ASG_ERR_INVALID, "plan_update_ops: ld too small for operator %d", tm);
+  }
+  return asg::pack_and_upload(p, ops, op_ld);
+}
+
+asg_status asg_plan_set_kernel(asg_plan* p, int kind) {
+  if (!p) return fail(ASG_ERR_INVALID, "plan_set_kernel: NULL plan");
+  if (kind == asg::KK_CHAIN_WARP && p->B > 256) return fail(ASG_ERR_UNSUPPORTED, "warp chain kernel needs deg^d <= 256");
+  if (kind == asg::KK_SINGLE_MODE) {
+    bool ok = (p->P == 3 || p->P == 4) && p->B >= 32 * p->P * p->P;
+    for (unsigned a : p->active) ok = ok && __builtin_popcount(a) == 1;
+    if (!ok) return fail(ASG_ERR_UNSUPPORTED, "single-mode kernel needs one non-identity factor per term");
+  }
+  if (kind < 0 || kind > 2) return fail(ASG_ERR_INVALID, "unknown kernel kind %d", kind);
+  p->kernel_kind = kind;
+  return ASG_OK;
+}
+
+asg_status asg_apply_f64(asg_plan* p, const double* f, double* y, void* stream) { return asg::apply_dev<double>(p, f, y, stream); }
+asg_status asg_apply_f32(asg_plan* p, const float* f, float* y, void* stream) { return asg::apply_dev<float>(p, f, y, stream); }
+asg_status asg_apply_host_f64(asg_plan* p, const double* f, double* y) { return asg::apply_host<double>(p, f, y); }
+asg_status asg_apply_host_f32(asg_plan* p, const float* f, float* y) { return asg::apply_host<float>(p, f, y); }
+
+}  // extern "C"

@@ -1,0 +1,140 @@
+/*
+ * asgkron -- GB300 (sm_103a) operator application y = A*f for the sparse-grid DG prototype
+ * of project-asgard/DG-SparseGrid (MATLAB).  Plain C ABI: caller-owned buffers, integer
+ * status codes, no CUDA or framework types in the signatures (streams are void*).
+ *
+ * Each entry point names the reference function whose behaviour it replaces
+ * (file:line within the reference project).
+ *
+ * Conventions
+ *   - Element blocks are deg^d contiguous values, dimension 1 slowest and dimension d
+ *     fastest (krond.m:17, combine_dimensions_D.m:40-51); element e occupies
+ *     [e*deg^d, (e+1)*deg^d) of f and y (apply_A.m:116).
+ *   - 1-D operators are dense column-major (n x n) matrices with leading dimension ld,
+ *     rows in the hierarchical 1-D order of OperatorTwoScale_wavelet2.m:127-144; the rows
+ *     of element e in dimension k are (idx1d[e][k]-base)*deg + (0..deg-1) (apply_A.m:119-122).
+ *   - Index arrays carry an explicit base (0 for C callers, 1 for MATLAB/MEX callers).
+ *   - Device-pointer entry points run asynchronously on the given stream (NULL = the
+ *     legacy default stream); host-pointer entry points are synchronous.
+ */
+#ifndef ASGKRON_H
+#define ASGKRON_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int asg_status;
+enum {
+  ASG_OK = 0,
+  ASG_ERR_INVALID = 1,      /* bad argument, size or index (the reference's error(sprintf(...))) */
+  ASG_ERR_UNSUPPORTED = 2,  /* valid but outside what the kernels handle (e.g. d > 6) */
+  ASG_ERR_CUDA = 3,         /* a CUDA runtime call failed; asg_last_error has the text */
+  ASG_ERR_NOMEM = 4,        /* host or device allocation failed */
+  ASG_ERR_TIMEOUT = 5,      /* a bounded device-side wait gave up */
+  ASG_ERR_CAPACITY = 6      /* caller buffer too small; the needed size is reported */
+};
+
+/* Structure handling of the 1-D operators (the work model the kernels execute). */
+enum {
+  ASG_STRUCT_NONE = 0,   /* reference work model: every listed pair x every term, full
+                            d-mode Kronecker chain (apply_A.m:124-201) */
+  ASG_STRUCT_DETECT = 1  /* skip (pair, term) products with a zero factor block and apply
+                            identity factors as copies; |entry| <= drop_tol * max|op| counts
+                            as zero (drop_tol = 0: exact zeros/identities only) */
+};
+
+enum { ASG_GRID_SG = 0, ASG_GRID_FG = 1 };
+
+typedef struct asg_plan asg_plan;
+
+typedef struct {
+  int num_dims;                /* d, 1..6 (kron_multd.m:30-42) */
+  int deg;                     /* p, 1..8, deg^d <= 4096 */
+  int num_terms;               /* T, 1..16: the terms with pde.terms{t}.imex == imex_flag */
+  int num_elems;               /* N = numel(A_data.element_global_row_index) */
+  int index_base;              /* 0 or 1 for idx1d and cols */
+  const int* idx1d;            /* [num_elems*num_dims]: A_data.element_local_index_D{k}(e) at [e*d+k] */
+  const long long* row_ptr;    /* [num_elems+1] CSR of the pair list, or NULL = all pairs
+                                  (opts.use_connectivity=false, apply_A.m:104-108) */
+  const int* cols;             /* [row_ptr[N]] connected column elements (pde.connectivity{e}) */
+  const double* const* ops;    /* [num_terms*num_dims]: pde.terms{t}.terms_1D{k}.mat at [t*d+k] */
+  const int* op_ld;            /* [num_terms*num_dims] leading dimension (rows) of each operator */
+  int structure;               /* ASG_STRUCT_* */
+  double drop_tol;             /* see ASG_STRUCT_DETECT */
+} asg_plan_desc;
+
+typedef struct {
+  long long num_pairs;         /* listed (row, col) pairs */
+  long long num_entries;       /* (row, col, term) products the kernels execute */
+  long long dof;               /* num_elems * deg^d */
+  double flops_reference;      /* num_pairs * T * d * 2 * deg^(d+1): the reference's work */
+  double flops_executed;       /* flops of the executed work model */
+  long long op_bytes_f64;      /* packed operator bytes on the device (FP64 copy) */
+  int kernel_kind;             /* 0 warp chain, 1 CTA chain, 2 single-mode fiber kernel */
+  int active_modes_max;        /* max over terms of non-identity factors */
+} asg_plan_stats;
+
+/* Library version string and last error text (per thread). */
+const char* asg_version(void);
+asg_status asg_last_error(char* buf, size_t len);
+
+/* ---------------------------------------------------------------------------------------
+ * apply_A (apply_A.m:1-252): plan once per operator set, apply many times.
+ * ------------------------------------------------------------------------------------- */
+/* Validates every index (the isok checks of kron_multd.m:7-12,24-28 and the asserts of
+ * apply_A.m), analyses structure, builds the work list and uploads FP64 + FP32 operator
+ * blocks.  Replaces the per-call setup inside apply_A.m:102-168. */
+asg_status asg_plan_create(const asg_plan_desc* desc, asg_plan** plan);
+asg_status asg_plan_destroy(asg_plan* plan);
+asg_status asg_plan_stats_get(const asg_plan* plan, asg_plan_stats* stats);
+/* Re-upload operator values with the same sparsity class (time-dependent terms rebuilt by
+ * get_coeff_mats.m with TD=1); the structure analysis is not redone. */
+asg_status asg_plan_update_ops(asg_plan* plan, const double* const* ops, const int* op_ld);
+
+/* Force a kernel family for this plan: 0 warp chain (deg^d <= 256), 1 CTA chain,
+ * 2 single-mode fiber kernel (every term has one non-identity factor).  The default is
+ * chosen by asg_plan_create; this exists for testing one family against another. */
+asg_status asg_plan_set_kernel(asg_plan* plan, int kind);
+
+/* ftmp = A*f on device pointers (apply_A.m:185-201). FP64, or FP32 with Kahan-compensated
+ * accumulation across the column reduction. */
+asg_status asg_apply_f64(asg_plan* plan, const double* d_f, double* d_y, void* stream);
+asg_status asg_apply_f32(asg_plan* plan, const float* d_f, float* d_y, void* stream);
+/* Same on host pointers: copies f in, applies, copies y out, synchronises (the call a
+ * MATLAB MEX gateway makes). */
+asg_status asg_apply_host_f64(asg_plan* plan, const double* h_f, double* h_y);
+asg_status asg_apply_host_f32(asg_plan* plan, const float* h_f, float* h_y);
+
+/* ---------------------------------------------------------------------------------------
+ * Element tables and index maps (hash_table_sparse_nD.m, global_matrix.m, connect_nD.m)
+ * ------------------------------------------------------------------------------------- */
+/* Element table in hash_table_sparse_nD.m order (hash_table_sparse_nD.m:35-116): level
+ * tuples with sum <= max(lev_vec) walked from the largest sum down (perm_leq_d.m:26-45),
+ * cells with dimension 1 fastest (lev_cell_to_1D_index_set.m:10-30).  grid ASG_GRID_FG
+ * uses perm_max.m.  Outputs [count*d] levels and cells, and the 0-based md keys
+ * (md_lev_pos_to_idx.m:10-26 minus one).  Pass capacity 0 to query count. */
+asg_status asg_hash_table_sparse_nd(int num_dims, const int* lev_vec, int max_lev, int grid,
+                                    int* levels, int* cells, unsigned long long* keys,
+                                    long long capacity, long long* count);
+/* Old-hash order of hash_table_nD.m:29-136 (perm_leq.m / perm_max.m), used with connectivity. */
+asg_status asg_hash_table_nd(int num_dims, int lev, int grid, int* levels, int* cells,
+                             long long capacity, long long* count);
+/* 1-based 1-D index 2^(lev-1)+cell+1 (1 at level 0) per element and dimension
+ * (lev_cell_to_1D_index.m:6-9, global_matrix.m:31-70). */
+asg_status asg_element_idx1d(int num_dims, long long num_elems, const int* levels, const int* cells,
+                             int* idx1d);
+/* Per-element sorted connected element lists (connect_nD.m:34-105, connect_1D.m:8-50) as
+ * CSR with 0-based columns. grid ASG_GRID_SG uses index_leq_max.m, ASG_GRID_FG index_max.m.
+ * Pass capacity 0 to query the number of pairs. */
+asg_status asg_connect_nd(int num_dims, long long num_elems, const int* levels, const int* cells,
+                          int levsum, int levmax, int grid, long long* row_ptr, int* cols,
+                          long long capacity, long long* num_pairs);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ASGKRON_H */
