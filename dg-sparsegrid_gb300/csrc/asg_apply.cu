@@ -299,24 +299,25 @@ __global__ void __launch_bounds__(256) k_single_mode(ApplyArgs<T> a) {
         __syncthreads();
       }
       cur_m = m;
-    }
-    if (m < 0) break;
-    {
+      if (m >= 0) {
+        // new term group: reset its sum and place this thread's tile over (m, d-1)
 #pragma unroll
-      for (int r = 0; r < P; ++r)
+        for (int r = 0; r < P; ++r)
 #pragma unroll
-        for (int c = 0; c < P; ++c) g[r][c] = gc[r][c] = T(0);
-      if (m < D - 1) {
-        int pw = 1;
-        for (int k = 0; k < D - 2 - m; ++k) pw *= P;
-        const int lo = tid % pw, hi = tid / pw;
-        s_g = a.stride[m];
-        base_g = hi * s_g * P + lo * P;
-      } else {
-        s_g = P;
-        base_g = tid * P * P;
+          for (int c = 0; c < P; ++c) g[r][c] = gc[r][c] = T(0);
+        if (m < D - 1) {
+          int pw = 1;
+          for (int k = 0; k < D - 2 - m; ++k) pw *= P;
+          const int lo = tid % pw, hi = tid / pw;
+          s_g = a.stride[m];
+          base_g = hi * s_g * P + lo * P;
+        } else {
+          s_g = P;
+          base_g = tid * P * P;
+        }
       }
     }
+    if (m < 0) break;
     // P x P block of operator (t, m) at (I_m(row), J_m(j))
     const int tm = t * D + m;
     const T* Ag = a.ops + a.op_off[tm] +
