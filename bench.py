@@ -355,7 +355,7 @@ def main():
             "data": "synthetic (continuity6 operators from the DG builder; f ~ N(0,1) seed 4)",
             "config": {"workload": WORKLOAD, "dof": dof, "work_model": "structured (zero blocks skipped, identity "
                        "factors as copies; drop_tol %.0e)" % asgkron.DEFAULT_DROP_TOL,
-                       "entries": st["num_entries"], "kernel": ["warp_chain", "cta_chain", "single_mode"][st["kernel_kind"]],
+                       "entries": st["num_entries"], "kernel": asgkron._lib.KERNEL_NAMES[st["kernel_kind"]],
                        "l2": "flushed before every step (512 MB write, outside the timed apply)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -22,7 +22,8 @@ ASG_STRUCT_NONE = 0
 ASG_STRUCT_DETECT = 1
 ASG_GRID_SG = 0
 ASG_GRID_FG = 1
-KERNEL_CHAIN_WARP, KERNEL_CHAIN_CTA, KERNEL_SINGLE_MODE = 0, 1, 2
+KERNEL_CHAIN_WARP, KERNEL_CHAIN_CTA, KERNEL_SINGLE_MODE, KERNEL_SINGLE_TMA = 0, 1, 2, 3
+KERNEL_NAMES = ["warp_chain", "cta_chain", "single_mode", "single_mode_tma"]
 
 
 class AsgError(RuntimeError):
@@ -70,6 +71,7 @@ SIGNATURES = {
     "asg_plan_stats_get": (C.c_int, [C.c_void_p, C.POINTER(PlanStats)]),
     "asg_plan_update_ops": (C.c_int, [C.c_void_p, C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.c_int)]),
     "asg_plan_set_kernel": (C.c_int, [C.c_void_p, C.c_int]),
+    "asg_plan_device_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "asg_apply_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "asg_apply_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "asg_apply_host_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),

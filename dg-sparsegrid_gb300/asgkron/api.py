@@ -107,6 +107,12 @@ class Plan:
     def set_kernel(self, kind):
         check(lib().asg_plan_set_kernel(self._handle, int(kind)))
 
+    def device_status(self):
+        """Synchronise and raise AsgError if a kernel of this plan reported a bounded-wait timeout."""
+        st = C.c_int(0)
+        check(lib().asg_plan_device_status(self._handle, C.byref(st)))
+        return st.value
+
     def update_ops(self, term_mats):
         mats = _as_term_mats(term_mats)
         ptrs = (C.POINTER(C.c_double) * (self.T * self.D))()

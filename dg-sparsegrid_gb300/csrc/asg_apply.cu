@@ -376,6 +376,269 @@ __global__ void __launch_bounds__(256) k_single_mode(ApplyArgs<T> a) {
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Single-mode fiber kernel, TMA-pipelined (deg 4).
+//
+// Same thread/tile mapping as k_single_mode, but the operand blocks stream into shared
+// memory with bulk asynchronous copies (cp.async.bulk, one elected thread, completion on an
+// mbarrier with a transaction count): the column element's whole f block (deg^d values)
+// plus its P x P operator block per work entry, S entries in flight.  The threads never
+// wait on a global load; they wait on the stage's mbarrier (bounded: after ~2^31 cycles
+// the CTA records ASG_ERR_TIMEOUT in the plan's status word and stops).  Per term group the
+// products are summed in FP32 registers; groups are merged into the output tile with Kahan
+// compensation.  FP32 products use the paired FMA (fma.rn.f32x2).
+// ---------------------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: true when the phase completed, false after ~2^31 cycles (~1 s).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  if (mbar_test(bar, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_test(bar, parity)) {
+    if (clock64() - t0 > (1LL << 31)) return false;
+  }
+  return true;
+}
+
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
+  unsigned long long d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;"
+      : "=l"(d)
+      : "l"(*reinterpret_cast<unsigned long long*>(&a)), "l"(*reinterpret_cast<unsigned long long*>(&b)),
+        "l"(*reinterpret_cast<unsigned long long*>(&c)));
+  return *reinterpret_cast<float2*>(&d);
+}
+
+// g[a][c] += sum_b A[a][b] * x[b][c]   (contraction across the tile rows)
+template <typename T>
+__device__ __forceinline__ void tile_rows(T (&g)[4][4], const T* A, const T* xs, int s) {
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    Row<T, 4> x;
+    x.load(xs + b * s);
+#pragma unroll
+    for (int aa = 0; aa < 4; ++aa)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) g[aa][c] = fma(A[aa * 4 + b], x.v[c], g[aa][c]);
+  }
+}
+template <>
+__device__ __forceinline__ void tile_rows<float>(float (&g)[4][4], const float* A, const float* xs, int s) {
+  float2 acc[4][2];
+#pragma unroll
+  for (int aa = 0; aa < 4; ++aa) {
+    acc[aa][0] = make_float2(g[aa][0], g[aa][1]);
+    acc[aa][1] = make_float2(g[aa][2], g[aa][3]);
+  }
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    const float4 x = *reinterpret_cast<const float4*>(xs + b * s);
+    const float2 x01 = make_float2(x.x, x.y), x23 = make_float2(x.z, x.w);
+#pragma unroll
+    for (int aa = 0; aa < 4; ++aa) {
+      const float2 ab = make_float2(A[aa * 4 + b], A[aa * 4 + b]);
+      acc[aa][0] = ffma2(ab, x01, acc[aa][0]);
+      acc[aa][1] = ffma2(ab, x23, acc[aa][1]);
+    }
+  }
+#pragma unroll
+  for (int aa = 0; aa < 4; ++aa) {
+    g[aa][0] = acc[aa][0].x; g[aa][1] = acc[aa][0].y;
+    g[aa][2] = acc[aa][1].x; g[aa][3] = acc[aa][1].y;
+  }
+}
+// g[r][a] += sum_b A[a][b] * x[r][b]   (contraction along the contiguous index)
+template <typename T>
+__device__ __forceinline__ void tile_cols(T (&g)[4][4], const T* A, const T* xs) {
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    Row<T, 4> x;
+    x.load(xs + r * 4);
+#pragma unroll
+    for (int aa = 0; aa < 4; ++aa)
+#pragma unroll
+      for (int b = 0; b < 4; ++b) g[r][aa] = fma(A[aa * 4 + b], x.v[b], g[r][aa]);
+  }
+}
+template <>
+__device__ __forceinline__ void tile_cols<float>(float (&g)[4][4], const float* A, const float* xs) {
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const float4 x = *reinterpret_cast<const float4*>(xs + r * 4);
+    const float xv[4] = {x.x, x.y, x.z, x.w};
+    float2 acc0 = make_float2(g[r][0], g[r][1]), acc1 = make_float2(g[r][2], g[r][3]);
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const float2 xb = make_float2(xv[b], xv[b]);
+      acc0 = ffma2(make_float2(A[0 * 4 + b], A[1 * 4 + b]), xb, acc0);
+      acc1 = ffma2(make_float2(A[2 * 4 + b], A[3 * 4 + b]), xb, acc1);
+    }
+    g[r][0] = acc0.x; g[r][1] = acc0.y; g[r][2] = acc1.x; g[r][3] = acc1.y;
+  }
+}
+
+template <typename T, int S, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_single_tma(ApplyArgs<T> a) {
+  constexpr int P = 4;
+  constexpr bool KAHAN = sizeof(T) == 4;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_abort;
+  const int tid = threadIdx.x;
+  const int B = a.B, D = a.D;
+  const int SST = B + P * P;  // stage: f block then the P x P operator block
+  T* stages = reinterpret_cast<T*>(smem_raw);
+  T* scratch = stages + S * SST;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(scratch + B);
+  const int row = blockIdx.x;
+  const long long q0 = a.row_ptr[row];
+  const int n = static_cast<int>(a.row_ptr[row + 1] - q0);
+  const EntryDesc* ed = a.ed + q0;
+  const uint32_t fbytes = static_cast<uint32_t>(B * sizeof(T)), abytes = P * P * sizeof(T);
+
+  if (tid == 0) {
+    s_abort = 0;
+    for (int k = 0; k < S; ++k) mbar_init(&bars[k], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  auto issue = [&](int k) {
+    const int st = k % S;
+    T* dst = stages + st * SST;
+    const EntryDesc e = ed[k];
+    mbar_expect_tx(&bars[st], fbytes + abytes);
+    bulk_g2s(dst, a.f + static_cast<size_t>(e.j) * B, fbytes, &bars[st]);
+    bulk_g2s(dst + B, a.ops + e.aoff, abytes, &bars[st]);
+  };
+  if (tid == 0) {
+    for (int k = 0; k < S && k < n; ++k) issue(k);
+  }
+
+  T nat[P][P], natc[P][P], g[P][P];
+#pragma unroll
+  for (int r = 0; r < P; ++r)
+#pragma unroll
+    for (int c = 0; c < P; ++c) nat[r][c] = natc[r][c] = g[r][c] = T(0);
+
+  int cur_m = -1, base_g = 0, s_g = 0;
+  int kab = -1;  // entry at which a bounded wait gave up
+  for (int k = 0; k <= n; ++k) {
+    const int m = (k < n) ? ed[k].m : -1;
+    if (m != cur_m) {
+      if (cur_m >= D - 2) {
+#pragma unroll
+        for (int r = 0; r < P; ++r)
+#pragma unroll
+          for (int c = 0; c < P; ++c) acc_add(nat[r][c], natc[r][c], g[r][c], KAHAN);
+      } else if (cur_m >= 0) {
+#pragma unroll
+        for (int r = 0; r < P; ++r) {
+          Row<T, P> rr;
+#pragma unroll
+          for (int c = 0; c < P; ++c) rr.v[c] = g[r][c];
+          rr.store(scratch + base_g + r * s_g);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < P; ++r) {
+          Row<T, P> rr;
+          rr.load(scratch + tid * P * P + r * P);
+#pragma unroll
+          for (int c = 0; c < P; ++c) acc_add(nat[r][c], natc[r][c], rr.v[c], KAHAN);
+        }
+        __syncthreads();
+      }
+      cur_m = m;
+      if (m >= 0) {
+#pragma unroll
+        for (int r = 0; r < P; ++r)
+#pragma unroll
+          for (int c = 0; c < P; ++c) g[r][c] = T(0);
+        if (m < D - 1) {
+          int pw = 1;
+          for (int k2 = 0; k2 < D - 2 - m; ++k2) pw *= P;
+          const int lo = tid % pw, hi = tid / pw;
+          s_g = a.stride[m];
+          base_g = hi * s_g * P + lo * P;
+        } else {
+          s_g = P;
+          base_g = tid * P * P;
+        }
+      }
+    }
+    if (m < 0) break;
+    const int st = k % S;
+    if (!mbar_wait_bounded(&bars[st], static_cast<uint32_t>((k / S) & 1))) s_abort = 1;
+    __syncthreads();
+    if (s_abort) {
+      kab = k;
+      break;
+    }
+    const T* sp = stages + st * SST;
+    T A[P * P];
+#pragma unroll
+    for (int r = 0; r < P; ++r) {
+      Row<T, P> rr;
+      rr.load(sp + B + r * P);
+#pragma unroll
+      for (int c = 0; c < P; ++c) A[r * P + c] = rr.v[c];
+    }
+    if (m == D - 1)
+      tile_cols<T>(g, A, sp + base_g);
+    else
+      tile_rows<T>(g, A, sp + base_g, s_g);
+    __syncthreads();  // every thread is done with stage st
+    if (tid == 0 && k + S < n) {
+      fence_proxy_async();
+      issue(k + S);
+    }
+  }
+  if (kab >= 0) {
+    if (tid == 0) {
+      atomicExch(a.err, static_cast<int>(ASG_ERR_TIMEOUT));
+      // let the copies still in flight (entries kab .. kab+S-1) land before the CTA's shared
+      // memory is released; each wait is bounded as well
+      for (int k = kab; k < kab + S && k < n; ++k) {
+        const long long t0 = clock64();
+        while (!mbar_test(&bars[k % S], static_cast<uint32_t>((k / S) & 1)) && clock64() - t0 < (1LL << 28)) {
+        }
+      }
+    }
+    return;
+  }
+  T* yr = a.y + static_cast<size_t>(row) * B + tid * P * P;
+#pragma unroll
+  for (int r = 0; r < P; ++r) {
+    Row<T, P> rr;
+#pragma unroll
+    for (int c = 0; c < P; ++c) rr.v[c] = nat[r][c];
+    rr.store(yr + r * P);
+  }
+}
+
 // Opt a kernel into more than 48 KB of dynamic shared memory (once per instantiation; the
 // limit set is the largest this kernel can request, so later plans need no new call).
 template <typename K>
@@ -410,6 +673,21 @@ cudaError_t launch_p(const ApplyArgs<T>& a, int kind, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     kern<<<a.N, NT, sm, s>>>(a);
     return cudaGetLastError();
+  }
+  if constexpr (P == 4) {
+    if (kind == KK_SINGLE_TMA) {
+      constexpr int S = sizeof(T) == 4 ? 4 : 3;
+      constexpr int MINB = sizeof(T) == 4 ? 2 : 1;
+      const int nt = a.B / (P * P);
+      const size_t sm = (static_cast<size_t>(S) * (a.B + P * P) + a.B) * sizeof(T) + S * sizeof(uint64_t);
+      auto kern = k_single_tma<T, S, MINB>;
+      static bool done = false;
+      cudaError_t e = ensure_smem(
+          kern, sm, (static_cast<size_t>(S) * (kMaxBlock + P * P) + kMaxBlock) * sizeof(T) + S * sizeof(uint64_t), done);
+      if (e != cudaSuccess) return e;
+      kern<<<a.N, nt, sm, s>>>(a);
+      return cudaGetLastError();
+    }
   }
   if constexpr (P == 3 || P == 4) {
     if (kind == KK_SINGLE_MODE) {

@@ -25,6 +25,14 @@ asg_status cuda_fail(cudaError_t e, const char* what);
     if (_e != cudaSuccess) return ::asg::cuda_fail(_e, #call); \
   } while (0)
 
+// Precomputed work entry of the single-mode kernels: column element, the entry's
+// non-identity dimension, and the element offset of its P x P operator block.
+struct EntryDesc {
+  int j;
+  int m;
+  long long aoff;
+};
+
 // Arguments of the operator-application kernels.  One work entry is one
 // (column element, term) product contributing to a row element; entries of a row are
 // contiguous (CSR by row), packed as (col << 4) | term.
@@ -41,12 +49,14 @@ struct ApplyArgs {
   const unsigned* active;    // [T] bit m set <=> operator (t,m) is applied (else identity)
   int N, D, B, nterms;
   int stride[kMaxDims];      // deg^(D-1-m): element-block stride of dimension m
+  const EntryDesc* ed;       // [entries] single-mode descriptors (NULL for chain plans)
+  int* err;                  // device status word (ASG_ERR_TIMEOUT after a bounded wait gave up)
 };
 
 template <typename T>
 cudaError_t launch_apply(const ApplyArgs<T>& a, int P, int kernel_kind, cudaStream_t s);
 
-enum KernelKind { KK_CHAIN_WARP = 0, KK_CHAIN_CTA = 1, KK_SINGLE_MODE = 2 };
+enum KernelKind { KK_CHAIN_WARP = 0, KK_CHAIN_CTA = 1, KK_SINGLE_MODE = 2, KK_SINGLE_TMA = 3 };
 
 }  // namespace asg
 
@@ -77,6 +87,9 @@ struct asg_plan {
   int* d_ent = nullptr;
   long long* d_tr_row_ptr = nullptr;
   int* d_tr_ent = nullptr;
+  std::vector<asg::EntryDesc> ed;   // single-mode descriptors (empty unless every term has one factor)
+  asg::EntryDesc* d_ed = nullptr;
+  int* d_err = nullptr;
   double* d_ops64 = nullptr;
   float* d_ops32 = nullptr;
   // host-pointer apply path (staging owned by the plan)

@@ -48,6 +48,8 @@ void free_device(asg_plan* p) {
   cudaFree(p->d_tr_ent);
   cudaFree(p->d_ops64);
   cudaFree(p->d_ops32);
+  cudaFree(p->d_ed);
+  cudaFree(p->d_err);
   cudaFree(p->d_io);
   if (p->stream) cudaStreamDestroy(p->stream);
 }
@@ -102,6 +104,8 @@ ApplyArgs<T> make_args(const asg_plan* p, const T* f, T* y, const T* ops) {
   a.D = p->D;
   a.B = p->B;
   a.nterms = p->T;
+  a.ed = p->d_ed;
+  a.err = p->d_err;
   int s = 1;
   for (int m = p->D - 1; m >= 0; --m) {
     a.stride[m] = s;
@@ -350,7 +354,8 @@ asg_status asg_plan_create(const asg_plan_desc* desc, asg_plan** out) {
     amax = std::max(amax, na);
     if (na != 1) single = false;
   }
-  p->kernel_kind = single ? asg::KK_SINGLE_MODE : (B <= 256 ? asg::KK_CHAIN_WARP : asg::KK_CHAIN_CTA);
+  p->kernel_kind = single ? (P == 4 ? asg::KK_SINGLE_TMA : asg::KK_SINGLE_MODE)
+                          : (B <= 256 ? asg::KK_CHAIN_WARP : asg::KK_CHAIN_CTA);
   // ---- pack operators -------------------------------------------------------------
   long long off = 0;
   for (int t = 0; t < T; ++t)
@@ -361,6 +366,20 @@ asg_status asg_plan_create(const asg_plan_desc* desc, asg_plan** out) {
       off += static_cast<long long>(p->op_nb[tm]) * p->op_nb[tm] * P * P;
     }
   p->packed_elems = off;
+  if (single) {
+    // per-entry descriptors of the single-mode kernels: column, dimension, block offset
+    p->ed.resize(ent.size());
+    for (int i = 0; i < N; ++i)
+      for (long long q = p->row_ptr[i]; q < p->row_ptr[i + 1]; ++q) {
+        const int j = ent[q] >> 4, t = ent[q] & 15;
+        const int m = __builtin_ctz(p->active[t]);
+        const int tm = t * D + m;
+        p->ed[q].j = j;
+        p->ed[q].m = m;
+        p->ed[q].aoff = p->op_off[tm] + (static_cast<long long>(p->idx1d[i * D + m]) * p->op_nb[tm] +
+                                         p->idx1d[j * D + m]) * P * P;
+      }
+  }
   asg_status st;
   if ((st = asg::pack_and_upload(p, desc->ops, desc->op_ld))) return bail(st);
   if ((st = asg::upload(&p->d_idx1d, p->idx1d))) return bail(st);
@@ -369,6 +388,12 @@ asg_status asg_plan_create(const asg_plan_desc* desc, asg_plan** out) {
   if ((st = asg::upload(&p->d_op_off, p->op_off))) return bail(st);
   if ((st = asg::upload(&p->d_row_ptr, p->row_ptr))) return bail(st);
   if ((st = asg::upload(&p->d_ent, p->ent))) return bail(st);
+  if ((st = asg::upload(&p->d_ed, p->ed))) return bail(st);
+  {
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p->d_err), sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(p->d_err, 0, sizeof(int));
+    if (e != cudaSuccess) return bail(asg::cuda_fail(e, "status word"));
+  }
   (void)amax;
   *out = p;
   return ASG_OK;
@@ -409,13 +434,26 @@ asg_status asg_plan_update_ops(asg_plan* p, const double* const* ops, const int*
 asg_status asg_plan_set_kernel(asg_plan* p, int kind) {
   if (!p) return fail(ASG_ERR_INVALID, "plan_set_kernel: NULL plan");
   if (kind == asg::KK_CHAIN_WARP && p->B > 256) return fail(ASG_ERR_UNSUPPORTED, "warp chain kernel needs deg^d <= 256");
-  if (kind == asg::KK_SINGLE_MODE) {
-    bool ok = (p->P == 3 || p->P == 4) && p->B >= 32 * p->P * p->P;
+  if (kind == asg::KK_SINGLE_MODE || kind == asg::KK_SINGLE_TMA) {
+    bool ok = (p->P == 4 || (kind == asg::KK_SINGLE_MODE && p->P == 3)) && p->B >= 32 * p->P * p->P;
     for (unsigned a : p->active) ok = ok && __builtin_popcount(a) == 1;
-    if (!ok) return fail(ASG_ERR_UNSUPPORTED, "single-mode kernel needs one non-identity factor per term");
+    if (!ok || p->ed.size() != p->ent.size())
+      return fail(ASG_ERR_UNSUPPORTED, "single-mode kernels need one non-identity factor per term (deg 3/4)");
   }
-  if (kind < 0 || kind > 2) return fail(ASG_ERR_INVALID, "unknown kernel kind %d", kind);
+  if (kind < 0 || kind > 3) return fail(ASG_ERR_INVALID, "unknown kernel kind %d", kind);
   p->kernel_kind = kind;
+  return ASG_OK;
+}
+
+asg_status asg_plan_device_status(asg_plan* p, int* status) {
+  if (!p || !status) return fail(ASG_ERR_INVALID, "plan_device_status: NULL argument");
+  int v = 0;
+  ASG_CUDA(cudaMemcpy(&v, p->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+  *status = v;
+  if (v != 0) {
+    ASG_CUDA(cudaMemset(p->d_err, 0, sizeof(int)));
+    return fail(v, "a kernel of this plan reported status %d (bounded wait gave up)", v);
+  }
   return ASG_OK;
 }
 

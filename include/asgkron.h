@@ -73,7 +73,7 @@ typedef struct {
   double flops_reference;      /* num_pairs * T * d * 2 * deg^(d+1): the reference's work */
   double flops_executed;       /* flops of the executed work model */
   long long op_bytes_f64;      /* packed operator bytes on the device (FP64 copy) */
-  int kernel_kind;             /* 0 warp chain, 1 CTA chain, 2 single-mode fiber kernel */
+  int kernel_kind;             /* 0 warp chain, 1 CTA chain, 2/3 single-mode fiber kernels */
   int active_modes_max;        /* max over terms of non-identity factors */
 } asg_plan_stats;
 
@@ -95,9 +95,14 @@ asg_status asg_plan_stats_get(const asg_plan* plan, asg_plan_stats* stats);
 asg_status asg_plan_update_ops(asg_plan* plan, const double* const* ops, const int* op_ld);
 
 /* Force a kernel family for this plan: 0 warp chain (deg^d <= 256), 1 CTA chain,
- * 2 single-mode fiber kernel (every term has one non-identity factor).  The default is
+ * 2 single-mode fiber kernel with direct loads, 3 single-mode fiber kernel with TMA bulk
+ * copies (2 and 3 need one non-identity factor per term; 3 needs deg 4).  The default is
  * chosen by asg_plan_create; this exists for testing one family against another. */
 asg_status asg_plan_set_kernel(asg_plan* plan, int kind);
+/* Synchronises and reads the plan's device status word: ASG_OK, or ASG_ERR_TIMEOUT when a
+ * kernel's bounded shared-memory pipeline wait gave up (the y it wrote is then undefined).
+ * The word is cleared after reading.  No reference counterpart: device-side waits are new. */
+asg_status asg_plan_device_status(asg_plan* plan, int* status);
 
 /* ftmp = A*f on device pointers (apply_A.m:185-201). FP64, or FP32 with Kahan-compensated
  * accumulation across the column reduction. */

@@ -107,12 +107,17 @@ def test_continuity6_lev4_deg4_kernels_agree(dev):
     want = O.apply_A_rows(mats, idx.astype(np.int64), 4, f, rows=rows)
     p = _plan(mats, idx, 4, structure="detect")
     st = p.stats()
-    assert st["kernel_kind"] == asgkron._lib.KERNEL_SINGLE_MODE
+    assert st["kernel_kind"] == asgkron._lib.KERNEL_SINGLE_TMA
     assert st["active_modes_max"] == 1
     y_single = _apply(p, f, dev)
+    assert p.device_status() == 0
     assert rel2(y_single.reshape(-1, B)[rows].ravel(), want) <= FP64_TOL
     y32 = _apply(p, f, dev, torch.float32)
+    assert p.device_status() == 0
     assert rel2(y32, y_single) <= FP32_TOL
+    p.set_kernel(asgkron._lib.KERNEL_SINGLE_MODE)
+    assert rel2(_apply(p, f, dev), y_single) <= FP64_TOL
+    assert rel2(_apply(p, f, dev, torch.float32), y_single) <= FP32_TOL
     p.set_kernel(asgkron._lib.KERNEL_CHAIN_CTA)
     y_chain = _apply(p, f, dev)
     assert rel2(y_chain, y_single) <= FP64_TOL
