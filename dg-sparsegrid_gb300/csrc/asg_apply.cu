@@ -471,13 +471,13 @@ __device__ __forceinline__ void tile_rows<float>(float (&g)[4][4], const float* 
     g[aa][2] = acc[aa][1].x; g[aa][3] = acc[aa][1].y;
   }
 }
-// g[r][a] += sum_b A[a][b] * x[r][b]   (contraction along the contiguous index)
+// g[r][a] += sum_b A[a][b] * x[r][b] with tile rows s apart
 template <typename T>
-__device__ __forceinline__ void tile_cols(T (&g)[4][4], const T* A, const T* xs) {
+__device__ __forceinline__ void tile_cols_s(T (&g)[4][4], const T* A, const T* xs, int s) {
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
     Row<T, 4> x;
-    x.load(xs + r * 4);
+    x.load(xs + r * s);
 #pragma unroll
     for (int aa = 0; aa < 4; ++aa)
 #pragma unroll
@@ -485,10 +485,10 @@ __device__ __forceinline__ void tile_cols(T (&g)[4][4], const T* A, const T* xs)
   }
 }
 template <>
-__device__ __forceinline__ void tile_cols<float>(float (&g)[4][4], const float* A, const float* xs) {
+__device__ __forceinline__ void tile_cols_s<float>(float (&g)[4][4], const float* A, const float* xs, int s) {
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
-    const float4 x = *reinterpret_cast<const float4*>(xs + r * 4);
+    const float4 x = *reinterpret_cast<const float4*>(xs + r * s);
     const float xv[4] = {x.x, x.y, x.z, x.w};
     float2 acc0 = make_float2(g[r][0], g[r][1]), acc1 = make_float2(g[r][2], g[r][3]);
 #pragma unroll
@@ -501,18 +501,42 @@ __device__ __forceinline__ void tile_cols<float>(float (&g)[4][4], const float* 
   }
 }
 
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void consumer_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
+
+// Base offset and row stride of a thread's P x P tile spanning dimensions (u, d-1): the
+// thread's other digits run over dimensions {0..d-2} \ {u}, the highest dimension fastest.
+__device__ __forceinline__ void tile_place(int tid, int u, int D, const int* stride, int& base, int& s) {
+  int pw = 1;
+  for (int k = 0; k < D - 2 - u; ++k) pw *= 4;
+  const int lo = tid % pw, hi = tid / pw;
+  s = stride[u];
+  base = hi * s * 4 + lo * 4;
+}
+
+// Warp-specialised pipeline: warps 0..7 consume (256 threads, one P x P output tile each),
+// warp 8 produces.  Stage st holds the column element's f block, its operator block and the
+// entry's dimension; full[st] completes when the bulk copies land (transaction count),
+// empty[st] when all 8 consumer warps are done reading it.  The natural output tile of a
+// thread spans dimensions (d-3, d-1), so consecutive threads sit 16 bytes apart in shared
+// memory; terms on dimensions d-3 and d-1 accumulate straight into it, the others through
+// one shared-memory transpose per term group.
 template <typename T, int S, int MINB>
-__global__ void __launch_bounds__(256, MINB) k_single_tma(ApplyArgs<T> a) {
+__global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
   constexpr int P = 4;
   constexpr bool KAHAN = sizeof(T) == 4;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_abort;
   const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
   const int B = a.B, D = a.D;
-  const int SST = B + P * P;  // stage: f block then the P x P operator block
+  const int SST = B + P * P;
   T* stages = reinterpret_cast<T*>(smem_raw);
   T* scratch = stages + S * SST;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(scratch + B);
+  uint64_t* full = reinterpret_cast<uint64_t*>(scratch + B);
+  uint64_t* empty = full + S;
   const int row = blockIdx.x;
   const long long q0 = a.row_ptr[row];
   const int n = static_cast<int>(a.row_ptr[row + 1] - q0);
@@ -521,34 +545,81 @@ __global__ void __launch_bounds__(256, MINB) k_single_tma(ApplyArgs<T> a) {
 
   if (tid == 0) {
     s_abort = 0;
-    for (int k = 0; k < S; ++k) mbar_init(&bars[k], 1);
+    for (int k = 0; k < S; ++k) {
+      mbar_init(&full[k], 1);
+      mbar_init(&empty[k], 8);
+    }
     mbar_fence_init();
   }
   __syncthreads();
-  auto issue = [&](int k) {
-    const int st = k % S;
-    T* dst = stages + st * SST;
-    const EntryDesc e = ed[k];
-    mbar_expect_tx(&bars[st], fbytes + abytes);
-    bulk_g2s(dst, a.f + static_cast<size_t>(e.j) * B, fbytes, &bars[st]);
-    bulk_g2s(dst + B, a.ops + e.aoff, abytes, &bars[st]);
-  };
-  if (tid == 0) {
-    for (int k = 0; k < S && k < n; ++k) issue(k);
+
+  volatile int* abort_flag = &s_abort;
+  if (warp == 8) {
+    // ---------------- producer warp ----------------
+    int kdone = 0;  // entries whose copies were issued
+    bool stop = false;
+    for (int k0 = 0; k0 < n && !stop; k0 += 32) {
+      EntryDesc mine{};
+      if (k0 + lane < n) mine = ed[k0 + lane];
+      const int cnt = min(32, n - k0);
+      for (int l = 0; l < cnt; ++l) {
+        const int j = __shfl_sync(0xffffffffu, mine.j, l);
+        const long long aoff = __shfl_sync(0xffffffffu, mine.aoff, l);
+        const int k = k0 + l;
+        const int st = k % S;
+        bool ok = true;
+        if (k >= S) ok = mbar_wait_bounded(&empty[st], static_cast<uint32_t>(((k / S) - 1) & 1));
+        if (!__all_sync(0xffffffffu, ok)) {
+          if (lane == 0) *abort_flag = 1;
+          stop = true;
+          break;
+        }
+        if (lane == 0) {
+          T* dst = stages + st * SST;
+          fence_proxy_async();
+          mbar_expect_tx(&full[st], fbytes + abytes);
+          bulk_g2s(dst, a.f + static_cast<size_t>(j) * B, fbytes, &full[st]);
+          bulk_g2s(dst + B, a.ops + aoff, abytes, &full[st]);
+        }
+        kdone = k + 1;
+        __syncwarp();
+      }
+    }
+    if (lane == 0) {
+      if (*abort_flag) atomicExch(a.err, static_cast<int>(ASG_ERR_TIMEOUT));
+      // every issued copy lands before the CTA's shared memory is released (bounded)
+      for (int k = max(0, kdone - S); k < kdone; ++k) {
+        const long long t0 = clock64();
+        while (!mbar_test(&full[k % S], static_cast<uint32_t>((k / S) & 1)) && clock64() - t0 < (1LL << 28)) {
+        }
+      }
+    }
+    return;
   }
 
+  // ---------------- consumer warps ----------------
   T nat[P][P], natc[P][P], g[P][P];
 #pragma unroll
   for (int r = 0; r < P; ++r)
 #pragma unroll
     for (int c = 0; c < P; ++c) nat[r][c] = natc[r][c] = g[r][c] = T(0);
-
+  int nat_base, nat_s;
+  tile_place(tid, D - 3, D, a.stride, nat_base, nat_s);
   int cur_m = -1, base_g = 0, s_g = 0;
-  int kab = -1;  // entry at which a bounded wait gave up
+  bool direct = false;
+  int mlane = -1;  // dimension of entry (k & ~31) + lane, prefetched per warp
   for (int k = 0; k <= n; ++k) {
-    const int m = (k < n) ? ed[k].m : -1;
+    int m = -1;
+    const int st = k % S;
+    if (k < n) {
+      if ((k & 31) == 0) mlane = (k + lane < n) ? ed[k + lane].m : -1;
+      // the dimension comes from the immutable descriptors, so consumer control flow (and
+      // every named barrier below) is uniform even after a timeout; later waits are skipped
+      m = __shfl_sync(0xffffffffu, mlane, k & 31);
+      if (!*abort_flag && !mbar_wait_bounded(&full[st], static_cast<uint32_t>((k / S) & 1))) *abort_flag = 1;
+    }
     if (m != cur_m) {
-      if (cur_m >= D - 2) {
+      if (direct) {
 #pragma unroll
         for (int r = 0; r < P; ++r)
 #pragma unroll
@@ -561,41 +632,29 @@ __global__ void __launch_bounds__(256, MINB) k_single_tma(ApplyArgs<T> a) {
           for (int c = 0; c < P; ++c) rr.v[c] = g[r][c];
           rr.store(scratch + base_g + r * s_g);
         }
-        __syncthreads();
+        consumer_sync();
 #pragma unroll
         for (int r = 0; r < P; ++r) {
           Row<T, P> rr;
-          rr.load(scratch + tid * P * P + r * P);
+          rr.load(scratch + nat_base + r * nat_s);
 #pragma unroll
           for (int c = 0; c < P; ++c) acc_add(nat[r][c], natc[r][c], rr.v[c], KAHAN);
         }
-        __syncthreads();
+        consumer_sync();
       }
       cur_m = m;
-      if (m >= 0) {
+      if (m < 0) break;
 #pragma unroll
-        for (int r = 0; r < P; ++r)
+      for (int r = 0; r < P; ++r)
 #pragma unroll
-          for (int c = 0; c < P; ++c) g[r][c] = T(0);
-        if (m < D - 1) {
-          int pw = 1;
-          for (int k2 = 0; k2 < D - 2 - m; ++k2) pw *= P;
-          const int lo = tid % pw, hi = tid / pw;
-          s_g = a.stride[m];
-          base_g = hi * s_g * P + lo * P;
-        } else {
-          s_g = P;
-          base_g = tid * P * P;
-        }
+        for (int c = 0; c < P; ++c) g[r][c] = T(0);
+      direct = (m == D - 1) || (m == D - 3);
+      if (m == D - 1) {
+        base_g = nat_base;
+        s_g = nat_s;
+      } else {
+        tile_place(tid, m, D, a.stride, base_g, s_g);
       }
-    }
-    if (m < 0) break;
-    const int st = k % S;
-    if (!mbar_wait_bounded(&bars[st], static_cast<uint32_t>((k / S) & 1))) s_abort = 1;
-    __syncthreads();
-    if (s_abort) {
-      kab = k;
-      break;
     }
     const T* sp = stages + st * SST;
     T A[P * P];
@@ -607,35 +666,20 @@ __global__ void __launch_bounds__(256, MINB) k_single_tma(ApplyArgs<T> a) {
       for (int c = 0; c < P; ++c) A[r * P + c] = rr.v[c];
     }
     if (m == D - 1)
-      tile_cols<T>(g, A, sp + base_g);
+      tile_cols_s<T>(g, A, sp + base_g, s_g);
     else
       tile_rows<T>(g, A, sp + base_g, s_g);
-    __syncthreads();  // every thread is done with stage st
-    if (tid == 0 && k + S < n) {
-      fence_proxy_async();
-      issue(k + S);
-    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[st]);
   }
-  if (kab >= 0) {
-    if (tid == 0) {
-      atomicExch(a.err, static_cast<int>(ASG_ERR_TIMEOUT));
-      // let the copies still in flight (entries kab .. kab+S-1) land before the CTA's shared
-      // memory is released; each wait is bounded as well
-      for (int k = kab; k < kab + S && k < n; ++k) {
-        const long long t0 = clock64();
-        while (!mbar_test(&bars[k % S], static_cast<uint32_t>((k / S) & 1)) && clock64() - t0 < (1LL << 28)) {
-        }
-      }
-    }
-    return;
-  }
-  T* yr = a.y + static_cast<size_t>(row) * B + tid * P * P;
+  if (*abort_flag) return;  // y is undefined; the plan's status word reports the timeout
+  T* yr = a.y + static_cast<size_t>(row) * B + nat_base;
 #pragma unroll
   for (int r = 0; r < P; ++r) {
     Row<T, P> rr;
 #pragma unroll
     for (int c = 0; c < P; ++c) rr.v[c] = nat[r][c];
-    rr.store(yr + r * P);
+    rr.store(yr + r * nat_s);
   }
 }
 
@@ -678,14 +722,13 @@ cudaError_t launch_p(const ApplyArgs<T>& a, int kind, cudaStream_t s) {
     if (kind == KK_SINGLE_TMA) {
       constexpr int S = sizeof(T) == 4 ? 4 : 3;
       constexpr int MINB = sizeof(T) == 4 ? 2 : 1;
-      const int nt = a.B / (P * P);
-      const size_t sm = (static_cast<size_t>(S) * (a.B + P * P) + a.B) * sizeof(T) + S * sizeof(uint64_t);
+      if (a.B != 256 * P * P) return cudaErrorInvalidValue;  // 8 consumer warps own one tile each
+      const size_t sm = (static_cast<size_t>(S) * (a.B + P * P) + a.B) * sizeof(T) + 2 * S * sizeof(uint64_t);
       auto kern = k_single_tma<T, S, MINB>;
       static bool done = false;
-      cudaError_t e = ensure_smem(
-          kern, sm, (static_cast<size_t>(S) * (kMaxBlock + P * P) + kMaxBlock) * sizeof(T) + S * sizeof(uint64_t), done);
+      cudaError_t e = ensure_smem(kern, sm, sm, done);
       if (e != cudaSuccess) return e;
-      kern<<<a.N, nt, sm, s>>>(a);
+      kern<<<a.N, 288, sm, s>>>(a);
       return cudaGetLastError();
     }
   }

@@ -354,7 +354,7 @@ asg_status asg_plan_create(const asg_plan_desc* desc, asg_plan** out) {
     amax = std::max(amax, na);
     if (na != 1) single = false;
   }
-  p->kernel_kind = single ? (P == 4 ? asg::KK_SINGLE_TMA : asg::KK_SINGLE_MODE)
+  p->kernel_kind = single ? ((P == 4 && B == 4096) ? asg::KK_SINGLE_TMA : asg::KK_SINGLE_MODE)
                           : (B <= 256 ? asg::KK_CHAIN_WARP : asg::KK_CHAIN_CTA);
   // ---- pack operators -------------------------------------------------------------
   long long off = 0;
@@ -435,7 +435,8 @@ asg_status asg_plan_set_kernel(asg_plan* p, int kind) {
   if (!p) return fail(ASG_ERR_INVALID, "plan_set_kernel: NULL plan");
   if (kind == asg::KK_CHAIN_WARP && p->B > 256) return fail(ASG_ERR_UNSUPPORTED, "warp chain kernel needs deg^d <= 256");
   if (kind == asg::KK_SINGLE_MODE || kind == asg::KK_SINGLE_TMA) {
-    bool ok = (p->P == 4 || (kind == asg::KK_SINGLE_MODE && p->P == 3)) && p->B >= 32 * p->P * p->P;
+    bool ok = kind == asg::KK_SINGLE_TMA ? (p->P == 4 && p->B == 4096)
+                                         : ((p->P == 3 || p->P == 4) && p->B >= 32 * p->P * p->P);
     for (unsigned a : p->active) ok = ok && __builtin_popcount(a) == 1;
     if (!ok || p->ed.size() != p->ent.size())
       return fail(ASG_ERR_UNSUPPORTED, "single-mode kernels need one non-identity factor per term (deg 3/4)");
