@@ -517,31 +517,80 @@ __device__ __forceinline__ void tile_place(int tid, int u, int D, const int* str
 }
 
 // Warp-specialised pipeline: warps 0..7 consume (256 threads, one P x P output tile each),
-// warp 8 produces.  Stage st holds the column element's f block, its operator block and the
-// entry's dimension; full[st] completes when the bulk copies land (transaction count),
-// empty[st] when all 8 consumer warps are done reading it.  The natural output tile of a
-// thread spans dimensions (d-3, d-1), so consecutive threads sit 16 bytes apart in shared
-// memory; terms on dimensions d-3 and d-1 accumulate straight into it, the others through
-// one shared-memory transpose per term group.
+// warp 8 produces.  Stage st holds the column element's f block and its operator block;
+// full[st] completes when both bulk copies land (transaction count), empty[st] when all 8
+// consumer warps have released it.  A consumer releases a stage one entry late, so at a term
+// group boundary the stage just consumed doubles as the transpose buffer (no separate
+// scratch).  The natural output tile of a thread spans dimensions (d-3, d-1): consecutive
+// threads sit 16 bytes apart in shared memory; terms on dimensions d-3 and d-1 accumulate
+// straight into it, the others through the transpose.  FP32 blocks arrive pair-duplicated
+// (see the plan's FP32 packing) so the paired FMA needs no register shuffling; groups merge
+// into the output tile with Kahan compensation.  Rows launch longest first (row_order).
+struct F32Tile {
+  float2 v[4][2];  // [tile row][column pair]
+};
+
+// g[a][c] += sum_b A[a][b] x[b][c]; A column b arrives as (A0b,A0b,A1b,A1b),(A2b,A2b,A3b,A3b)
+__device__ __forceinline__ void f32_rows(F32Tile& g, const float* Ad, const float* xs, int s) {
+#pragma unroll
+  for (int b = 0; b < 4; ++b) {
+    const float4 x = *reinterpret_cast<const float4*>(xs + b * s);
+    const float4 q0 = *reinterpret_cast<const float4*>(Ad + b * 8);
+    const float4 q1 = *reinterpret_cast<const float4*>(Ad + b * 8 + 4);
+    const float2 x01 = make_float2(x.x, x.y), x23 = make_float2(x.z, x.w);
+    const float2 a0 = make_float2(q0.x, q0.y), a1 = make_float2(q0.z, q0.w);
+    const float2 a2 = make_float2(q1.x, q1.y), a3 = make_float2(q1.z, q1.w);
+    g.v[0][0] = ffma2(a0, x01, g.v[0][0]); g.v[0][1] = ffma2(a0, x23, g.v[0][1]);
+    g.v[1][0] = ffma2(a1, x01, g.v[1][0]); g.v[1][1] = ffma2(a1, x23, g.v[1][1]);
+    g.v[2][0] = ffma2(a2, x01, g.v[2][0]); g.v[2][1] = ffma2(a2, x23, g.v[2][1]);
+    g.v[3][0] = ffma2(a3, x01, g.v[3][0]); g.v[3][1] = ffma2(a3, x23, g.v[3][1]);
+  }
+}
+// g[r][a] += sum_b A[a][b] x[r][b]; A column b arrives as (A0b,A1b,A2b,A3b)
+__device__ __forceinline__ void f32_cols(F32Tile& g, const float* Ap, const float* xs, int s) {
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const float4 x = *reinterpret_cast<const float4*>(xs + r * s);
+    const float xv[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      const float4 q = *reinterpret_cast<const float4*>(Ap + b * 8);
+      const float2 xb = make_float2(xv[b], xv[b]);
+      g.v[r][0] = ffma2(make_float2(q.x, q.y), xb, g.v[r][0]);
+      g.v[r][1] = ffma2(make_float2(q.z, q.w), xb, g.v[r][1]);
+    }
+  }
+}
+__device__ __forceinline__ void kahan2(float2& s, float2& c, float2 v) {
+  float y = v.x - c.x, t = s.x + y;
+  c.x = (t - s.x) - y;
+  s.x = t;
+  y = v.y - c.y;
+  t = s.y + y;
+  c.y = (t - s.y) - y;
+  s.y = t;
+}
+
 template <typename T, int S, int MINB>
 __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
   constexpr int P = 4;
-  constexpr bool KAHAN = sizeof(T) == 4;
+  constexpr bool F32 = sizeof(T) == 4;
+  constexpr int AB = F32 ? 32 : 16;  // operator block values per stage
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_abort;
   const int tid = threadIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
   const int B = a.B, D = a.D;
-  const int SST = B + P * P;
+  const int SST = B + AB;
   T* stages = reinterpret_cast<T*>(smem_raw);
-  T* scratch = stages + S * SST;
-  uint64_t* full = reinterpret_cast<uint64_t*>(scratch + B);
+  uint64_t* full = reinterpret_cast<uint64_t*>(stages + S * SST);
   uint64_t* empty = full + S;
-  const int row = blockIdx.x;
+  const int row = a.row_order ? a.row_order[blockIdx.x] : blockIdx.x;
   const long long q0 = a.row_ptr[row];
   const int n = static_cast<int>(a.row_ptr[row + 1] - q0);
   const EntryDesc* ed = a.ed + q0;
-  const uint32_t fbytes = static_cast<uint32_t>(B * sizeof(T)), abytes = P * P * sizeof(T);
+  const uint32_t fbytes = static_cast<uint32_t>(B * sizeof(T)), abytes = AB * sizeof(T);
+  const T* opsrc = F32 ? reinterpret_cast<const T*>(a.ops_pair) : a.ops;
 
   if (tid == 0) {
     s_abort = 0;
@@ -552,11 +601,11 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
     mbar_fence_init();
   }
   __syncthreads();
-
   volatile int* abort_flag = &s_abort;
+
   if (warp == 8) {
     // ---------------- producer warp ----------------
-    int kdone = 0;  // entries whose copies were issued
+    int kdone = 0;
     bool stop = false;
     for (int k0 = 0; k0 < n && !stop; k0 += 32) {
       EntryDesc mine{};
@@ -579,7 +628,7 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
           fence_proxy_async();
           mbar_expect_tx(&full[st], fbytes + abytes);
           bulk_g2s(dst, a.f + static_cast<size_t>(j) * B, fbytes, &full[st]);
-          bulk_g2s(dst + B, a.ops + aoff, abytes, &full[st]);
+          bulk_g2s(dst + B, opsrc + aoff * (AB / 16), abytes, &full[st]);
         }
         kdone = k + 1;
         __syncwarp();
@@ -598,88 +647,134 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
   }
 
   // ---------------- consumer warps ----------------
-  T nat[P][P], natc[P][P], g[P][P];
-#pragma unroll
-  for (int r = 0; r < P; ++r)
-#pragma unroll
-    for (int c = 0; c < P; ++c) nat[r][c] = natc[r][c] = g[r][c] = T(0);
   int nat_base, nat_s;
   tile_place(tid, D - 3, D, a.stride, nat_base, nat_s);
-  int cur_m = -1, base_g = 0, s_g = 0;
+  int cur_m = -1, base_g = 0, s_g = 0, pend = -1;
   bool direct = false;
-  int mlane = -1;  // dimension of entry (k & ~31) + lane, prefetched per warp
+  int mlane = -1;
+  // FP32: paired state; FP64: scalar state
+  F32Tile g32, n32, c32;
+  T g[P][P], nat[P][P];
+#pragma unroll
+  for (int r = 0; r < P; ++r) {
+#pragma unroll
+    for (int cp = 0; cp < 2; ++cp) g32.v[r][cp] = n32.v[r][cp] = c32.v[r][cp] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int c = 0; c < P; ++c) g[r][c] = nat[r][c] = T(0);
+  }
   for (int k = 0; k <= n; ++k) {
     int m = -1;
     const int st = k % S;
     if (k < n) {
       if ((k & 31) == 0) mlane = (k + lane < n) ? ed[k + lane].m : -1;
-      // the dimension comes from the immutable descriptors, so consumer control flow (and
-      // every named barrier below) is uniform even after a timeout; later waits are skipped
+      // the dimension comes from the immutable descriptors: consumer control flow (and every
+      // named barrier below) is uniform even after a timeout; later waits are skipped
       m = __shfl_sync(0xffffffffu, mlane, k & 31);
       if (!*abort_flag && !mbar_wait_bounded(&full[st], static_cast<uint32_t>((k / S) & 1))) *abort_flag = 1;
     }
     if (m != cur_m) {
       if (direct) {
+        if constexpr (F32) {
 #pragma unroll
-        for (int r = 0; r < P; ++r)
+          for (int r = 0; r < P; ++r)
 #pragma unroll
-          for (int c = 0; c < P; ++c) acc_add(nat[r][c], natc[r][c], g[r][c], KAHAN);
+            for (int cp = 0; cp < 2; ++cp) kahan2(n32.v[r][cp], c32.v[r][cp], g32.v[r][cp]);
+        } else {
+#pragma unroll
+          for (int r = 0; r < P; ++r)
+#pragma unroll
+            for (int c = 0; c < P; ++c) nat[r][c] += g[r][c];
+        }
       } else if (cur_m >= 0) {
+        // transpose the group's sums onto the natural tiles through the stage just consumed
+        consumer_sync();
+        T* scr = stages + pend * SST;
 #pragma unroll
         for (int r = 0; r < P; ++r) {
-          Row<T, P> rr;
+          if constexpr (F32) {
+            *reinterpret_cast<float4*>(scr + base_g + r * s_g) =
+                make_float4(g32.v[r][0].x, g32.v[r][0].y, g32.v[r][1].x, g32.v[r][1].y);
+          } else {
+            Row<T, P> rr;
 #pragma unroll
-          for (int c = 0; c < P; ++c) rr.v[c] = g[r][c];
-          rr.store(scratch + base_g + r * s_g);
+            for (int c = 0; c < P; ++c) rr.v[c] = g[r][c];
+            rr.store(scr + base_g + r * s_g);
+          }
         }
         consumer_sync();
 #pragma unroll
         for (int r = 0; r < P; ++r) {
-          Row<T, P> rr;
-          rr.load(scratch + nat_base + r * nat_s);
+          if constexpr (F32) {
+            const float4 v = *reinterpret_cast<const float4*>(scr + nat_base + r * nat_s);
+            kahan2(n32.v[r][0], c32.v[r][0], make_float2(v.x, v.y));
+            kahan2(n32.v[r][1], c32.v[r][1], make_float2(v.z, v.w));
+          } else {
+            Row<T, P> rr;
+            rr.load(scr + nat_base + r * nat_s);
 #pragma unroll
-          for (int c = 0; c < P; ++c) acc_add(nat[r][c], natc[r][c], rr.v[c], KAHAN);
+            for (int c = 0; c < P; ++c) nat[r][c] += rr.v[c];
+          }
         }
-        consumer_sync();
       }
       cur_m = m;
-      if (m < 0) break;
+      if (m >= 0) {
 #pragma unroll
-      for (int r = 0; r < P; ++r)
+        for (int r = 0; r < P; ++r) {
 #pragma unroll
-        for (int c = 0; c < P; ++c) g[r][c] = T(0);
-      direct = (m == D - 1) || (m == D - 3);
-      if (m == D - 1) {
-        base_g = nat_base;
-        s_g = nat_s;
-      } else {
-        tile_place(tid, m, D, a.stride, base_g, s_g);
+          for (int cp = 0; cp < 2; ++cp) g32.v[r][cp] = make_float2(0.f, 0.f);
+#pragma unroll
+          for (int c = 0; c < P; ++c) g[r][c] = T(0);
+        }
+        direct = (m == D - 1) || (m == D - 3);
+        if (m == D - 1) {
+          base_g = nat_base;
+          s_g = nat_s;
+        } else {
+          tile_place(tid, m, D, a.stride, base_g, s_g);
+        }
       }
     }
-    const T* sp = stages + st * SST;
-    T A[P * P];
-#pragma unroll
-    for (int r = 0; r < P; ++r) {
-      Row<T, P> rr;
-      rr.load(sp + B + r * P);
-#pragma unroll
-      for (int c = 0; c < P; ++c) A[r * P + c] = rr.v[c];
+    if (pend >= 0) {
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[pend]);
+      pend = -1;
     }
-    if (m == D - 1)
-      tile_cols_s<T>(g, A, sp + base_g, s_g);
-    else
-      tile_rows<T>(g, A, sp + base_g, s_g);
-    __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[st]);
+    if (m < 0) break;
+    const T* sp = stages + st * SST;
+    if constexpr (F32) {
+      if (m == D - 1)
+        f32_cols(g32, reinterpret_cast<const float*>(sp + B), reinterpret_cast<const float*>(sp + base_g), s_g);
+      else
+        f32_rows(g32, reinterpret_cast<const float*>(sp + B), reinterpret_cast<const float*>(sp + base_g), s_g);
+    } else {
+      T A[P * P];
+#pragma unroll
+      for (int r = 0; r < P; ++r) {
+        Row<T, P> rr;
+        rr.load(sp + B + r * P);
+#pragma unroll
+        for (int c = 0; c < P; ++c) A[r * P + c] = rr.v[c];
+      }
+      if (m == D - 1)
+        tile_cols_s<T>(g, A, sp + base_g, s_g);
+      else
+        tile_rows<T>(g, A, sp + base_g, s_g);
+    }
+    pend = st;
   }
   if (*abort_flag) return;  // y is undefined; the plan's status word reports the timeout
   T* yr = a.y + static_cast<size_t>(row) * B + nat_base;
 #pragma unroll
   for (int r = 0; r < P; ++r) {
-    Row<T, P> rr;
+    if constexpr (F32) {
+      *reinterpret_cast<float4*>(reinterpret_cast<float*>(yr) + r * nat_s) =
+          make_float4(n32.v[r][0].x, n32.v[r][0].y, n32.v[r][1].x, n32.v[r][1].y);
+    } else {
+      Row<T, P> rr;
 #pragma unroll
-    for (int c = 0; c < P; ++c) rr.v[c] = nat[r][c];
-    rr.store(yr + r * nat_s);
+      for (int c = 0; c < P; ++c) rr.v[c] = nat[r][c];
+      rr.store(yr + r * nat_s);
+    }
   }
 }
 
@@ -719,12 +814,23 @@ cudaError_t launch_p(const ApplyArgs<T>& a, int kind, cudaStream_t s) {
     return cudaGetLastError();
   }
   if constexpr (P == 4) {
-    if (kind == KK_SINGLE_TMA) {
+    if (kind == KK_SINGLE_TMA || kind == KK_SINGLE_TMA3) {
+      // FP32: 4 stages, 2 or 3 CTAs per SM (kind 3 / kind 4); FP64: 3 stages, 1 CTA per SM
       constexpr int S = sizeof(T) == 4 ? 4 : 3;
-      constexpr int MINB = sizeof(T) == 4 ? 2 : 1;
       if (a.B != 256 * P * P) return cudaErrorInvalidValue;  // 8 consumer warps own one tile each
-      const size_t sm = (static_cast<size_t>(S) * (a.B + P * P) + a.B) * sizeof(T) + 2 * S * sizeof(uint64_t);
-      auto kern = k_single_tma<T, S, MINB>;
+      if (sizeof(T) == 4 && !a.ops_pair) return cudaErrorInvalidValue;
+      const size_t sm = static_cast<size_t>(S) * (a.B + (sizeof(T) == 4 ? 32 : 16)) * sizeof(T) + 2 * S * sizeof(uint64_t);
+      if constexpr (sizeof(T) == 4) {
+        if (kind == KK_SINGLE_TMA3) {
+          auto kern = k_single_tma<T, S, 3>;
+          static bool done = false;
+          cudaError_t e = ensure_smem(kern, sm, sm, done);
+          if (e != cudaSuccess) return e;
+          kern<<<a.N, 288, sm, s>>>(a);
+          return cudaGetLastError();
+        }
+      }
+      auto kern = k_single_tma<T, S, sizeof(T) == 4 ? 2 : 1>;
       static bool done = false;
       cudaError_t e = ensure_smem(kern, sm, sm, done);
       if (e != cudaSuccess) return e;

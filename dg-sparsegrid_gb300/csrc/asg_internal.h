@@ -50,13 +50,15 @@ struct ApplyArgs {
   int N, D, B, nterms;
   int stride[kMaxDims];      // deg^(D-1-m): element-block stride of dimension m
   const EntryDesc* ed;       // [entries] single-mode descriptors (NULL for chain plans)
+  const float* ops_pair;     // FP32 blocks in paired-FMA order (32 values per block), single-mode plans
+  const int* row_order;      // [N] launch order of rows (longest work first) or NULL
   int* err;                  // device status word (ASG_ERR_TIMEOUT after a bounded wait gave up)
 };
 
 template <typename T>
 cudaError_t launch_apply(const ApplyArgs<T>& a, int P, int kernel_kind, cudaStream_t s);
 
-enum KernelKind { KK_CHAIN_WARP = 0, KK_CHAIN_CTA = 1, KK_SINGLE_MODE = 2, KK_SINGLE_TMA = 3 };
+enum KernelKind { KK_CHAIN_WARP = 0, KK_CHAIN_CTA = 1, KK_SINGLE_MODE = 2, KK_SINGLE_TMA = 3, KK_SINGLE_TMA3 = 4 };
 
 }  // namespace asg
 
@@ -89,6 +91,9 @@ struct asg_plan {
   int* d_tr_ent = nullptr;
   std::vector<asg::EntryDesc> ed;   // single-mode descriptors (empty unless every term has one factor)
   asg::EntryDesc* d_ed = nullptr;
+  std::vector<int> row_order;
+  int* d_row_order = nullptr;
+  float* d_ops_pair = nullptr;
   int* d_err = nullptr;
   double* d_ops64 = nullptr;
   float* d_ops32 = nullptr;

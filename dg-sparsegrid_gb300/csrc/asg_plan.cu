@@ -1,6 +1,7 @@
 // Plan creation, structure analysis, work-list construction and the apply entry points of
 // the C ABI.  Host-side code (compiled by nvcc for the runtime API); the kernels live in
 // asg_apply.cu.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -49,6 +50,8 @@ void free_device(asg_plan* p) {
   cudaFree(p->d_ops64);
   cudaFree(p->d_ops32);
   cudaFree(p->d_ed);
+  cudaFree(p->d_row_order);
+  cudaFree(p->d_ops_pair);
   cudaFree(p->d_err);
   cudaFree(p->d_io);
   if (p->stream) cudaStreamDestroy(p->stream);
@@ -77,6 +80,33 @@ asg_status pack_and_upload(asg_plan* p, const double* const* ops, const int* op_
     }
   std::vector<float> h32(h64.size());
   for (size_t i = 0; i < h64.size(); ++i) h32[i] = static_cast<float>(h64[i]);
+  if (!p->ed.empty() && p->P == 4) {
+    // FP32 blocks for the paired FMA (fma.rn.f32x2): per column b, 8 values.  Blocks used on
+    // the last dimension hold (A0b,A1b,A2b,A3b) + padding, all others the duplicated pairs
+    // (A0b,A0b,A1b,A1b,A2b,A2b,A3b,A3b).  Block k of a packed operator sits at 32*k.
+    std::vector<float> pr(h64.size() * 2, 0.f);
+    for (int t = 0; t < p->T; ++t)
+      for (int m = 0; m < p->D; ++m) {
+        const int tm = t * p->D + m;
+        if (p->op_off[tm] < 0) continue;
+        const long long nblk = static_cast<long long>(p->op_nb[tm]) * p->op_nb[tm];
+        for (long long k = 0; k < nblk; ++k) {
+          const double* A = h64.data() + p->op_off[tm] + k * 16;
+          float* d = pr.data() + (p->op_off[tm] + k * 16) * 2;
+          for (int b = 0; b < 4; ++b)
+            for (int r = 0; r < 4; ++r) {
+              if (m == p->D - 1) {
+                d[b * 8 + r] = static_cast<float>(A[r * 4 + b]);
+              } else {
+                d[b * 8 + 2 * r] = static_cast<float>(A[r * 4 + b]);
+                d[b * 8 + 2 * r + 1] = static_cast<float>(A[r * 4 + b]);
+              }
+            }
+        }
+      }
+    if (!p->d_ops_pair) ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_ops_pair), pr.size() * sizeof(float)));
+    ASG_CUDA(cudaMemcpy(p->d_ops_pair, pr.data(), pr.size() * sizeof(float), cudaMemcpyHostToDevice));
+  }
   if (!p->d_ops64 && !h64.empty()) {
     ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_ops64), h64.size() * sizeof(double)));
     ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_ops32), h32.size() * sizeof(float)));
@@ -106,6 +136,8 @@ ApplyArgs<T> make_args(const asg_plan* p, const T* f, T* y, const T* ops) {
   a.nterms = p->T;
   a.ed = p->d_ed;
   a.err = p->d_err;
+  a.ops_pair = p->d_ops_pair;
+  a.row_order = p->d_row_order;
   int s = 1;
   for (int m = p->D - 1; m >= 0; --m) {
     a.stride[m] = s;
@@ -367,6 +399,12 @@ asg_status asg_plan_create(const asg_plan_desc* desc, asg_plan** out) {
     }
   p->packed_elems = off;
   if (single) {
+    // rows launch longest first so the last wave is made of short rows
+    p->row_order.resize(N);
+    for (int i = 0; i < N; ++i) p->row_order[i] = i;
+    std::stable_sort(p->row_order.begin(), p->row_order.end(), [&](int x, int y) {
+      return p->row_ptr[x + 1] - p->row_ptr[x] > p->row_ptr[y + 1] - p->row_ptr[y];
+    });
     // per-entry descriptors of the single-mode kernels: column, dimension, block offset
     p->ed.resize(ent.size());
     for (int i = 0; i < N; ++i)
@@ -381,6 +419,7 @@ asg_status asg_plan_create(const asg_plan_desc* desc, asg_plan** out) {
       }
   }
   asg_status st;
+  if ((st = asg::upload(&p->d_row_order, p->row_order))) return bail(st);
   if ((st = asg::pack_and_upload(p, desc->ops, desc->op_ld))) return bail(st);
   if ((st = asg::upload(&p->d_idx1d, p->idx1d))) return bail(st);
   if ((st = asg::upload(&p->d_op_nb, p->op_nb))) return bail(st);
@@ -434,14 +473,14 @@ asg_status asg_plan_update_ops(asg_plan* p, const double* const* ops, const int*
 asg_status asg_plan_set_kernel(asg_plan* p, int kind) {
   if (!p) return fail(ASG_ERR_INVALID, "plan_set_kernel: NULL plan");
   if (kind == asg::KK_CHAIN_WARP && p->B > 256) return fail(ASG_ERR_UNSUPPORTED, "warp chain kernel needs deg^d <= 256");
-  if (kind == asg::KK_SINGLE_MODE || kind == asg::KK_SINGLE_TMA) {
-    bool ok = kind == asg::KK_SINGLE_TMA ? (p->P == 4 && p->B == 4096)
+  if (kind == asg::KK_SINGLE_MODE || kind == asg::KK_SINGLE_TMA || kind == asg::KK_SINGLE_TMA3) {
+    bool ok = kind != asg::KK_SINGLE_MODE ? (p->P == 4 && p->B == 4096)
                                          : ((p->P == 3 || p->P == 4) && p->B >= 32 * p->P * p->P);
     for (unsigned a : p->active) ok = ok && __builtin_popcount(a) == 1;
     if (!ok || p->ed.size() != p->ent.size())
       return fail(ASG_ERR_UNSUPPORTED, "single-mode kernels need one non-identity factor per term (deg 3/4)");
   }
-  if (kind < 0 || kind > 3) return fail(ASG_ERR_INVALID, "unknown kernel kind %d", kind);
+  if (kind < 0 || kind > 4) return fail(ASG_ERR_INVALID, "unknown kernel kind %d", kind);
   p->kernel_kind = kind;
   return ASG_OK;
 }

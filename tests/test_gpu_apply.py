@@ -115,9 +115,11 @@ def test_continuity6_lev4_deg4_kernels_agree(dev):
     y32 = _apply(p, f, dev, torch.float32)
     assert p.device_status() == 0
     assert rel2(y32, y_single) <= FP32_TOL
-    p.set_kernel(asgkron._lib.KERNEL_SINGLE_MODE)
-    assert rel2(_apply(p, f, dev), y_single) <= FP64_TOL
-    assert rel2(_apply(p, f, dev, torch.float32), y_single) <= FP32_TOL
+    for kind in (asgkron._lib.KERNEL_SINGLE_TMA3, asgkron._lib.KERNEL_SINGLE_MODE):
+        p.set_kernel(kind)
+        assert rel2(_apply(p, f, dev), y_single) <= FP64_TOL
+        assert rel2(_apply(p, f, dev, torch.float32), y_single) <= FP32_TOL
+        assert p.device_status() == 0
     p.set_kernel(asgkron._lib.KERNEL_CHAIN_CTA)
     y_chain = _apply(p, f, dev)
     assert rel2(y_chain, y_single) <= FP64_TOL
