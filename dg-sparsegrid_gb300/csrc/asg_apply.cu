@@ -424,14 +424,8 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
   return true;
 }
 
-__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) {
-  unsigned long long d;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;"
-      : "=l"(d)
-      : "l"(*reinterpret_cast<unsigned long long*>(&a)), "l"(*reinterpret_cast<unsigned long long*>(&b)),
-        "l"(*reinterpret_cast<unsigned long long*>(&c)));
-  return *reinterpret_cast<float2*>(&d);
-}
+// Paired FP32 FMA (fma.rn.f32x2): two FMAs per instruction issue.
+__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
 
 // g[a][c] += sum_b A[a][b] * x[b][c]   (contraction across the tile rows)
 template <typename T>
@@ -650,7 +644,7 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
   int nat_base, nat_s;
   tile_place(tid, D - 3, D, a.stride, nat_base, nat_s);
   int cur_m = -1, base_g = 0, s_g = 0, pend = -1;
-  bool direct = false;
+  bool direct = false, gave_up = false;
   int mlane = -1;
   // FP32: paired state; FP64: scalar state
   F32Tile g32, n32, c32;
@@ -670,7 +664,10 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
       // the dimension comes from the immutable descriptors: consumer control flow (and every
       // named barrier below) is uniform even after a timeout; later waits are skipped
       m = __shfl_sync(0xffffffffu, mlane, k & 31);
-      if (!*abort_flag && !mbar_wait_bounded(&full[st], static_cast<uint32_t>((k / S) & 1))) *abort_flag = 1;
+      if (!gave_up && !mbar_wait_bounded(&full[st], static_cast<uint32_t>((k / S) & 1))) {
+        gave_up = true;  // this thread skips its later waits; the CTA reports the timeout
+        *abort_flag = 1;
+      }
     }
     if (m != cur_m) {
       if (direct) {
