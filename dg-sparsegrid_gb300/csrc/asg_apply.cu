@@ -664,9 +664,15 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
       // the dimension comes from the immutable descriptors: consumer control flow (and every
       // named barrier below) is uniform even after a timeout; later waits are skipped
       m = __shfl_sync(0xffffffffu, mlane, k & 31);
-      if (!gave_up && !mbar_wait_bounded(&full[st], static_cast<uint32_t>((k / S) & 1))) {
-        gave_up = true;  // this thread skips its later waits; the CTA reports the timeout
-        *abort_flag = 1;
+      if (!gave_up) {
+        const bool ok = mbar_wait_bounded(&full[st], static_cast<uint32_t>((k / S) & 1));
+        // a warp that gave up on a stage never releases a stage again: the producer then
+        // cannot re-arm a stage whose copy may still be in flight; its own bounded wait on
+        // the empty barrier expires and it waits for its issued copies before exiting
+        if (!__all_sync(0xffffffffu, ok)) {
+          gave_up = true;
+          *abort_flag = 1;
+        }
       }
     }
     if (m != cur_m) {
@@ -733,7 +739,7 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
     }
     if (pend >= 0) {
       __syncwarp();
-      if (lane == 0) mbar_arrive(&empty[pend]);
+      if (lane == 0 && !gave_up) mbar_arrive(&empty[pend]);
       pend = -1;
     }
     if (m < 0) break;
