@@ -577,7 +577,9 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
   const int B = a.B, D = a.D;
   const int SST = B + AB;
   T* stages = reinterpret_cast<T*>(smem_raw);
-  uint64_t* full = reinterpret_cast<uint64_t*>(stages + S * SST);
+  // FP32: the Kahan compensation of the output tiles lives in shared memory (B values)
+  float* comp = reinterpret_cast<float*>(stages + S * SST);
+  uint64_t* full = reinterpret_cast<uint64_t*>(comp + (F32 ? B : 0));
   uint64_t* empty = full + S;
   const int row = a.row_order ? a.row_order[blockIdx.x] : blockIdx.x;
   const long long q0 = a.row_ptr[row];
@@ -646,15 +648,16 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
   int cur_m = -1, base_g = 0, s_g = 0, pend = -1;
   bool direct = false, gave_up = false;
   int mlane = -1;
-  // FP32: paired state; FP64: scalar state
-  F32Tile g32, n32, c32;
+  // FP32: paired state (compensation in shared memory); FP64: scalar state
+  F32Tile g32, n32;
   T g[P][P], nat[P][P];
 #pragma unroll
   for (int r = 0; r < P; ++r) {
 #pragma unroll
-    for (int cp = 0; cp < 2; ++cp) g32.v[r][cp] = n32.v[r][cp] = c32.v[r][cp] = make_float2(0.f, 0.f);
+    for (int cp = 0; cp < 2; ++cp) g32.v[r][cp] = n32.v[r][cp] = make_float2(0.f, 0.f);
 #pragma unroll
     for (int c = 0; c < P; ++c) g[r][c] = nat[r][c] = T(0);
+    if constexpr (F32) *reinterpret_cast<float4*>(comp + nat_base + r * nat_s) = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   for (int k = 0; k <= n; ++k) {
     int m = -1;
@@ -679,9 +682,14 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
       if (direct) {
         if constexpr (F32) {
 #pragma unroll
-          for (int r = 0; r < P; ++r)
-#pragma unroll
-            for (int cp = 0; cp < 2; ++cp) kahan2(n32.v[r][cp], c32.v[r][cp], g32.v[r][cp]);
+          for (int r = 0; r < P; ++r) {
+            float4* cq = reinterpret_cast<float4*>(comp + nat_base + r * nat_s);
+            const float4 c4 = *cq;
+            float2 c0 = make_float2(c4.x, c4.y), c1 = make_float2(c4.z, c4.w);
+            kahan2(n32.v[r][0], c0, g32.v[r][0]);
+            kahan2(n32.v[r][1], c1, g32.v[r][1]);
+            *cq = make_float4(c0.x, c0.y, c1.x, c1.y);
+          }
         } else {
 #pragma unroll
           for (int r = 0; r < P; ++r)
@@ -709,8 +717,12 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
         for (int r = 0; r < P; ++r) {
           if constexpr (F32) {
             const float4 v = *reinterpret_cast<const float4*>(scr + nat_base + r * nat_s);
-            kahan2(n32.v[r][0], c32.v[r][0], make_float2(v.x, v.y));
-            kahan2(n32.v[r][1], c32.v[r][1], make_float2(v.z, v.w));
+            float4* cq = reinterpret_cast<float4*>(comp + nat_base + r * nat_s);
+            const float4 c4 = *cq;
+            float2 c0 = make_float2(c4.x, c4.y), c1 = make_float2(c4.z, c4.w);
+            kahan2(n32.v[r][0], c0, make_float2(v.x, v.y));
+            kahan2(n32.v[r][1], c1, make_float2(v.z, v.w));
+            *cq = make_float4(c0.x, c0.y, c1.x, c1.y);
           } else {
             Row<T, P> rr;
             rr.load(scr + nat_base + r * nat_s);
@@ -819,13 +831,18 @@ cudaError_t launch_p(const ApplyArgs<T>& a, int kind, cudaStream_t s) {
   if constexpr (P == 4) {
     if (kind == KK_SINGLE_TMA || kind == KK_SINGLE_TMA3) {
       // FP32: 4 stages, 2 or 3 CTAs per SM (kind 3 / kind 4); FP64: 3 stages, 1 CTA per SM
-      constexpr int S = sizeof(T) == 4 ? 4 : 3;
+      // FP32: 3 stages + compensation tile (3 CTAs per SM), or 4 stages (2 per SM, kind 4);
+      // FP64: 3 stages, 1 CTA per SM
       if (a.B != 256 * P * P) return cudaErrorInvalidValue;  // 8 consumer warps own one tile each
       if (sizeof(T) == 4 && !a.ops_pair) return cudaErrorInvalidValue;
-      const size_t sm = static_cast<size_t>(S) * (a.B + (sizeof(T) == 4 ? 32 : 16)) * sizeof(T) + 2 * S * sizeof(uint64_t);
+      auto smem_for = [&](int S) {
+        return static_cast<size_t>(S) * (a.B + (sizeof(T) == 4 ? 32 : 16)) * sizeof(T) +
+               (sizeof(T) == 4 ? a.B * sizeof(float) : 0) + 2 * S * sizeof(uint64_t);
+      };
       if constexpr (sizeof(T) == 4) {
         if (kind == KK_SINGLE_TMA3) {
-          auto kern = k_single_tma<T, S, 3>;
+          const size_t sm = smem_for(4);
+          auto kern = k_single_tma<T, 4, 2>;
           static bool done = false;
           cudaError_t e = ensure_smem(kern, sm, sm, done);
           if (e != cudaSuccess) return e;
@@ -833,7 +850,8 @@ cudaError_t launch_p(const ApplyArgs<T>& a, int kind, cudaStream_t s) {
           return cudaGetLastError();
         }
       }
-      auto kern = k_single_tma<T, S, sizeof(T) == 4 ? 2 : 1>;
+      const size_t sm = smem_for(3);
+      auto kern = k_single_tma<T, 3, sizeof(T) == 4 ? 3 : 1>;
       static bool done = false;
       cudaError_t e = ensure_smem(kern, sm, sm, done);
       if (e != cudaSuccess) return e;
