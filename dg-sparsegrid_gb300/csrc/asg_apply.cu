@@ -565,10 +565,11 @@ __device__ __forceinline__ void kahan2(float2& s, float2& c, float2 v) {
   s.y = t;
 }
 
-template <typename T, int S, int MINB>
+template <typename T, int S, int MINB, bool CSMEM>
 __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
   constexpr int P = 4;
   constexpr bool F32 = sizeof(T) == 4;
+  constexpr bool CS = F32 && CSMEM;  // FP32 compensation tile in shared memory (else registers)
   constexpr int AB = F32 ? 32 : 16;  // operator block values per stage
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_abort;
@@ -579,7 +580,7 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
   T* stages = reinterpret_cast<T*>(smem_raw);
   // FP32: the Kahan compensation of the output tiles lives in shared memory (B values)
   float* comp = reinterpret_cast<float*>(stages + S * SST);
-  uint64_t* full = reinterpret_cast<uint64_t*>(comp + (F32 ? B : 0));
+  uint64_t* full = reinterpret_cast<uint64_t*>(comp + (CS ? B : 0));
   uint64_t* empty = full + S;
   const int row = a.row_order ? a.row_order[blockIdx.x] : blockIdx.x;
   const long long q0 = a.row_ptr[row];
@@ -648,17 +649,31 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
   int cur_m = -1, base_g = 0, s_g = 0, pend = -1;
   bool direct = false, gave_up = false;
   int mlane = -1;
-  // FP32: paired state (compensation in shared memory); FP64: scalar state
-  F32Tile g32, n32;
+  // FP32: paired state, compensation in registers or shared memory; FP64: scalar state
+  F32Tile g32, n32, c32;
   T g[P][P], nat[P][P];
 #pragma unroll
   for (int r = 0; r < P; ++r) {
 #pragma unroll
-    for (int cp = 0; cp < 2; ++cp) g32.v[r][cp] = n32.v[r][cp] = make_float2(0.f, 0.f);
+    for (int cp = 0; cp < 2; ++cp) g32.v[r][cp] = n32.v[r][cp] = c32.v[r][cp] = make_float2(0.f, 0.f);
 #pragma unroll
     for (int c = 0; c < P; ++c) g[r][c] = nat[r][c] = T(0);
-    if constexpr (F32) *reinterpret_cast<float4*>(comp + nat_base + r * nat_s) = make_float4(0.f, 0.f, 0.f, 0.f);
+    if constexpr (CS) *reinterpret_cast<float4*>(comp + nat_base + r * nat_s) = make_float4(0.f, 0.f, 0.f, 0.f);
   }
+  // Kahan-merge a tile row pair into the output tile (compensation where this variant keeps it)
+  auto merge_row = [&](int r, float2 v0, float2 v1) {
+    if constexpr (CS) {
+      float4* cq = reinterpret_cast<float4*>(comp + nat_base + r * nat_s);
+      const float4 c4 = *cq;
+      float2 c0 = make_float2(c4.x, c4.y), c1 = make_float2(c4.z, c4.w);
+      kahan2(n32.v[r][0], c0, v0);
+      kahan2(n32.v[r][1], c1, v1);
+      *cq = make_float4(c0.x, c0.y, c1.x, c1.y);
+    } else {
+      kahan2(n32.v[r][0], c32.v[r][0], v0);
+      kahan2(n32.v[r][1], c32.v[r][1], v1);
+    }
+  };
   for (int k = 0; k <= n; ++k) {
     int m = -1;
     const int st = k % S;
@@ -682,14 +697,7 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
       if (direct) {
         if constexpr (F32) {
 #pragma unroll
-          for (int r = 0; r < P; ++r) {
-            float4* cq = reinterpret_cast<float4*>(comp + nat_base + r * nat_s);
-            const float4 c4 = *cq;
-            float2 c0 = make_float2(c4.x, c4.y), c1 = make_float2(c4.z, c4.w);
-            kahan2(n32.v[r][0], c0, g32.v[r][0]);
-            kahan2(n32.v[r][1], c1, g32.v[r][1]);
-            *cq = make_float4(c0.x, c0.y, c1.x, c1.y);
-          }
+          for (int r = 0; r < P; ++r) merge_row(r, g32.v[r][0], g32.v[r][1]);
         } else {
 #pragma unroll
           for (int r = 0; r < P; ++r)
@@ -717,12 +725,7 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
         for (int r = 0; r < P; ++r) {
           if constexpr (F32) {
             const float4 v = *reinterpret_cast<const float4*>(scr + nat_base + r * nat_s);
-            float4* cq = reinterpret_cast<float4*>(comp + nat_base + r * nat_s);
-            const float4 c4 = *cq;
-            float2 c0 = make_float2(c4.x, c4.y), c1 = make_float2(c4.z, c4.w);
-            kahan2(n32.v[r][0], c0, make_float2(v.x, v.y));
-            kahan2(n32.v[r][1], c1, make_float2(v.z, v.w));
-            *cq = make_float4(c0.x, c0.y, c1.x, c1.y);
+            merge_row(r, make_float2(v.x, v.y), make_float2(v.z, v.w));
           } else {
             Row<T, P> rr;
             rr.load(scr + nat_base + r * nat_s);
@@ -835,14 +838,14 @@ cudaError_t launch_p(const ApplyArgs<T>& a, int kind, cudaStream_t s) {
       // FP64: 3 stages, 1 CTA per SM
       if (a.B != 256 * P * P) return cudaErrorInvalidValue;  // 8 consumer warps own one tile each
       if (sizeof(T) == 4 && !a.ops_pair) return cudaErrorInvalidValue;
-      auto smem_for = [&](int S) {
+      auto smem_for = [&](int S, bool csmem) {
         return static_cast<size_t>(S) * (a.B + (sizeof(T) == 4 ? 32 : 16)) * sizeof(T) +
-               (sizeof(T) == 4 ? a.B * sizeof(float) : 0) + 2 * S * sizeof(uint64_t);
+               (csmem ? a.B * sizeof(float) : 0) + 2 * S * sizeof(uint64_t);
       };
       if constexpr (sizeof(T) == 4) {
         if (kind == KK_SINGLE_TMA3) {
-          const size_t sm = smem_for(4);
-          auto kern = k_single_tma<T, 4, 2>;
+          const size_t sm = smem_for(3, true);
+          auto kern = k_single_tma<T, 3, 3, true>;
           static bool done = false;
           cudaError_t e = ensure_smem(kern, sm, sm, done);
           if (e != cudaSuccess) return e;
@@ -850,8 +853,9 @@ cudaError_t launch_p(const ApplyArgs<T>& a, int kind, cudaStream_t s) {
           return cudaGetLastError();
         }
       }
-      const size_t sm = smem_for(3);
-      auto kern = k_single_tma<T, 3, sizeof(T) == 4 ? 3 : 1>;
+      constexpr int S0 = sizeof(T) == 4 ? 4 : 3;
+      const size_t sm = smem_for(S0, false);
+      auto kern = k_single_tma<T, S0, sizeof(T) == 4 ? 2 : 1, false>;
       static bool done = false;
       cudaError_t e = ensure_smem(kern, sm, sm, done);
       if (e != cudaSuccess) return e;

@@ -96,8 +96,9 @@ asg_status asg_plan_update_ops(asg_plan* plan, const double* const* ops, const i
 
 /* Force a kernel family for this plan: 0 warp chain (deg^d <= 256), 1 CTA chain,
  * 2 single-mode fiber kernel with direct loads, 3 single-mode fiber kernel with TMA bulk
- * copies (3 stages, 3 CTAs per SM), 4 the same with 4 stages and 2 CTAs per SM (2-4 need one
- * non-identity factor per term; 3-4 need deg 4, d 6).  The default is chosen by asg_plan_create; this exists
+ * copies (4 stages, 2 CTAs per SM), 4 the same with 3 stages, the FP32 compensation tile in
+ * shared memory and 3 CTAs per SM (2-4 need one non-identity factor per term; 3-4 need deg 4,
+ * d 6).  The default is chosen by asg_plan_create; this exists
  * for testing one family against another and for launch-shape tuning. */
 asg_status asg_plan_set_kernel(asg_plan* plan, int kind);
 /* Synchronises and reads the plan's device status word: ASG_OK, or ASG_ERR_TIMEOUT when a
