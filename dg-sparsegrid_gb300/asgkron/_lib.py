@@ -62,6 +62,19 @@ class PlanStats(C.Structure):
     ]
 
 
+class GemmDesc(C.Structure):
+    _fields_ = [
+        ("level", C.c_int), ("m", C.c_int), ("n", C.c_int), ("k", C.c_int),
+        ("trans_a", C.c_char), ("trans_b", C.c_char), ("alpha", C.c_double), ("beta", C.c_double),
+        ("a_operand", C.c_int), ("b_operand", C.c_int), ("c_operand", C.c_int),
+        ("a_offset", C.c_longlong), ("b_offset", C.c_longlong), ("c_offset", C.c_longlong),
+        ("lda", C.c_int), ("ldb", C.c_int), ("ldc", C.c_int),
+    ]
+
+
+_P = C.c_void_p
+_I = C.POINTER(C.c_int)
+
 # name -> (restype, argtypes); every symbol include/asgkron.h declares
 SIGNATURES = {
     "asg_version": (C.c_char_p, []),
@@ -86,6 +99,17 @@ SIGNATURES = {
     "asg_connect_nd": (C.c_int, [C.c_int, C.c_longlong, C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_int, C.c_int,
                                  C.c_int, C.POINTER(C.c_longlong), C.POINTER(C.c_int), C.c_longlong,
                                  C.POINTER(C.c_longlong)]),
+    "asg_gemm_vbatched_f64": (C.c_int, [C.c_char, C.c_char, _P, _P, _P, C.c_double, _P, _P, _P, _P, C.c_double, _P, _P,
+                                        C.c_int, _P]),
+    "asg_gemm_vbatched_f32": (C.c_int, [C.c_char, C.c_char, _P, _P, _P, C.c_float, _P, _P, _P, _P, C.c_float, _P, _P,
+                                        C.c_int, _P]),
+    "asg_kron_plan_create": (C.c_int, [C.c_int, _I, _I, C.c_longlong, C.POINTER(C.c_void_p)]),
+    "asg_kron_plan_destroy": (C.c_int, [C.c_void_p]),
+    "asg_kron_plan_workspace": (C.c_int, [C.c_void_p, C.POINTER(C.c_size_t), C.POINTER(C.c_size_t)]),
+    "asg_kron_plan_lists": (C.c_int, [C.c_void_p, C.POINTER(GemmDesc), C.c_int, _I]),
+    "asg_kron_batch_f64": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), _P, _P, _P, C.c_size_t, _P]),
+    "asg_kron_batch_f32": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), _P, _P, _P, C.c_size_t, _P]),
+    "asg_krond_f64": (C.c_int, [C.c_int, _I, _I, C.POINTER(C.c_void_p), _P, _P]),
 }
 
 _LIB = None

@@ -140,6 +140,58 @@ asg_status asg_connect_nd(int num_dims, long long num_elems, const int* levels, 
                           int levsum, int levmax, int grid, long long* row_ptr, int* cols,
                           long long capacity, long long* num_pairs);
 
+/* ---------------------------------------------------------------------------------------
+ * Kronecker products and batched small GEMMs (Kronmult/)
+ * All matrices are column-major; pointer arguments are device pointers unless stated.
+ * ------------------------------------------------------------------------------------- */
+/* C_i = alpha*op(A_i)*op(B_i) + beta*C_i for a batch of independent small GEMMs with their own
+ * sizes (Kronmult/gemm_vbatched.m:1-44, the MAGMA magmablas_dgemm_vbatched convention: every
+ * array -- sizes, leading dimensions and the pointer arrays -- lives in device memory; one
+ * transA/transB/alpha/beta for the whole batch).  k is read from k[] (the reference reads
+ * nlist at gemm_vbatched.m:25; that is a bug, not reproduced here). */
+asg_status asg_gemm_vbatched_f64(char trans_a, char trans_b, const int* m, const int* n, const int* k, double alpha,
+                                 const double* const* A, const int* lda, const double* const* B, const int* ldb,
+                                 double beta, double* const* C, const int* ldc, int batch, void* stream);
+asg_status asg_gemm_vbatched_f32(char trans_a, char trans_b, const int* m, const int* n, const int* k, float alpha,
+                                 const float* const* A, const int* lda, const float* const* B, const int* ldb,
+                                 float beta, float* const* C, const int* ldc, int batch, void* stream);
+
+/* One recorded GEMM of the kronmultN_batch lists (the fields of batch_list{level} entries,
+ * Kronmult/kronmult2_batch.m:86-110).  Operands: 0..nkron-1 the factors A1..An, nkron = X,
+ * nkron+1 = Y, nkron+2 = the workspace (the recursion's temporaries); offsets are element
+ * offsets into them. */
+typedef struct {
+  int level;                   /* 1-based batch list the reference appends to */
+  int m, n, k;
+  char trans_a, trans_b;
+  double alpha, beta;          /* always 1 and 0 in the reference */
+  int a_operand, b_operand, c_operand;
+  long long a_offset, b_offset, c_offset;
+  int lda, ldb, ldc;
+} asg_gemm_desc;
+
+typedef struct asg_kron_plan asg_kron_plan;
+/* Plans Y = kron(A1,...,An) * X for X with nvec columns the way kronmultN_batch.m does
+ * (Kronmult/kronmult{1..6}_batch.m, method chosen per level by flops_kron{n}.m): the GEMMs
+ * go into per-level lists executed level by level, each level one batched launch.  Planning
+ * is host-only; the descriptor table moves to the device on the first execution. */
+asg_status asg_kron_plan_create(int nkron, const int* nrow, const int* ncol, long long nvec, asg_kron_plan** plan);
+asg_status asg_kron_plan_destroy(asg_kron_plan* plan);
+/* Workspace (the recursion's Ytmp buffers) the executor needs, per precision. */
+asg_status asg_kron_plan_workspace(const asg_kron_plan* plan, size_t* bytes_f64, size_t* bytes_f32);
+/* The recorded batch lists (host memory), level by level; capacity 0 queries the count. */
+asg_status asg_kron_plan_lists(const asg_kron_plan* plan, asg_gemm_desc* out, int capacity, int* count);
+/* Y = kron(A1..An) * X (kron_multd.m / kronmultN.m results, kronmultN_batch.m execution).
+ * A: host array of nkron device pointers; X, Y, work: device; work_bytes >= the workspace. */
+asg_status asg_kron_batch_f64(const asg_kron_plan* plan, const double* const* A, const double* X, double* Y,
+                              void* work, size_t work_bytes, void* stream);
+asg_status asg_kron_batch_f32(const asg_kron_plan* plan, const float* const* A, const float* X, float* Y,
+                              void* work, size_t work_bytes, void* stream);
+/* out = kron(A1, kron(A2, ...)) (krond.m:7-17), column-major prod(nrow) x prod(ncol).
+ * A: host array of nkron device pointers (each nrow_i x ncol_i, ld = nrow_i). */
+asg_status asg_krond_f64(int nkron, const int* nrow, const int* ncol, const double* const* A, double* out,
+                         void* stream);
+
 #ifdef __cplusplus
 }
 #endif
