@@ -84,9 +84,16 @@ SIGNATURES = {
     "asg_plan_stats_get": (C.c_int, [C.c_void_p, C.POINTER(PlanStats)]),
     "asg_plan_update_ops": (C.c_int, [C.c_void_p, C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.c_int)]),
     "asg_plan_set_kernel": (C.c_int, [C.c_void_p, C.c_int]),
+    "asg_plan_active": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint)]),
     "asg_plan_device_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "asg_apply_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "asg_apply_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "asg_apply_T_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "asg_apply_T_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "asg_grad_ops_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_int),
+                                   C.c_void_p]),
+    "asg_grad_ops_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_int),
+                                   C.c_void_p]),
     "asg_apply_host_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "asg_apply_host_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "asg_hash_table_sparse_nd": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.c_int, C.c_int, C.POINTER(C.c_int),

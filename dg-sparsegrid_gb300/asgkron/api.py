@@ -145,6 +145,60 @@ class Plan:
             raise TypeError("f must be float64 or float32")
         return y
 
+    def apply_T(self, ybar, fbar=None, stream=None):
+        """Adjoint on CUDA tensors: fbar = A^T ybar."""
+        import torch
+
+        if not (ybar.is_cuda and ybar.is_contiguous() and ybar.numel() == self.dof):
+            raise ValueError("ybar must be a contiguous CUDA tensor with %d values" % self.dof)
+        if fbar is None:
+            fbar = torch.empty_like(ybar)
+        s = stream if stream is not None else torch.cuda.current_stream(ybar.device)
+        fn = lib().asg_apply_T_f64 if ybar.dtype == torch.float64 else lib().asg_apply_T_f32
+        check(fn(self._handle, C.c_void_p(ybar.data_ptr()), C.c_void_p(fbar.data_ptr()), C.c_void_p(s.cuda_stream)))
+        return fbar
+
+    def grad_ops(self, f, r, stream=None):
+        """dL/dA_{t,k} for every applied factor given y = A f and r = dL/dy (CUDA tensors).
+
+        Returns T lists of d dense (n x n) column-major tensors (as [n, n] torch tensors in
+        row-major view of the transposed storage, i.e. G[t][k][row, col]); identity factors the
+        structure analysis skipped get None."""
+        import torch
+
+        T, D = self.T, self.D
+        outs = [[None] * D for _ in range(T)]
+        ptrs = (C.c_void_p * (T * D))()
+        lds = (C.c_int * (T * D))()
+        keep = []
+        for t in range(T):
+            for d in range(D):
+                n = self.term_mats[t][d].shape[0]
+                g = torch.zeros(n * n, dtype=f.dtype, device=f.device)
+                keep.append(g)
+                ptrs[t * D + d] = g.data_ptr()
+                lds[t * D + d] = n
+                outs[t][d] = g
+        s = stream if stream is not None else torch.cuda.current_stream(f.device)
+        fn = lib().asg_grad_ops_f64 if f.dtype == torch.float64 else lib().asg_grad_ops_f32
+        check(fn(self._handle, C.c_void_p(f.data_ptr()), C.c_void_p(r.data_ptr()), ptrs, lds,
+                 C.c_void_p(s.cuda_stream)))
+        active = self.active_factors()
+        res = []
+        for t in range(T):
+            row = []
+            for d in range(D):
+                n = self.term_mats[t][d].shape[0]
+                row.append(outs[t][d].view(n, n).t() if active[t][d] else None)
+            res.append(row)
+        return res
+
+    def active_factors(self):
+        """[t][d] True where the plan applies operator (t, d) (False: a detected identity)."""
+        masks = (C.c_uint * self.T)()
+        check(lib().asg_plan_active(self._handle, masks))
+        return [[bool((masks[t] >> d) & 1) for d in range(self.D)] for t in range(self.T)]
+
     def apply_host(self, f, out=None):
         """Host apply (copies in/out inside the library); numpy float64 or float32."""
         f = np.ascontiguousarray(f)
@@ -216,3 +270,66 @@ def apply_A(pde, opts, A_data, f, deg, Vmax=None, Emax=None, imex_flag="N"):
         plan = Plan.create(mats, idx, deg, pairs=pairs, structure="detect", index_base=1)
         _PLAN_CACHE[key] = plan
     return plan.apply_host(np.asarray(f, dtype=np.float64).reshape(-1))
+
+
+# -------------------------------------------------------------------------------------
+# torch.autograd harness: y = A(ops) f with gradients for f and the 1-D operators
+# -------------------------------------------------------------------------------------
+def autograd_apply(plan, f, op_tensors=None):
+    """y = A f through the plan with autograd support.
+
+    ``op_tensors`` (optional) is a T x d nested list of torch tensors holding the plan's 1-D
+    operators; gradients flow into those of them that require grad (the plan must have been
+    created from the same values).  The backward pass runs the adjoint kernel for f and the
+    deterministic operator-gradient kernel for the operators."""
+    import torch
+
+    flat = [] if op_tensors is None else [x for row in op_tensors for x in row]
+    return _ApplyA.apply(plan, f, *flat)
+
+
+def _make_function():
+    import torch
+
+    class ApplyA(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, plan, f, *ops):
+            ctx.plan = plan
+            ctx.nops = len(ops)
+            ctx.save_for_backward(f)
+            return plan.apply(f.contiguous())
+
+        @staticmethod
+        def backward(ctx, ybar):
+            plan = ctx.plan
+            (f,) = ctx.saved_tensors
+            ybar = ybar.contiguous()
+            fbar = plan.apply_T(ybar) if ctx.needs_input_grad[1] else None
+            grads = [None] * ctx.nops
+            if ctx.nops and any(ctx.needs_input_grad[2:]):
+                G = plan.grad_ops(f, ybar)
+                k = 0
+                for t in range(plan.T):
+                    for d in range(plan.D):
+                        if ctx.needs_input_grad[2 + k]:
+                            g = G[t][d]
+                            n = plan.term_mats[t][d].shape[0]
+                            grads[k] = g.contiguous() if g is not None else torch.zeros(n, n, dtype=f.dtype,
+                                                                                        device=f.device)
+                        k += 1
+            return (None, fbar, *grads)
+
+    return ApplyA
+
+
+class _Lazy:
+    fn = None
+
+    @classmethod
+    def apply(cls, *a):
+        if cls.fn is None:
+            cls.fn = _make_function()
+        return cls.fn.apply(*a)
+
+
+_ApplyA = _Lazy

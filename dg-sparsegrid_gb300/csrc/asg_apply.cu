@@ -796,6 +796,115 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Gradient with respect to the 1-D operators.  For a work entry (i, j, t) and an applied
+// factor k of term t, d L / d A_{t,k}[I_k(i), J_k(j)] (a P x P block) is the contraction of
+// r_i with Z = (kron of the term's other applied factors) f_j over every dimension but k:
+// G[a][b] = sum over the fibers along k of r_i[.., a, ..] * Z[.., b, ..].  Z is recomputed
+// from f_j (mode products in shared memory) instead of being stored by the forward pass.
+// One CTA owns one target block and sums its contributors in a fixed order; the P x P
+// partial sums are reduced across the CTA with shuffles and one shared-memory pass, so the
+// result is bitwise deterministic without atomics.
+// ---------------------------------------------------------------------------------------
+template <typename T, int P>
+__global__ void __launch_bounds__(256) k_grad(GradArgs<T> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int B = a.B, D = a.D, tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  const int Bpad = (B + 3) & ~3;
+  T* buf0 = reinterpret_cast<T*>(smem_raw);
+  T* buf1 = buf0 + Bpad;
+  T* red = buf1 + Bpad;  // [8][P*P]
+  for (int g = blockIdx.x; g < a.ntgt; g += gridDim.x) {
+    const GradTarget tg = a.tgt[g];
+    T* Gout = a.G[tg.tm];
+    if (Gout == nullptr) continue;  // uniform across the CTA
+    T acc[P][P];
+#pragma unroll
+    for (int x = 0; x < P; ++x)
+#pragma unroll
+      for (int y = 0; y < P; ++y) acc[x][y] = T(0);
+    for (long long c = a.tgt_ptr[g]; c < a.tgt_ptr[g + 1]; ++c) {
+      const GradContrib e = a.contrib[c];
+      const unsigned others = a.active[e.t] & ~(1u << e.k);
+      const T* ri = a.r + static_cast<size_t>(e.i) * B;
+      const T* z = a.f + static_cast<size_t>(e.j) * B;
+      if (others) {
+        team_copy(buf0, z, B, tid, 256);
+        __syncthreads();
+        T* in = buf0;
+        T* out = buf1;
+        for (int m = D - 1; m >= 0; --m) {
+          if (!((others >> m) & 1u)) continue;
+          const int tm = e.t * D + m;
+          const T* Ag = a.ops + a.op_off[tm] +
+                        (static_cast<long long>(a.idx1d[e.i * D + m]) * a.op_nb[tm] + a.idx1d[e.j * D + m]) * (P * P);
+          T A[P * P];
+#pragma unroll
+          for (int r = 0; r < P * P; ++r) A[r] = Ag[r];
+          mode_pass<T, P>(in, out, A, B, a.stride[m], tid, 256);
+          __syncthreads();
+          T* tmp = in;
+          in = out;
+          out = tmp;
+        }
+        z = in;
+      }
+      const int s = a.stride[e.k];
+      const int nf = B / P;
+      for (int fi = tid; fi < nf; fi += 256) {
+        const int hi = fi / s, lo = fi - hi * s;
+        const int base = hi * s * P + lo;
+        T rv[P], zv[P];
+#pragma unroll
+        for (int x = 0; x < P; ++x) {
+          rv[x] = ri[base + x * s];
+          zv[x] = z[base + x * s];
+        }
+#pragma unroll
+        for (int x = 0; x < P; ++x)
+#pragma unroll
+          for (int y = 0; y < P; ++y) acc[x][y] = fma(rv[x], zv[y], acc[x][y]);
+      }
+      __syncthreads();  // the staging buffers are reused by the next contributor
+    }
+#pragma unroll
+    for (int x = 0; x < P; ++x)
+#pragma unroll
+      for (int y = 0; y < P; ++y) {
+        T v = acc[x][y];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if (lane == 0) red[warp * P * P + x * P + y] = v;
+      }
+    __syncthreads();
+    if (tid < P * P) {
+      T sum = T(0);
+      for (int w = 0; w < 8; ++w) sum += red[w * P * P + tid];
+      const int x = tid / P, y = tid % P;
+      Gout[static_cast<long long>(tg.beta * P + y) * a.ldg[tg.tm] + tg.alpha * P + x] = sum;
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T, int P>
+cudaError_t launch_grad_p(const GradArgs<T>& a, cudaStream_t s) {
+  const int Bpad = (a.B + 3) & ~3;
+  const size_t sm = (static_cast<size_t>(2) * Bpad + 8 * P * P) * sizeof(T);
+  auto kern = k_grad<T, P>;
+  static bool done = false;
+  if (sm > 48 * 1024 && !done) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>((2 * kMaxBlock + 8 * P * P) * sizeof(T)));
+    if (e != cudaSuccess) return e;
+    done = true;
+  }
+  const int grid = a.ntgt < 152 * 8 ? a.ntgt : 152 * 8;
+  kern<<<grid, 256, sm, s>>>(a);
+  return cudaGetLastError();
+}
+
 // Opt a kernel into more than 48 KB of dynamic shared memory (once per instantiation; the
 // limit set is the largest this kernel can request, so later plans need no new call).
 template <typename K>
@@ -896,6 +1005,24 @@ cudaError_t launch_apply(const ApplyArgs<T>& a, int P, int kind, cudaStream_t s)
   }
 }
 
+template <typename T>
+cudaError_t launch_grad(const GradArgs<T>& a, int P, cudaStream_t s) {
+  if (a.ntgt == 0) return cudaSuccess;
+  switch (P) {
+    case 1: return launch_grad_p<T, 1>(a, s);
+    case 2: return launch_grad_p<T, 2>(a, s);
+    case 3: return launch_grad_p<T, 3>(a, s);
+    case 4: return launch_grad_p<T, 4>(a, s);
+    case 5: return launch_grad_p<T, 5>(a, s);
+    case 6: return launch_grad_p<T, 6>(a, s);
+    case 7: return launch_grad_p<T, 7>(a, s);
+    case 8: return launch_grad_p<T, 8>(a, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+
+template cudaError_t launch_grad<double>(const GradArgs<double>&, int, cudaStream_t);
+template cudaError_t launch_grad<float>(const GradArgs<float>&, int, cudaStream_t);
 template cudaError_t launch_apply<double>(const ApplyArgs<double>&, int, int, cudaStream_t);
 template cudaError_t launch_apply<float>(const ApplyArgs<float>&, int, int, cudaStream_t);
 

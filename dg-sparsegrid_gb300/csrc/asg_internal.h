@@ -58,6 +58,36 @@ struct ApplyArgs {
 template <typename T>
 cudaError_t launch_apply(const ApplyArgs<T>& a, int P, int kernel_kind, cudaStream_t s);
 
+// Gradient with respect to the 1-D operators: one CTA per target block (t, k, alpha, beta)
+// sums its contributing work entries (i, j, t, k) in a fixed order.
+struct GradContrib {
+  int i, j, t, k;
+};
+struct GradTarget {
+  int tm;     // t*D + k
+  int alpha;  // block row (1-D index of the row element in dimension k)
+  int beta;   // block column
+};
+template <typename T>
+struct GradArgs {
+  const T* f;                   // forward input
+  const T* r;                   // cotangent (d L / d y)
+  const T* ops;                 // packed blocks (same layout as the apply)
+  const long long* op_off;
+  const int* op_nb;
+  const int* idx1d;
+  const unsigned* active;
+  const long long* tgt_ptr;     // [ntgt+1] contributors of each target
+  const GradContrib* contrib;
+  const GradTarget* tgt;
+  T* const* G;                  // [T*D] dense column-major outputs (device), NULL = skip
+  const int* ldg;               // [T*D]
+  int ntgt, D, B;
+  int stride[kMaxDims];
+};
+template <typename T>
+cudaError_t launch_grad(const GradArgs<T>& a, int P, cudaStream_t s);
+
 enum KernelKind { KK_CHAIN_WARP = 0, KK_CHAIN_CTA = 1, KK_SINGLE_MODE = 2, KK_SINGLE_TMA = 3, KK_SINGLE_TMA3 = 4 };
 
 }  // namespace asg
@@ -89,6 +119,17 @@ struct asg_plan {
   int* d_ent = nullptr;
   long long* d_tr_row_ptr = nullptr;
   int* d_tr_ent = nullptr;
+  std::vector<double> h64;           // packed FP64 blocks (host copy: transposes and gradients)
+  asg_plan* tr = nullptr;            // transposed plan (A^T), built on first use
+  // gradient targets (built on first use)
+  std::vector<long long> g_ptr;
+  std::vector<asg::GradContrib> g_contrib;
+  std::vector<asg::GradTarget> g_tgt;
+  long long* d_g_ptr = nullptr;
+  asg::GradContrib* d_g_contrib = nullptr;
+  asg::GradTarget* d_g_tgt = nullptr;
+  int* d_ldg = nullptr;
+  void** d_gptrs = nullptr;
   std::vector<asg::EntryDesc> ed;   // single-mode descriptors (empty unless every term has one factor)
   asg::EntryDesc* d_ed = nullptr;
   std::vector<int> row_order;

@@ -38,7 +38,22 @@ asg_status upload(X** dst, const std::vector<X>& src) {
   return ASG_OK;
 }
 
+void free_device(asg_plan* p);
+void free_plan(asg_plan* p) {
+  if (!p) return;
+  free_device(p);
+  delete p;
+}
 void free_device(asg_plan* p) {
+  if (p->tr) {
+    free_plan(p->tr);
+    p->tr = nullptr;
+  }
+  cudaFree(p->d_g_ptr);
+  cudaFree(p->d_g_contrib);
+  cudaFree(p->d_g_tgt);
+  cudaFree(p->d_ldg);
+  cudaFree(p->d_gptrs);
   cudaFree(p->d_idx1d);
   cudaFree(p->d_op_nb);
   cudaFree(p->d_active);
@@ -70,14 +85,19 @@ void pack_op(const double* op, int ld, int nb, int P, double* dst) {
     }
 }
 
-asg_status pack_and_upload(asg_plan* p, const double* const* ops, const int* op_ld) {
-  std::vector<double> h64(static_cast<size_t>(p->packed_elems));
+void pack_host(asg_plan* p, const double* const* ops, const int* op_ld) {
+  p->h64.assign(static_cast<size_t>(p->packed_elems), 0.0);
   for (int t = 0; t < p->T; ++t)
     for (int m = 0; m < p->D; ++m) {
       const int tm = t * p->D + m;
       if (p->op_off[tm] < 0) continue;
-      pack_op(ops[tm], op_ld[tm], p->op_nb[tm], p->P, h64.data() + p->op_off[tm]);
+      pack_op(ops[tm], op_ld[tm], p->op_nb[tm], p->P, p->h64.data() + p->op_off[tm]);
     }
+}
+
+// Uploads the packed blocks in the three device layouts (FP64, FP32, FP32 paired).
+asg_status upload_ops(asg_plan* p) {
+  const std::vector<double>& h64 = p->h64;
   std::vector<float> h32(h64.size());
   for (size_t i = 0; i < h64.size(); ++i) h32[i] = static_cast<float>(h64[i]);
   if (!p->ed.empty() && p->P == 4) {
@@ -115,6 +135,201 @@ asg_status pack_and_upload(asg_plan* p, const double* const* ops, const int* op_
     ASG_CUDA(cudaMemcpy(p->d_ops64, h64.data(), h64.size() * sizeof(double), cudaMemcpyHostToDevice));
     ASG_CUDA(cudaMemcpy(p->d_ops32, h32.data(), h32.size() * sizeof(float), cudaMemcpyHostToDevice));
   }
+  return ASG_OK;
+}
+
+// Kernel choice, launch order, single-mode descriptors and every upload; shared by a plan
+// and its transpose.  Expects idx1d, op_nb, active, op_off, row_ptr, ent and h64 filled.
+asg_status finalize(asg_plan* p) {
+  const int D = p->D, P = p->P, T = p->T, N = p->N;
+  const long long B = p->B;
+  const bool detect = p->structure == ASG_STRUCT_DETECT;
+  std::vector<int>& ent = p->ent;
+  double pd1 = 1.0;
+  for (int k = 0; k <= D; ++k) pd1 *= P;
+  p->flops_exec = 0.0;
+  for (int i = 0; i < N; ++i)
+    for (long long q = p->row_ptr[i]; q < p->row_ptr[i + 1]; ++q)
+      p->flops_exec += 2.0 * pd1 * __builtin_popcount(p->active[ent[q] & 15]);
+  bool single = detect && (P == 3 || P == 4) && B >= 32LL * P * P;
+  for (int t = 0; t < T; ++t)
+    if (__builtin_popcount(p->active[t]) != 1) single = false;
+  p->kernel_kind = single ? ((P == 4 && B == 4096) ? KK_SINGLE_TMA : KK_SINGLE_MODE)
+                          : (B <= 256 ? KK_CHAIN_WARP : KK_CHAIN_CTA);
+  p->row_order.clear();
+  p->ed.clear();
+  if (single) {
+    // rows launch longest first so the last wave is made of short rows
+    p->row_order.resize(N);
+    for (int i = 0; i < N; ++i) p->row_order[i] = i;
+    std::stable_sort(p->row_order.begin(), p->row_order.end(), [&](int x, int y) {
+      return p->row_ptr[x + 1] - p->row_ptr[x] > p->row_ptr[y + 1] - p->row_ptr[y];
+    });
+    // per-entry descriptors of the single-mode kernels: column, dimension, block offset
+    p->ed.resize(ent.size());
+    for (int i = 0; i < N; ++i)
+      for (long long q = p->row_ptr[i]; q < p->row_ptr[i + 1]; ++q) {
+        const int j = ent[q] >> 4, t = ent[q] & 15;
+        const int m = __builtin_ctz(p->active[t]);
+        const int tm = t * D + m;
+        p->ed[q].j = j;
+        p->ed[q].m = m;
+        p->ed[q].aoff = p->op_off[tm] + (static_cast<long long>(p->idx1d[i * D + m]) * p->op_nb[tm] +
+                                         p->idx1d[j * D + m]) * P * P;
+      }
+  }
+  asg_status st;
+  if ((st = upload(&p->d_row_order, p->row_order))) return st;
+  if ((st = upload_ops(p))) return st;
+  if ((st = upload(&p->d_idx1d, p->idx1d))) return st;
+  if ((st = upload(&p->d_op_nb, p->op_nb))) return st;
+  if ((st = upload(&p->d_active, p->active))) return st;
+  if ((st = upload(&p->d_op_off, p->op_off))) return st;
+  if ((st = upload(&p->d_row_ptr, p->row_ptr))) return st;
+  if ((st = upload(&p->d_ent, p->ent))) return st;
+  if ((st = upload(&p->d_ed, p->ed))) return st;
+  ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_err), sizeof(int)));
+  ASG_CUDA(cudaMemset(p->d_err, 0, sizeof(int)));
+  return ASG_OK;
+}
+
+// The transposed plan: A^T has block (j, i) = kron_d (A_td^T)[J_d(j), I_d(i)], so it is
+// the same operator application with every packed block (a, b) replaced by block (b, a)
+// transposed and the work list transposed (row j collects the entries (i, t) that had column
+// j).  Structure classes (zero / identity) are invariant under transposition.
+asg_status build_transpose(asg_plan* p) {
+  if (p->tr) return ASG_OK;
+  asg_plan* t = new (std::nothrow) asg_plan;
+  if (!t) return fail(ASG_ERR_NOMEM, "transpose: out of host memory");
+  t->D = p->D;
+  t->P = p->P;
+  t->T = p->T;
+  t->N = p->N;
+  t->B = p->B;
+  t->structure = p->structure;
+  t->drop_tol = p->drop_tol;
+  t->idx1d = p->idx1d;
+  t->op_nb = p->op_nb;
+  t->active = p->active;
+  t->op_off = p->op_off;
+  t->packed_elems = p->packed_elems;
+  t->pairs = p->pairs;
+  t->flops_dense = p->flops_dense;
+  const int P = p->P, PP = P * P;
+  t->h64.assign(p->h64.size(), 0.0);
+  for (int tm = 0; tm < p->T * p->D; ++tm) {
+    if (p->op_off[tm] < 0) continue;
+    const int nb = p->op_nb[tm];
+    const double* src = p->h64.data() + p->op_off[tm];
+    double* dst = t->h64.data() + p->op_off[tm];
+    for (int a = 0; a < nb; ++a)
+      for (int b = 0; b < nb; ++b)
+        for (int r = 0; r < P; ++r)
+          for (int c = 0; c < P; ++c)
+            dst[(static_cast<long long>(a) * nb + b) * PP + r * P + c] =
+                src[(static_cast<long long>(b) * nb + a) * PP + c * P + r];
+  }
+  // CSR transpose of the work list (row order of the forward plan preserved per column)
+  const int N = p->N;
+  t->row_ptr.assign(N + 1, 0);
+  for (int e : p->ent) t->row_ptr[(e >> 4) + 1]++;
+  for (int i = 0; i < N; ++i) t->row_ptr[i + 1] += t->row_ptr[i];
+  t->ent.assign(p->ent.size(), 0);
+  std::vector<long long> fill(t->row_ptr.begin(), t->row_ptr.end() - 1);
+  for (int i = 0; i < N; ++i)
+    for (long long q = p->row_ptr[i]; q < p->row_ptr[i + 1]; ++q) {
+      const int j = p->ent[q] >> 4, term = p->ent[q] & 15;
+      t->ent[fill[j]++] = (i << 4) | term;
+    }
+  if (p->structure == ASG_STRUCT_DETECT)  // single-mode kernels walk a row's entries term by term
+    for (int j = 0; j < N; ++j)
+      std::stable_sort(t->ent.begin() + t->row_ptr[j], t->ent.begin() + t->row_ptr[j + 1],
+                       [](int x, int y) { return (x & 15) < (y & 15); });
+  asg_status st = finalize(t);
+  if (st) {
+    free_plan(t);
+    return st;
+  }
+  p->tr = t;
+  return ASG_OK;
+}
+
+asg_status check_ptr(const void* ptr, const char* name);
+
+// Gradient targets: every (t, k, alpha, beta) block of an applied factor that some work
+// entry touches, with its contributing entries in work-list order (deterministic sums).
+asg_status build_grad(asg_plan* p) {
+  if (p->d_g_ptr) return ASG_OK;
+  const int D = p->D;
+  std::map<long long, std::vector<GradContrib>> tg;
+  for (int i = 0; i < p->N; ++i)
+    for (long long q = p->row_ptr[i]; q < p->row_ptr[i + 1]; ++q) {
+      const int j = p->ent[q] >> 4, t = p->ent[q] & 15;
+      for (int k = 0; k < D; ++k) {
+        if (!((p->active[t] >> k) & 1u)) continue;
+        const long long key = (static_cast<long long>(t * D + k) << 48) |
+                              (static_cast<long long>(p->idx1d[i * D + k]) << 24) | p->idx1d[j * D + k];
+        tg[key].push_back({i, j, t, k});
+      }
+    }
+  p->g_ptr.assign(1, 0);
+  p->g_contrib.clear();
+  p->g_tgt.clear();
+  for (auto& kv : tg) {
+    p->g_tgt.push_back({static_cast<int>(kv.first >> 48), static_cast<int>((kv.first >> 24) & 0xFFFFFF),
+                        static_cast<int>(kv.first & 0xFFFFFF)});
+    p->g_contrib.insert(p->g_contrib.end(), kv.second.begin(), kv.second.end());
+    p->g_ptr.push_back(static_cast<long long>(p->g_contrib.size()));
+  }
+  asg_status st;
+  if ((st = upload(&p->d_g_ptr, p->g_ptr))) return st;
+  if ((st = upload(&p->d_g_contrib, p->g_contrib))) return st;
+  if ((st = upload(&p->d_g_tgt, p->g_tgt))) return st;
+  ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_ldg), sizeof(int) * p->T * D));
+  ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_gptrs), sizeof(void*) * p->T * D));
+  return ASG_OK;
+}
+
+template <typename T>
+asg_status grad_ops(asg_plan* p, const T* f, const T* r, T* const* G, const int* ldg, void* stream) {
+  if (!p || !G || !ldg) return fail(ASG_ERR_INVALID, "grad_ops: NULL argument");
+  asg_status st = check_ptr(f, "f");
+  if (st) return st;
+  if ((st = check_ptr(r, "r"))) return st;
+  for (int tm = 0; tm < p->T * p->D; ++tm)
+    if (G[tm] && p->op_off[tm] >= 0 && ldg[tm] < p->op_nb[tm] * p->P)
+      return fail(ASG_ERR_INVALID, "grad_ops: ldg[%d]=%d < %d", tm, ldg[tm], p->op_nb[tm] * p->P);
+  if ((st = build_grad(p))) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  std::vector<void*> gp(p->T * p->D);
+  for (int tm = 0; tm < p->T * p->D; ++tm) gp[tm] = p->op_off[tm] >= 0 ? static_cast<void*>(G[tm]) : nullptr;
+  ASG_CUDA(cudaMemcpyAsync(p->d_gptrs, gp.data(), sizeof(void*) * gp.size(), cudaMemcpyHostToDevice, s));
+  ASG_CUDA(cudaMemcpyAsync(p->d_ldg, ldg, sizeof(int) * gp.size(), cudaMemcpyHostToDevice, s));
+  GradArgs<T> a{};
+  a.f = f;
+  a.r = r;
+  a.ops = sizeof(T) == 8 ? reinterpret_cast<const T*>(p->d_ops64) : reinterpret_cast<const T*>(p->d_ops32);
+  a.op_off = p->d_op_off;
+  a.op_nb = p->d_op_nb;
+  a.idx1d = p->d_idx1d;
+  a.active = p->d_active;
+  a.tgt_ptr = p->d_g_ptr;
+  a.contrib = p->d_g_contrib;
+  a.tgt = p->d_g_tgt;
+  a.G = reinterpret_cast<T* const*>(p->d_gptrs);
+  a.ldg = p->d_ldg;
+  a.ntgt = static_cast<int>(p->g_tgt.size());
+  a.D = p->D;
+  a.B = p->B;
+  int sd = 1;
+  for (int m = p->D - 1; m >= 0; --m) {
+    a.stride[m] = sd;
+    sd *= p->P;
+  }
+  cudaError_t e = launch_grad<T>(a, p->P, s);
+  if (e != cudaSuccess) return cuda_fail(e, "grad kernel launch");
+  // the pointer/ld tables are read by the kernel: keep the host arrays alive until the copy
+  // is done (pageable copies are staged before cudaMemcpyAsync returns)
   return ASG_OK;
 }
 
@@ -371,23 +586,6 @@ asg_status asg_plan_create(const asg_plan_desc* desc, asg_plan** out) {
       p->row_ptr[i + 1] = static_cast<long long>(ent.size());
     }
   }
-  // ---- flop model and kernel choice --------------------------------------------------
-  double pd1 = 1.0;
-  for (int k = 0; k <= D; ++k) pd1 *= P;
-  p->flops_dense = static_cast<double>(p->pairs) * T * D * 2.0 * pd1;
-  p->flops_exec = 0.0;
-  int amax = 0;
-  for (int i = 0; i < N; ++i)
-    for (long long q = p->row_ptr[i]; q < p->row_ptr[i + 1]; ++q)
-      p->flops_exec += 2.0 * pd1 * __builtin_popcount(p->active[ent[q] & 15]);
-  bool single = detect && (P == 3 || P == 4) && B >= 32LL * P * P;
-  for (int t = 0; t < T; ++t) {
-    const int na = __builtin_popcount(p->active[t]);
-    amax = std::max(amax, na);
-    if (na != 1) single = false;
-  }
-  p->kernel_kind = single ? ((P == 4 && B == 4096) ? asg::KK_SINGLE_TMA : asg::KK_SINGLE_MODE)
-                          : (B <= 256 ? asg::KK_CHAIN_WARP : asg::KK_CHAIN_CTA);
   // ---- pack operators -------------------------------------------------------------
   long long off = 0;
   for (int t = 0; t < T; ++t)
@@ -398,42 +596,12 @@ asg_status asg_plan_create(const asg_plan_desc* desc, asg_plan** out) {
       off += static_cast<long long>(p->op_nb[tm]) * p->op_nb[tm] * P * P;
     }
   p->packed_elems = off;
-  if (single) {
-    // rows launch longest first so the last wave is made of short rows
-    p->row_order.resize(N);
-    for (int i = 0; i < N; ++i) p->row_order[i] = i;
-    std::stable_sort(p->row_order.begin(), p->row_order.end(), [&](int x, int y) {
-      return p->row_ptr[x + 1] - p->row_ptr[x] > p->row_ptr[y + 1] - p->row_ptr[y];
-    });
-    // per-entry descriptors of the single-mode kernels: column, dimension, block offset
-    p->ed.resize(ent.size());
-    for (int i = 0; i < N; ++i)
-      for (long long q = p->row_ptr[i]; q < p->row_ptr[i + 1]; ++q) {
-        const int j = ent[q] >> 4, t = ent[q] & 15;
-        const int m = __builtin_ctz(p->active[t]);
-        const int tm = t * D + m;
-        p->ed[q].j = j;
-        p->ed[q].m = m;
-        p->ed[q].aoff = p->op_off[tm] + (static_cast<long long>(p->idx1d[i * D + m]) * p->op_nb[tm] +
-                                         p->idx1d[j * D + m]) * P * P;
-      }
-  }
-  asg_status st;
-  if ((st = asg::upload(&p->d_row_order, p->row_order))) return bail(st);
-  if ((st = asg::pack_and_upload(p, desc->ops, desc->op_ld))) return bail(st);
-  if ((st = asg::upload(&p->d_idx1d, p->idx1d))) return bail(st);
-  if ((st = asg::upload(&p->d_op_nb, p->op_nb))) return bail(st);
-  if ((st = asg::upload(&p->d_active, p->active))) return bail(st);
-  if ((st = asg::upload(&p->d_op_off, p->op_off))) return bail(st);
-  if ((st = asg::upload(&p->d_row_ptr, p->row_ptr))) return bail(st);
-  if ((st = asg::upload(&p->d_ent, p->ent))) return bail(st);
-  if ((st = asg::upload(&p->d_ed, p->ed))) return bail(st);
-  {
-    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p->d_err), sizeof(int));
-    if (e == cudaSuccess) e = cudaMemset(p->d_err, 0, sizeof(int));
-    if (e != cudaSuccess) return bail(asg::cuda_fail(e, "status word"));
-  }
-  (void)amax;
+  asg::pack_host(p, desc->ops, desc->op_ld);
+  double pd1 = 1.0;
+  for (int k = 0; k <= D; ++k) pd1 *= P;
+  p->flops_dense = static_cast<double>(p->pairs) * T * D * 2.0 * pd1;
+  asg_status st = asg::finalize(p);
+  if (st) return bail(st);
   *out = p;
   return ASG_OK;
 }
@@ -460,6 +628,12 @@ asg_status asg_plan_stats_get(const asg_plan* p, asg_plan_stats* s) {
   return ASG_OK;
 }
 
+asg_status asg_plan_active(const asg_plan* p, unsigned* masks) {
+  if (!p || !masks) return fail(ASG_ERR_INVALID, "plan_active: NULL argument");
+  for (int t = 0; t < p->T; ++t) masks[t] = p->active[t];
+  return ASG_OK;
+}
+
 asg_status asg_plan_update_ops(asg_plan* p, const double* const* ops, const int* op_ld) {
   if (!p || !ops || !op_ld) return fail(ASG_ERR_INVALID, "plan_update_ops: NULL argument");
   for (int tm = 0; tm < p->T * p->D; ++tm) {
@@ -467,7 +641,12 @@ asg_status asg_plan_update_ops(asg_plan* p, const double* const* ops, const int*
     if (!ops[tm]) return fail(ASG_ERR_INVALID, "plan_update_ops: operator %d is NULL", tm);
     if (op_ld[tm] < p->op_nb[tm] * p->P) return fail(ASG_ERR_INVALID, "plan_update_ops: ld too small for operator %d", tm);
   }
-  return asg::pack_and_upload(p, ops, op_ld);
+  asg::pack_host(p, ops, op_ld);
+  if (p->tr) {  // the transpose is rebuilt from the new values on its next use
+    asg::free_plan(p->tr);
+    p->tr = nullptr;
+  }
+  return asg::upload_ops(p);
 }
 
 asg_status asg_plan_set_kernel(asg_plan* p, int kind) {
@@ -495,6 +674,26 @@ asg_status asg_plan_device_status(asg_plan* p, int* status) {
     return fail(v, "a kernel of this plan reported status %d (bounded wait gave up)", v);
   }
   return ASG_OK;
+}
+
+asg_status asg_grad_ops_f64(asg_plan* p, const double* f, const double* r, double* const* G, const int* ldg,
+                            void* stream) {
+  return asg::grad_ops<double>(p, f, r, G, ldg, stream);
+}
+asg_status asg_grad_ops_f32(asg_plan* p, const float* f, const float* r, float* const* G, const int* ldg,
+                            void* stream) {
+  return asg::grad_ops<float>(p, f, r, G, ldg, stream);
+}
+
+asg_status asg_apply_T_f64(asg_plan* p, const double* ybar, double* fbar, void* stream) {
+  if (!p) return fail(ASG_ERR_INVALID, "apply_T: NULL plan");
+  asg_status st = asg::build_transpose(p);
+  return st ? st : asg::apply_dev<double>(p->tr, ybar, fbar, stream);
+}
+asg_status asg_apply_T_f32(asg_plan* p, const float* ybar, float* fbar, void* stream) {
+  if (!p) return fail(ASG_ERR_INVALID, "apply_T: NULL plan");
+  asg_status st = asg::build_transpose(p);
+  return st ? st : asg::apply_dev<float>(p->tr, ybar, fbar, stream);
 }
 
 asg_status asg_apply_f64(asg_plan* p, const double* f, double* y, void* stream) { return asg::apply_dev<double>(p, f, y, stream); }

@@ -90,6 +90,9 @@ asg_status asg_last_error(char* buf, size_t len);
 asg_status asg_plan_create(const asg_plan_desc* desc, asg_plan** plan);
 asg_status asg_plan_destroy(asg_plan* plan);
 asg_status asg_plan_stats_get(const asg_plan* plan, asg_plan_stats* stats);
+/* Bit k of masks[t] is set when the plan applies operator (t, k); clear bits are factors the
+ * structure analysis found to be the identity (always all set under ASG_STRUCT_NONE). */
+asg_status asg_plan_active(const asg_plan* plan, unsigned* masks);
 /* Re-upload operator values with the same sparsity class (time-dependent terms rebuilt by
  * get_coeff_mats.m with TD=1); the structure analysis is not redone. */
 asg_status asg_plan_update_ops(asg_plan* plan, const double* const* ops, const int* op_ld);
@@ -110,6 +113,20 @@ asg_status asg_plan_device_status(asg_plan* plan, int* status);
  * accumulation across the column reduction. */
 asg_status asg_apply_f64(asg_plan* plan, const double* d_f, double* d_y, void* stream);
 asg_status asg_apply_f32(asg_plan* plan, const float* d_f, float* d_y, void* stream);
+/* Adjoint: fbar = A^T * ybar (device pointers).  No reference counterpart (the prototype has
+ * no adjoint); built from the transposed operator blocks and the transposed work list. */
+asg_status asg_apply_T_f64(asg_plan* plan, const double* d_ybar, double* d_fbar, void* stream);
+asg_status asg_apply_T_f32(asg_plan* plan, const float* d_ybar, float* d_fbar, void* stream);
+/* Gradient of a scalar L with cotangent r = dL/dy (y = A f) with respect to every applied
+ * 1-D operator (t, k): the P x P blocks that some work entry touches are written (not added)
+ * into G[t*d+k] (device, column-major, leading dimension ldg[t*d+k]); all other entries of G
+ * are left as they are, so zero G first for the full gradient.  G[t*d+k] may be NULL to skip;
+ * identity factors detected by ASG_STRUCT_DETECT are not differentiated.  G and ldg are host
+ * arrays.  Deterministic (fixed-order sums, no atomics).  No reference counterpart. */
+asg_status asg_grad_ops_f64(asg_plan* plan, const double* d_f, const double* d_r, double* const* G,
+                            const int* ldg, void* stream);
+asg_status asg_grad_ops_f32(asg_plan* plan, const float* d_f, const float* d_r, float* const* G,
+                            const int* ldg, void* stream);
 /* Same on host pointers: copies f in, applies, copies y out, synchronises (the call a
  * MATLAB MEX gateway makes). */
 asg_status asg_apply_host_f64(asg_plan* plan, const double* h_f, double* h_y);

@@ -828,6 +828,33 @@ def apply_A_rows(term_mats, idx1d, deg, f, rows=None, conn=None):
     return out.reshape(-1)
 
 
+def grad_ops_loop(term_mats, idx1d, deg, f, r, conn=None):
+    """dL/dA_{t,d} for y = apply_A(f) and dL/dy = r, by differentiating each krond block
+    (apply_A.m:170-201): d/dA_k[a,b] of r_i' kron(B_1..B_d) f_j = r_i' kron(.., E_ab, ..) f_j.
+    Small cases only (p^2 krond products per pair, term and dimension)."""
+    N, D = idx1d.shape
+    B = deg ** D
+    f = np.asarray(f, dtype=np.float64).reshape(N, B)
+    r = np.asarray(r, dtype=np.float64).reshape(N, B)
+    G = [[np.zeros_like(m) for m in tm] for tm in term_mats]
+    ar = np.arange(deg)
+    for e in range(N):
+        II = [(idx1d[e, d] - 1) * deg + ar for d in range(D)]
+        cols = (np.asarray(conn[e]) - 1) if conn is not None else range(N)
+        for j in cols:
+            JJ = [(idx1d[j, d] - 1) * deg + ar for d in range(D)]
+            for t, tm in enumerate(term_mats):
+                blocks = [tm[d][np.ix_(II[d], JJ[d])] for d in range(D)]
+                for k in range(D):
+                    for a in range(deg):
+                        for b in range(deg):
+                            E = np.zeros((deg, deg))
+                            E[a, b] = 1.0
+                            K = krond(blocks[:k] + [E] + blocks[k + 1:])
+                            G[t][k][II[k][a], JJ[k][b]] += r[e] @ K @ f[j]
+    return G
+
+
 # ------------------------------------------------------------------------------------------
 # Projections, sources and RK3 (md_eval_function.m, forward_wavelet_transform.m,
 # combine_dimensions_D.m, time_advance.m:151-204)
