@@ -72,6 +72,16 @@ class GemmDesc(C.Structure):
     ]
 
 
+class GmresOpts(C.Structure):
+    _fields_ = [("restart", C.c_int), ("max_outer", C.c_int), ("tol", C.c_double), ("inner_reduction", C.c_double),
+                ("mixed", C.c_int)]
+
+
+class GmresInfo(C.Structure):
+    _fields_ = [("outer_iters", C.c_int), ("inner_iters", C.c_int), ("converged", C.c_int),
+                ("rel_residual", C.c_double)]
+
+
 _P = C.c_void_p
 _I = C.POINTER(C.c_int)
 
@@ -117,6 +127,12 @@ SIGNATURES = {
     "asg_kron_batch_f64": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), _P, _P, _P, C.c_size_t, _P]),
     "asg_kron_batch_f32": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), _P, _P, _P, C.c_size_t, _P]),
     "asg_krond_f64": (C.c_int, [C.c_int, _I, _I, C.POINTER(C.c_void_p), _P, _P]),
+    "asg_rk3_step_f64": (C.c_int, [C.c_void_p, _P, C.c_double, C.POINTER(C.c_void_p), _P, C.c_size_t, _P]),
+    "asg_rk3_step_f32": (C.c_int, [C.c_void_p, _P, C.c_double, C.POINTER(C.c_void_p), _P, C.c_size_t, _P]),
+    "asg_lincomb_f64": (C.c_int, [C.c_longlong, C.c_int, _P, _P, _P, _P]),
+    "asg_be_workspace": (C.c_int, [C.c_void_p, C.POINTER(GmresOpts), C.POINTER(C.c_size_t)]),
+    "asg_be_solve": (C.c_int, [C.c_void_p, C.c_double, _P, _P, C.POINTER(GmresOpts), C.POINTER(GmresInfo), _P,
+                               C.c_size_t, _P]),
 }
 
 _LIB = None

@@ -1,0 +1,125 @@
+"""Time steppers on the GPU operator application (time_advance.m).
+
+* ``RK3Stepper``  RungeKutta3 (time_advance.m:151-204): separable sources s(t) = sum_s c_s(t)
+  v_s are formed on the device from precomputed spatial parts; one step (three source
+  combinations + three applies + three fused stage updates) can be captured once into a CUDA
+  graph and replayed, with only the time factors copied in before each replay.
+* ``be_solve`` / ``be_step``  backward Euler (time_advance.m:267-349): (I - dt A) f1 =
+  f0 + dt s solved matrix-free by GMRES inside iterative refinement (asg_be_solve).
+
+torch provides device memory, streams and the graph object; every kernel is libasgkron's.
+"""
+import ctypes as C
+
+import numpy as np
+
+from ._lib import GmresInfo, GmresOpts, check, lib
+
+
+class RK3Stepper:
+    def __init__(self, plan, pde=None, idx1d=None, dtype="float64", source_parts=None, time_factors=None):
+        import torch
+
+        self.plan = plan
+        self.torch_dtype = torch.float64 if dtype in ("float64", torch.float64) else torch.float32
+        self.n = plan.dof
+        dev = torch.device("cuda")
+        if source_parts is None and pde is not None and pde.sources:
+            source_parts, time_factors = pde.source_parts(plan.deg, np.asarray(idx1d))
+        self.tfac = list(time_factors or [])
+        ns = len(self.tfac)
+        self.ns = ns
+        self.vecs = [torch.from_numpy(np.asarray(v, dtype=np.float64)).to(dev) for v in (source_parts or [])]
+        self.vec_ptrs = torch.tensor([v.data_ptr() for v in self.vecs] or [0], dtype=torch.int64, device=dev)
+        self.coef = torch.zeros(3 * max(ns, 1), dtype=torch.float64, device=dev)
+        self.coef_host = torch.zeros(3 * max(ns, 1), dtype=torch.float64).pin_memory()
+        self.src64 = [torch.zeros(self.n, dtype=torch.float64, device=dev) for _ in range(3)]
+        self.src = self.src64 if self.torch_dtype == torch.float64 else [
+            torch.zeros(self.n, dtype=torch.float32, device=dev) for _ in range(3)]
+        self.work = torch.empty(4 * self.n, dtype=self.torch_dtype, device=dev)
+        self.graph = None
+        self._f_static = None
+
+    def _sources(self, stream):
+        import torch
+
+        if self.ns == 0:
+            return None
+        for k in range(3):
+            check(lib().asg_lincomb_f64(self.n, self.ns, C.c_void_p(self.coef.data_ptr() + 8 * k * self.ns),
+                                        C.c_void_p(self.vec_ptrs.data_ptr()), C.c_void_p(self.src64[k].data_ptr()),
+                                        C.c_void_p(stream.cuda_stream)))
+            if self.torch_dtype != torch.float64:
+                self.src[k].copy_(self.src64[k])
+        return (C.c_void_p * 3)(*[x.data_ptr() for x in self.src])
+
+    def _set_time(self, t, dt):
+        import torch
+
+        if self.ns == 0:
+            return
+        vals = [fn(tt) for tt in (t, t + 0.5 * dt, t + dt) for fn in self.tfac]
+        self.coef_host.copy_(torch.tensor(vals, dtype=torch.float64))
+        self.coef.copy_(self.coef_host, non_blocking=True)
+
+    def _launch(self, f, dt, stream):
+        src = self._sources(stream)
+        fn = lib().asg_rk3_step_f64 if self.torch_dtype.itemsize == 8 else lib().asg_rk3_step_f32
+        check(fn(self.plan.handle, C.c_void_p(f.data_ptr()), float(dt), src, C.c_void_p(self.work.data_ptr()),
+                 self.work.numel() * self.work.element_size(), C.c_void_p(stream.cuda_stream)))
+
+    def step(self, f, t, dt):
+        """Advance f (CUDA tensor, in place) from t to t + dt."""
+        import torch
+
+        self._set_time(t, dt)
+        self._launch(f, dt, torch.cuda.current_stream())
+        return f
+
+    def capture(self, f, dt):
+        """Capture one step on the static tensor f into a CUDA graph (dt fixed)."""
+        import torch
+
+        self._f_static = f
+        s = torch.cuda.Stream()
+        s.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(s):  # warm-up outside the capture (kernel attributes, lazy state)
+            saved = f.clone()
+            self._launch(f, dt, s)
+            f.copy_(saved)
+        torch.cuda.current_stream().wait_stream(s)
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self._launch(f, dt, torch.cuda.current_stream())
+        self._dt = dt
+        return self.graph
+
+    def replay(self, t):
+        """One captured step from time t (the graph reads the time factors from the device)."""
+        self._set_time(t, self._dt)
+        self.graph.replay()
+        return self._f_static
+
+
+def be_solve(plan, dt, b, x, restart=30, tol=1e-10, max_outer=60, inner_reduction=1e-5, mixed=True):
+    """Solve (I - dt A) x = b in place (FP64 CUDA tensors); returns the info dict."""
+    import torch
+
+    opts = GmresOpts(int(restart), int(max_outer), float(tol), float(inner_reduction), 1 if mixed else 0)
+    nbytes = C.c_size_t(0)
+    check(lib().asg_be_workspace(plan.handle, C.byref(opts), C.byref(nbytes)))
+    work = torch.empty(max(1, nbytes.value), dtype=torch.uint8, device=x.device)
+    info = GmresInfo()
+    check(lib().asg_be_solve(plan.handle, float(dt), C.c_void_p(b.data_ptr()), C.c_void_p(x.data_ptr()), C.byref(opts),
+                             C.byref(info), C.c_void_p(work.data_ptr()), nbytes.value,
+                             C.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    return {k: getattr(info, k) for k, _ in GmresInfo._fields_}
+
+
+def be_step(plan, f0, dt, source=None, **kw):
+    """f1 for backward Euler: (I - dt A) f1 = f0 + dt * source, initial guess f0."""
+    b = f0.clone() if source is None else f0 + dt * source
+    x = f0.clone()
+    info = be_solve(plan, dt, b, x, **kw)
+    return x, info

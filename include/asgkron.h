@@ -158,6 +158,44 @@ asg_status asg_connect_nd(int num_dims, long long num_elems, const int* levels, 
                           long long capacity, long long* num_pairs);
 
 /* ---------------------------------------------------------------------------------------
+ * Time steppers on the operator application (time_advance.m)
+ * ------------------------------------------------------------------------------------- */
+/* One RK3 step f <- f + dt (k1/6 + 2 k2/3 + k3/6), k_s = A y_s + src_s (RungeKutta3,
+ * time_advance.m:151-204, without LHS mass or boundary vectors).  d_src: host array of the
+ * three device source vectors at t, t+dt/2, t+dt (NULL array or entries = zero sources).
+ * d_work: device workspace of 4*dof values.  Asynchronous, allocation-free, capturable into a
+ * CUDA graph. */
+asg_status asg_rk3_step_f64(asg_plan* plan, double* d_f, double dt, const double* const* d_src, double* d_work,
+                            size_t work_bytes, void* stream);
+asg_status asg_rk3_step_f32(asg_plan* plan, float* d_f, double dt, const float* const* d_src, float* d_work,
+                            size_t work_bytes, void* stream);
+/* d_out = sum_s d_coef[s] * d_vecs[s] (the separable sources of source_vector.m: spatial parts
+ * times time factors); d_coef and d_vecs (an array of device pointers) live on the device. */
+asg_status asg_lincomb_f64(long long n, int ns, const double* d_coef, const double* const* d_vecs, double* d_out,
+                           void* stream);
+
+typedef struct {
+  int restart;             /* GMRES(m) Krylov dimension per cycle */
+  int max_outer;           /* refinement steps (each one GMRES cycle on the FP64 residual) */
+  double tol;              /* stop when ||b - (I - dt A) x|| <= tol * ||b|| */
+  double inner_reduction;  /* each cycle stops once its residual drops by this factor */
+  int mixed;               /* 1: FP32 operator application and basis inside GMRES; 0: all FP64 */
+} asg_gmres_opts;
+typedef struct {
+  int outer_iters;
+  int inner_iters;
+  int converged;
+  double rel_residual;     /* final FP64 ||b - (I - dt A) x|| / ||b|| */
+} asg_gmres_info;
+/* Backward Euler solve (I - dt A) x = b (backward_euler, time_advance.m:267-349, which
+ * assembles A and uses a direct solve): matrix-free GMRES(m) inside iterative refinement;
+ * the residual, the update of x and all Arnoldi dot products and norms are FP64.  d_x holds the
+ * initial guess on entry.  Synchronises the stream (one host read per Arnoldi step). */
+asg_status asg_be_workspace(const asg_plan* plan, const asg_gmres_opts* opts, size_t* bytes);
+asg_status asg_be_solve(asg_plan* plan, double dt, const double* d_b, double* d_x, const asg_gmres_opts* opts,
+                        asg_gmres_info* info, void* d_work, size_t work_bytes, void* stream);
+
+/* ---------------------------------------------------------------------------------------
  * Kronecker products and batched small GEMMs (Kronmult/)
  * All matrices are column-major; pointer arguments are device pointers unless stated.
  * ------------------------------------------------------------------------------------- */

@@ -1,0 +1,130 @@
+"""GPU time steppers: RK3 against the reference's gold trajectories and the oracle; backward
+Euler (mixed-precision GMRES + iterative refinement) against a direct solve."""
+import os
+
+import numpy as np
+import pytest
+
+from cases import rel2
+from oracle import asgard_oracle as O
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+G = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="module")
+def dev():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch.device("cuda:0")
+
+
+@pytest.mark.parametrize("name,pdename,lev,deg", [("continuity2_sg_l4_d3", "continuity2", 4, 3),
+                                                  ("continuity3_sg_l4_d3", "continuity3", 4, 3),
+                                                  ("continuity2_sg_l2_d2", "continuity2", 2, 2)])
+@pytest.mark.parametrize("graph", [False, True])
+def test_rk3_matches_gold_trajectory(dev, name, pdename, lev, deg, graph):
+    """5 RK3 steps at CFL 0.01 on the GPU reproduce gold/generated-inputs/time_advance (central
+    flux, operators built at max_lev 8, sources without the mass solve, as the gold was made)."""
+    import asgkron
+    from asgkron import pdes
+    from asgkron.steppers import RK3Stepper
+
+    pde = getattr(pdes, pdename)(lev, 0.0)
+    table = asgkron.hash_table_sparse_nD(pde.levels, 8)
+    idx = table.idx1d()
+    mats = pde.term_mats(deg, construction_level=8)
+    plan = asgkron.Plan.create(mats, idx, deg)
+    st = RK3Stepper(plan, pde, idx)
+    f = torch.from_numpy(pde.initial_condition(deg, idx)).to(dev)
+    dt = pde.dt(0.01)
+    gold = np.load(os.path.join(G, "time_advance.npz"))
+    if graph:
+        st.capture(f, dt)
+    for i in range(5):
+        if graph:
+            st.replay(i * dt)
+        else:
+            st.step(f, i * dt, dt)
+        torch.cuda.synchronize()
+        g = gold["%s_t%d" % (name, i)]
+        assert rel2(f.cpu().numpy(), g) <= 1e-13, i
+
+
+def test_rk3_cfg1_lf_upwind_vs_oracle(dev):
+    """The CPU-runnable configuration: continuity2 lev 4 deg 2 (current PDE file, LF = -1),
+    5 RK3 steps at CFL 0.01: GPU FP64 vs the oracle's RK3; FP32 within 1e-6."""
+    import asgkron
+    from asgkron import pdes
+    from asgkron.steppers import RK3Stepper
+
+    pde = pdes.continuity2(4)
+    opde = O.continuity2(4)
+    table = asgkron.hash_table_sparse_nD(pde.levels, 8)
+    idx = table.idx1d()
+    mats = pde.term_mats(2)
+    plan = asgkron.Plan.create(mats, idx, 2)
+    f0 = np.random.default_rng(0).standard_normal(plan.dof)
+    dt = pde.dt(0.01)
+    _, blocks = O.operator_two_scale(2, 8)
+    idx64 = idx.astype(np.int64)
+    omats = O.build_term_mats(opde, 2)
+    fo = f0.copy()
+    for i in range(5):
+        fo = O.rk3_step(lambda v: O.apply_A_rows(omats, idx64, 2, v), fo, i * dt, dt,
+                        lambda t: O.md_eval(opde, 2, opde.sources, idx64, blocks, t))
+    for dtype, tol in (("float64", 1e-12), ("float32", 1e-6)):
+        st = RK3Stepper(plan, pde, idx, dtype=dtype)
+        f = torch.from_numpy(f0).to(dev, torch.float64 if dtype == "float64" else torch.float32)
+        for i in range(5):
+            st.step(f, i * dt, dt)
+        torch.cuda.synchronize()
+        assert rel2(f.double().cpu().numpy(), fo) <= tol, dtype
+
+
+@pytest.mark.parametrize("mixed", [True, False])
+def test_be_solve_vs_direct(dev, mixed):
+    """diffusion2 LDG (Dirichlet zero), lev 4 deg 3: (I - dt A) x = b by GMRES/IR vs a dense
+    direct solve of the oracle-assembled A (the reference's AA \\ b, time_advance.m:349)."""
+    import asgkron
+    from asgkron import pdes
+    from asgkron.steppers import be_step
+
+    pde = pdes.diffusion2(4)
+    table = asgkron.hash_table_sparse_nD(pde.levels, 8)
+    idx = table.idx1d()
+    mats = pde.term_mats(3)
+    plan = asgkron.Plan.create(mats, idx, 3)
+    f0 = pde.initial_condition(3, idx) + 1e-3 * np.random.default_rng(2).standard_normal(plan.dof)
+    dt = pde.dt(1.0)
+    _, A = O.apply_A_loop(mats, idx.astype(np.int64), 3, f0, build_A=True)
+    want = O.backward_euler_step(A, f0, dt, np.zeros_like(f0))
+    x, info = be_step(plan, torch.from_numpy(f0).to(dev), dt, mixed=mixed, tol=1e-10)
+    assert info["converged"] and info["rel_residual"] <= 1e-10, info
+    assert rel2(x.cpu().numpy(), want) <= 1e-9
+
+
+def test_be_cfg3_ten_steps_mixed_vs_fp64(dev):
+    """Implicit configuration: diffusion2 SG lev 8, deg 4 (20,480 DOF), dt = h^2, 10 steps from
+    sin(pi x) sin(pi y) + 1e-3 N(0,1) (seed 2): mixed GMRES(30) and FP64 GMRES(30) both reach
+    1e-10 relative residual each step and agree."""
+    import asgkron
+    from asgkron import pdes
+    from asgkron.steppers import be_step
+
+    pde = pdes.diffusion2(8)
+    table = asgkron.hash_table_sparse_nD(pde.levels, 8)
+    idx = table.idx1d()
+    mats = pde.term_mats(4)
+    plan = asgkron.Plan.create(mats, idx, 4)
+    f0 = pde.initial_condition(4, idx) + 1e-3 * np.random.default_rng(2).standard_normal(plan.dof)
+    dt = pde.dt(1.0)
+    fm = torch.from_numpy(f0).to(dev)
+    fd = fm.clone()
+    for step in range(10):
+        fm, im = be_step(plan, fm, dt, mixed=True)
+        fd, idd = be_step(plan, fd, dt, mixed=False)
+        assert im["converged"] and im["rel_residual"] <= 1e-10, (step, im)
+        assert idd["converged"] and idd["rel_residual"] <= 1e-10, (step, idd)
+    assert rel2(fm.cpu().numpy(), fd.cpu().numpy()) <= 1e-9
