@@ -120,6 +120,10 @@ struct asg_plan {
   long long* d_tr_row_ptr = nullptr;
   int* d_tr_ent = nullptr;
   std::vector<double> h64;           // packed FP64 blocks (host copy: transposes and gradients)
+  bool all_pairs = true;             // listed pairs: all, or the CSR below (0-based)
+  std::vector<long long> pr_ptr;
+  std::vector<int> pr_col;
+  std::vector<std::vector<uint8_t>> zero_blk;  // per (t,d): block (a,b) is zero (DETECT mode)
   asg_plan* tr = nullptr;            // transposed plan (A^T), built on first use
   // gradient targets (built on first use)
   std::vector<long long> g_ptr;

@@ -258,20 +258,51 @@ asg_status check_ptr(const void* ptr, const char* name);
 
 // Gradient targets: every (t, k, alpha, beta) block of an applied factor that some work
 // entry touches, with its contributing entries in work-list order (deterministic sums).
+// The derivative with respect to factor k is nonzero even where k's own block is zero, so the
+// contributors are all listed pairs whose identity dimensions match and whose other applied
+// factors have nonzero blocks (not only the forward work entries).
 asg_status build_grad(asg_plan* p) {
   if (p->d_g_ptr) return ASG_OK;
-  const int D = p->D;
+  const int D = p->D, N = p->N;
   std::map<long long, std::vector<GradContrib>> tg;
-  for (int i = 0; i < p->N; ++i)
-    for (long long q = p->row_ptr[i]; q < p->row_ptr[i + 1]; ++q) {
-      const int j = p->ent[q] >> 4, t = p->ent[q] & 15;
-      for (int k = 0; k < D; ++k) {
-        if (!((p->active[t] >> k) & 1u)) continue;
-        const long long key = (static_cast<long long>(t * D + k) << 48) |
-                              (static_cast<long long>(p->idx1d[i * D + k]) << 24) | p->idx1d[j * D + k];
-        tg[key].push_back({i, j, t, k});
-      }
+  auto blk_zero = [&](int t, int m, int i, int j) {
+    const auto& zb = p->zero_blk[t * D + m];
+    return !zb.empty() && zb[static_cast<size_t>(p->idx1d[i * D + m]) * p->op_nb[t * D + m] + p->idx1d[j * D + m]];
+  };
+  auto add = [&](int i, int j, int t) {
+    for (int m = 0; m < D; ++m)
+      if (!((p->active[t] >> m) & 1u) && p->idx1d[i * D + m] != p->idx1d[j * D + m]) return;
+    for (int k = 0; k < D; ++k) {
+      if (!((p->active[t] >> k) & 1u)) continue;
+      bool others_nonzero = true;
+      for (int m = 0; m < D && others_nonzero; ++m)
+        if (m != k && ((p->active[t] >> m) & 1u) && blk_zero(t, m, i, j)) others_nonzero = false;
+      if (!others_nonzero) continue;
+      const long long key = (static_cast<long long>(t * D + k) << 48) |
+                            (static_cast<long long>(p->idx1d[i * D + k]) << 24) | p->idx1d[j * D + k];
+      tg[key].push_back({i, j, t, k});
     }
+  };
+  for (int t = 0; t < p->T; ++t) {
+    if (p->all_pairs) {
+      std::map<std::vector<int>, std::vector<int>> groups;  // columns by identity-dimension indices
+      for (int e = 0; e < N; ++e) {
+        std::vector<int> key;
+        for (int m = 0; m < D; ++m)
+          if (!((p->active[t] >> m) & 1u)) key.push_back(p->idx1d[e * D + m]);
+        groups[key].push_back(e);
+      }
+      for (int i = 0; i < N; ++i) {
+        std::vector<int> key;
+        for (int m = 0; m < D; ++m)
+          if (!((p->active[t] >> m) & 1u)) key.push_back(p->idx1d[i * D + m]);
+        for (int j : groups[key]) add(i, j, t);
+      }
+    } else {
+      for (int i = 0; i < N; ++i)
+        for (long long q = p->pr_ptr[i]; q < p->pr_ptr[i + 1]; ++q) add(i, p->pr_col[q], t);
+    }
+  }
   p->g_ptr.assign(1, 0);
   p->g_contrib.clear();
   p->g_tgt.clear();
@@ -471,7 +502,8 @@ asg_status asg_plan_create(const asg_plan_desc* desc, asg_plan** out) {
   p->op_nb.assign(static_cast<size_t>(T) * D, 0);
   p->op_off.assign(static_cast<size_t>(T) * D, -1);
   p->active.assign(T, 0u);
-  std::vector<std::vector<uint8_t>> zero_blk(static_cast<size_t>(T) * D);
+  std::vector<std::vector<uint8_t>>& zero_blk = p->zero_blk;
+  zero_blk.assign(static_cast<size_t>(T) * D, {});
   const bool detect = desc->structure == ASG_STRUCT_DETECT;
   for (int t = 0; t < T; ++t)
     for (int m = 0; m < D; ++m) {
@@ -525,6 +557,10 @@ asg_status asg_plan_create(const asg_plan_desc* desc, asg_plan** out) {
       if (j < 0 || j >= N) return bail(fail(ASG_ERR_INVALID, "cols[%lld]=%d outside the element table", q, desc->cols[q]));
     }
     p->pairs = desc->row_ptr[N];
+    p->all_pairs = false;
+    p->pr_ptr.assign(desc->row_ptr, desc->row_ptr + N + 1);
+    p->pr_col.resize(desc->row_ptr[N]);
+    for (long long q = 0; q < desc->row_ptr[N]; ++q) p->pr_col[q] = desc->cols[q] - base;
   } else {
     p->pairs = static_cast<long long>(N) * N;
   }

@@ -118,7 +118,8 @@ asg_status asg_apply_f32(asg_plan* plan, const float* d_f, float* d_y, void* str
 asg_status asg_apply_T_f64(asg_plan* plan, const double* d_ybar, double* d_fbar, void* stream);
 asg_status asg_apply_T_f32(asg_plan* plan, const float* d_ybar, float* d_fbar, void* stream);
 /* Gradient of a scalar L with cotangent r = dL/dy (y = A f) with respect to every applied
- * 1-D operator (t, k): the P x P blocks that some work entry touches are written (not added)
+ * 1-D operator (t, k), including its zero blocks (the derivative there is generally nonzero):
+ * every block some listed pair reaches is written (not added)
  * into G[t*d+k] (device, column-major, leading dimension ldg[t*d+k]); all other entries of G
  * are left as they are, so zero G first for the full gradient.  G[t*d+k] may be NULL to skip;
  * identity factors detected by ASG_STRUCT_DETECT are not differentiated.  G and ldg are host
