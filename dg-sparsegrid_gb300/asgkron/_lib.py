@@ -127,6 +127,14 @@ SIGNATURES = {
     "asg_kron_batch_f64": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), _P, _P, _P, C.c_size_t, _P]),
     "asg_kron_batch_f32": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), _P, _P, _P, C.c_size_t, _P]),
     "asg_krond_f64": (C.c_int, [C.c_int, _I, _I, C.POINTER(C.c_void_p), _P, _P]),
+    "asg_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),
+    "asg_batch_destroy": (C.c_int, [C.c_void_p]),
+    "asg_batch_set_io_f64": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+    "asg_batch_set_io_f32": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+    "asg_batch_prepare": (C.c_int, [C.c_void_p, C.c_int]),
+    "asg_batch_apply": (C.c_int, [C.c_void_p, C.c_int, _P]),
+    "asg_batch_tune": (C.c_int, [C.c_void_p, C.c_int, _P, C.POINTER(C.c_float)]),
+    "asg_batch_info": (C.c_int, [C.c_void_p, _I, _I, C.POINTER(C.c_double)]),
     "asg_rk3_step_f64": (C.c_int, [C.c_void_p, _P, C.c_double, C.POINTER(C.c_void_p), _P, C.c_size_t, _P]),
     "asg_rk3_step_f32": (C.c_int, [C.c_void_p, _P, C.c_double, C.POINTER(C.c_void_p), _P, C.c_size_t, _P]),
     "asg_lincomb_f64": (C.c_int, [C.c_longlong, C.c_int, _P, _P, _P, _P]),

@@ -1,0 +1,66 @@
+"""Many independent y_k = A_k f_k in one persistent launch (asg_batch_*), optionally captured
+into a CUDA graph."""
+import ctypes as C
+
+from ._lib import check, lib
+
+
+class Batch:
+    def __init__(self, plans):
+        self.plans = list(plans)
+        arr = (C.c_void_p * len(self.plans))(*[p.handle for p in self.plans])
+        self._h = C.c_void_p()
+        check(lib().asg_batch_create(arr, len(self.plans), C.byref(self._h)))
+        self.graph = None
+
+    def set_io(self, fs, ys):
+        """Device tensors per problem (all float64 or all float32); uploads the problem table."""
+        import torch
+
+        self._io = (list(fs), list(ys))
+        fp = (C.c_void_p * len(fs))(*[f.data_ptr() for f in fs])
+        yp = (C.c_void_p * len(ys))(*[y.data_ptr() for y in ys])
+        self.precision = 0 if fs[0].dtype == torch.float64 else 1
+        fn = lib().asg_batch_set_io_f64 if self.precision == 0 else lib().asg_batch_set_io_f32
+        check(fn(self._h, fp, yp))
+        check(lib().asg_batch_prepare(self._h, self.precision))
+
+    def apply(self, stream=None):
+        import torch
+
+        s = stream if stream is not None else torch.cuda.current_stream()
+        check(lib().asg_batch_apply(self._h, self.precision, C.c_void_p(s.cuda_stream)))
+
+    def tune(self):
+        import torch
+
+        ms = C.c_float(0)
+        check(lib().asg_batch_tune(self._h, self.precision, C.c_void_p(torch.cuda.current_stream().cuda_stream),
+                                   C.byref(ms)))
+        return ms.value
+
+    def info(self):
+        w, r, fl = C.c_int(0), C.c_int(0), C.c_double(0)
+        check(lib().asg_batch_info(self._h, C.byref(w), C.byref(r), C.byref(fl)))
+        return {"warps_per_cta": w.value, "rows_per_item": r.value, "flops": fl.value}
+
+    def capture(self):
+        import torch
+
+        self.apply()
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            self.apply()
+        return self.graph
+
+    def close(self):
+        if self._h:
+            lib().asg_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

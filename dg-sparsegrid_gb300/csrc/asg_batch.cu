@@ -1,0 +1,365 @@
+// Many independent operator applications in one persistent launch.
+//
+// A batch is built from existing plans whose element blocks hold at most 256 values.  Its
+// packed work list holds (problem, first row) items of `rows_per_item` rows, sorted by
+// descending cost (chain flops); persistent warps take items from a device counter (reset
+// by a memset in the same stream, so the launch is graph-capturable) and run the warp chain
+// algorithm of the single-problem kernel for each row, dispatching on the problem's degree.
+// Each row is still computed by one warp in a fixed order: results do not depend on which
+// warp took the item.  A tuner times (warps per CTA, rows per item) candidates.
+#include <algorithm>
+#include <new>
+#include <vector>
+
+#include "asg_internal.h"
+
+namespace asg {
+namespace {
+
+struct BatchProblem {
+  const void* f;
+  void* y;
+  const double* ops64;
+  const float* ops32;
+  const long long* op_off;
+  const int* op_nb;
+  const int* idx1d;
+  const long long* row_ptr;
+  const int* ent;
+  const unsigned* active;
+  int N, D, B, P;
+  int stride[kMaxDims];
+};
+
+struct BatchItem {
+  int prob;
+  int row;
+};
+
+template <typename T>
+__device__ __forceinline__ void team_copy_w(T* dst, const T* src, int n, int lane) {
+  for (int k = lane; k < n; k += 32) dst[k] = src[k];
+}
+
+template <typename T, int P>
+__device__ __forceinline__ void warp_row(const BatchProblem& pb, int row, T* buf0, T* buf1, int lane) {
+  constexpr int MAXE = 8;
+  constexpr bool KAHAN = sizeof(T) == 4;
+  const T* f = static_cast<const T*>(pb.f);
+  T* y = static_cast<T*>(pb.y);
+  const T* ops = sizeof(T) == 8 ? reinterpret_cast<const T*>(pb.ops64) : reinterpret_cast<const T*>(pb.ops32);
+  const int B = pb.B, D = pb.D;
+  T acc[MAXE], cmp[MAXE];
+#pragma unroll
+  for (int k = 0; k < MAXE; ++k) acc[k] = cmp[k] = T(0);
+  const long long q1 = pb.row_ptr[row + 1];
+  for (long long q = pb.row_ptr[row]; q < q1; ++q) {
+    const int e = pb.ent[q];
+    const int j = e >> 4, t = e & 15;
+    const unsigned act = pb.active[t];
+    team_copy_w(buf0, f + static_cast<size_t>(j) * B, B, lane);
+    __syncwarp();
+    T* in = buf0;
+    T* out = buf1;
+    for (int m = D - 1; m >= 0; --m) {
+      if (!((act >> m) & 1u)) continue;
+      const int tm = t * D + m;
+      const T* Ag = ops + pb.op_off[tm] +
+                    (static_cast<long long>(pb.idx1d[row * D + m]) * pb.op_nb[tm] + pb.idx1d[j * D + m]) * (P * P);
+      T A[P * P];
+#pragma unroll
+      for (int r = 0; r < P * P; ++r) A[r] = Ag[r];
+      const int s = pb.stride[m];
+      for (int fi = lane; fi < B / P; fi += 32) {
+        const int hi = fi / s, lo = fi - hi * s;
+        const int base = hi * s * P + lo;
+        T x[P];
+#pragma unroll
+        for (int b = 0; b < P; ++b) x[b] = in[base + b * s];
+#pragma unroll
+        for (int a = 0; a < P; ++a) {
+          T sum = A[a * P] * x[0];
+#pragma unroll
+          for (int b = 1; b < P; ++b) sum = fma(A[a * P + b], x[b], sum);
+          out[base + a * s] = sum;
+        }
+      }
+      __syncwarp();
+      T* tmp = in;
+      in = out;
+      out = tmp;
+    }
+#pragma unroll
+    for (int k = 0; k < MAXE; ++k) {
+      const int idx = lane + 32 * k;
+      if (idx < B) {
+        if (KAHAN) {
+          const T yv = in[idx] - cmp[k];
+          const T tt = acc[k] + yv;
+          cmp[k] = (tt - acc[k]) - yv;
+          acc[k] = tt;
+        } else {
+          acc[k] += in[idx];
+        }
+      }
+    }
+    __syncwarp();
+  }
+  T* yr = y + static_cast<size_t>(row) * B;
+#pragma unroll
+  for (int k = 0; k < MAXE; ++k) {
+    const int idx = lane + 32 * k;
+    if (idx < B) yr[idx] = acc[k];
+  }
+}
+
+template <typename T>
+__global__ void k_batch(const BatchProblem* __restrict__ probs, const BatchItem* __restrict__ items, int nitems,
+                        int rows_per_item, int* counter) {
+  __shared__ __align__(16) T sbuf[8][2][256];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T* buf0 = sbuf[warp][0];
+  T* buf1 = sbuf[warp][1];
+  while (true) {
+    int it = 0;
+    if (lane == 0) it = atomicAdd(counter, 1);
+    it = __shfl_sync(0xffffffffu, it, 0);
+    if (it >= nitems) break;
+    const BatchItem w = items[it];
+    const BatchProblem pb = probs[w.prob];
+    const int r1 = min(pb.N, w.row + rows_per_item);
+    for (int row = w.row; row < r1; ++row) {
+      switch (pb.P) {
+        case 1: warp_row<T, 1>(pb, row, buf0, buf1, lane); break;
+        case 2: warp_row<T, 2>(pb, row, buf0, buf1, lane); break;
+        case 3: warp_row<T, 3>(pb, row, buf0, buf1, lane); break;
+        case 4: warp_row<T, 4>(pb, row, buf0, buf1, lane); break;
+        default: break;  // rejected at batch creation
+      }
+    }
+  }
+}
+
+}  // namespace
+}  // namespace asg
+
+struct asg_batch {
+  std::vector<asg_plan*> plans;
+  std::vector<asg::BatchProblem> probs;  // host copy (pointers filled per precision)
+  asg::BatchProblem* d_probs = nullptr;
+  asg::BatchItem* d_items[3] = {nullptr, nullptr, nullptr};  // per rows_per_item choice
+  int nitems[3] = {0, 0, 0};
+  int* d_counter = nullptr;
+  int wpb = 4;          // tuned warps per CTA
+  int rpi_choice = 0;   // tuned rows per item (index into kRowsPerItem)
+  int io_set = 0;       // bit 0: FP64 io set, bit 1: FP32 io set
+  std::vector<const void*> f64, f32;
+  std::vector<void*> y64, y32;
+  double flops = 0;
+};
+
+namespace {
+constexpr int kRowsPerItem[3] = {1, 2, 4};
+
+asg_status upload_probs(asg_batch* b, bool f32) {
+  for (size_t k = 0; k < b->probs.size(); ++k) {
+    b->probs[k].f = f32 ? b->f32[k] : b->f64[k];
+    b->probs[k].y = f32 ? b->y32[k] : b->y64[k];
+  }
+  ASG_CUDA(cudaMemcpy(b->d_probs, b->probs.data(), b->probs.size() * sizeof(asg::BatchProblem),
+                      cudaMemcpyHostToDevice));
+  return ASG_OK;
+}
+}  // namespace
+
+using asg::fail;
+
+extern "C" {
+
+asg_status asg_batch_create(asg_plan* const* plans, int count, asg_batch** out) {
+  if (!plans || !out || count < 1) return fail(ASG_ERR_INVALID, "batch_create: bad arguments");
+  *out = nullptr;
+  asg_batch* b = new (std::nothrow) asg_batch;
+  if (!b) return fail(ASG_ERR_NOMEM, "batch_create: out of host memory");
+  struct Cost {
+    double c;
+    int prob, row;
+  };
+  std::vector<Cost> rows;
+  for (int k = 0; k < count; ++k) {
+    asg_plan* p = plans[k];
+    if (!p) {
+      delete b;
+      return fail(ASG_ERR_INVALID, "batch_create: plan %d is NULL", k);
+    }
+    if (p->B > 256 || p->P > 4) {
+      delete b;
+      return fail(ASG_ERR_UNSUPPORTED, "batch_create: plan %d has deg^d=%d (batch rows need <= 256, deg <= 4)", k, p->B);
+    }
+    b->plans.push_back(p);
+    asg::BatchProblem pb{};
+    pb.ops64 = p->d_ops64;
+    pb.ops32 = p->d_ops32;
+    pb.op_off = p->d_op_off;
+    pb.op_nb = p->d_op_nb;
+    pb.idx1d = p->d_idx1d;
+    pb.row_ptr = p->d_row_ptr;
+    pb.ent = p->d_ent;
+    pb.active = p->d_active;
+    pb.N = p->N;
+    pb.D = p->D;
+    pb.B = p->B;
+    pb.P = p->P;
+    int sd = 1;
+    for (int m = p->D - 1; m >= 0; --m) {
+      pb.stride[m] = sd;
+      sd *= p->P;
+    }
+    b->probs.push_back(pb);
+    b->flops += p->flops_exec;
+    double pd1 = 1.0;
+    for (int q = 0; q <= p->D; ++q) pd1 *= p->P;
+    for (int i = 0; i < p->N; ++i) {
+      double c = 0;
+      for (long long q = p->row_ptr[i]; q < p->row_ptr[i + 1]; ++q)
+        c += 2.0 * pd1 * (1 + __builtin_popcount(p->active[p->ent[q] & 15]));
+      rows.push_back({c, k, i});
+    }
+  }
+  b->f64.assign(count, nullptr);
+  b->f32.assign(count, nullptr);
+  b->y64.assign(count, nullptr);
+  b->y32.assign(count, nullptr);
+  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&b->d_probs), count * sizeof(asg::BatchProblem));
+  if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&b->d_counter), sizeof(int));
+  for (int c = 0; c < 3 && e == cudaSuccess; ++c) {
+    // items of kRowsPerItem[c] consecutive rows, most expensive first
+    std::vector<std::pair<double, asg::BatchItem>> its;
+    for (size_t q = 0; q < rows.size();) {
+      const int prob = rows[q].prob;
+      double cost = 0;
+      const int r0 = rows[q].row;
+      int n = 0;
+      while (q < rows.size() && rows[q].prob == prob && n < kRowsPerItem[c]) {
+        cost += rows[q].c;
+        ++q;
+        ++n;
+      }
+      its.push_back({cost, {prob, r0}});
+    }
+    std::stable_sort(its.begin(), its.end(), [](const auto& x, const auto& y) { return x.first > y.first; });
+    std::vector<asg::BatchItem> v;
+    for (auto& x : its) v.push_back(x.second);
+    b->nitems[c] = static_cast<int>(v.size());
+    e = cudaMalloc(reinterpret_cast<void**>(&b->d_items[c]), v.size() * sizeof(asg::BatchItem));
+    if (e == cudaSuccess) e = cudaMemcpy(b->d_items[c], v.data(), v.size() * sizeof(asg::BatchItem), cudaMemcpyHostToDevice);
+  }
+  if (e != cudaSuccess) {
+    asg_status st = asg::cuda_fail(e, "batch_create upload");
+    asg_batch_destroy(b);
+    return st;
+  }
+  *out = b;
+  return ASG_OK;
+}
+
+asg_status asg_batch_destroy(asg_batch* b) {
+  if (!b) return ASG_OK;
+  cudaFree(b->d_probs);
+  cudaFree(b->d_counter);
+  for (auto* p : b->d_items) cudaFree(p);
+  delete b;
+  return ASG_OK;
+}
+
+asg_status asg_batch_set_io_f64(asg_batch* b, const double* const* f, double* const* y) {
+  if (!b || !f || !y) return fail(ASG_ERR_INVALID, "batch_set_io: NULL argument");
+  for (size_t k = 0; k < b->plans.size(); ++k) {
+    if (!f[k] || !y[k] || f[k] == y[k]) return fail(ASG_ERR_INVALID, "batch_set_io: bad buffers for problem %zu", k);
+    b->f64[k] = f[k];
+    b->y64[k] = y[k];
+  }
+  b->io_set |= 1;
+  return ASG_OK;
+}
+
+asg_status asg_batch_set_io_f32(asg_batch* b, const float* const* f, float* const* y) {
+  if (!b || !f || !y) return fail(ASG_ERR_INVALID, "batch_set_io: NULL argument");
+  for (size_t k = 0; k < b->plans.size(); ++k) {
+    if (!f[k] || !y[k] || f[k] == y[k]) return fail(ASG_ERR_INVALID, "batch_set_io: bad buffers for problem %zu", k);
+    b->f32[k] = f[k];
+    b->y32[k] = y[k];
+  }
+  b->io_set |= 2;
+  return ASG_OK;
+}
+
+// Uploads the problem table for the precision (synchronous); apply then only launches.
+asg_status asg_batch_prepare(asg_batch* b, int precision) {
+  if (!b) return fail(ASG_ERR_INVALID, "batch_prepare: NULL batch");
+  const bool f32 = precision == 1;
+  if (!(b->io_set & (f32 ? 2 : 1))) return fail(ASG_ERR_INVALID, "batch_prepare: buffers not set for this precision");
+  return upload_probs(b, f32);
+}
+
+asg_status asg_batch_apply(asg_batch* b, int precision, void* stream) {
+  if (!b) return fail(ASG_ERR_INVALID, "batch_apply: NULL batch");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  ASG_CUDA(cudaMemsetAsync(b->d_counter, 0, sizeof(int), s));
+  const int c = b->rpi_choice;
+  const int grid = 152 * (b->wpb == 4 ? 8 : 4);
+  if (precision == 1)
+    asg::k_batch<float><<<grid, b->wpb * 32, 0, s>>>(b->d_probs, b->d_items[c], b->nitems[c], kRowsPerItem[c],
+                                                     b->d_counter);
+  else
+    asg::k_batch<double><<<grid, b->wpb * 32, 0, s>>>(b->d_probs, b->d_items[c], b->nitems[c], kRowsPerItem[c],
+                                                      b->d_counter);
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? ASG_OK : asg::cuda_fail(e, "batch launch");
+}
+
+asg_status asg_batch_tune(asg_batch* b, int precision, void* stream, float* best_ms) {
+  if (!b) return fail(ASG_ERR_INVALID, "batch_tune: NULL batch");
+  asg_status st = asg_batch_prepare(b, precision);
+  if (st) return st;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaEvent_t e0, e1;
+  ASG_CUDA(cudaEventCreate(&e0));
+  ASG_CUDA(cudaEventCreate(&e1));
+  float best = 1e30f;
+  int bw = 4, bc = 0;
+  for (int wpb : {4, 8})
+    for (int c = 0; c < 3; ++c) {
+      b->wpb = wpb;
+      b->rpi_choice = c;
+      if ((st = asg_batch_apply(b, precision, stream))) return st;  // warm-up
+      ASG_CUDA(cudaEventRecord(e0, s));
+      for (int r = 0; r < 3; ++r)
+        if ((st = asg_batch_apply(b, precision, stream))) return st;
+      ASG_CUDA(cudaEventRecord(e1, s));
+      ASG_CUDA(cudaEventSynchronize(e1));
+      float ms = 0;
+      ASG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms < best) {
+        best = ms;
+        bw = wpb;
+        bc = c;
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  b->wpb = bw;
+  b->rpi_choice = bc;
+  if (best_ms) *best_ms = best / 3;
+  return ASG_OK;
+}
+
+asg_status asg_batch_info(const asg_batch* b, int* warps_per_cta, int* rows_per_item, double* flops) {
+  if (!b) return fail(ASG_ERR_INVALID, "batch_info: NULL batch");
+  if (warps_per_cta) *warps_per_cta = b->wpb;
+  if (rows_per_item) *rows_per_item = kRowsPerItem[b->rpi_choice];
+  if (flops) *flops = b->flops;
+  return ASG_OK;
+}
+
+}  // extern "C"

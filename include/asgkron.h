@@ -159,6 +159,27 @@ asg_status asg_connect_nd(int num_dims, long long num_elems, const int* levels, 
                           long long capacity, long long* num_pairs);
 
 /* ---------------------------------------------------------------------------------------
+ * Many independent problems in one persistent launch (no reference counterpart: the
+ * prototype applies one operator at a time)
+ * ------------------------------------------------------------------------------------- */
+typedef struct asg_batch asg_batch;
+/* A batch over existing plans (deg <= 4, deg^d <= 256); the plans must outlive it.  The packed
+ * work list holds (problem, row block) items, most expensive first. */
+asg_status asg_batch_create(asg_plan* const* plans, int count, asg_batch** batch);
+asg_status asg_batch_destroy(asg_batch* batch);
+/* Device input/output vectors of every problem (host arrays of device pointers). */
+asg_status asg_batch_set_io_f64(asg_batch* batch, const double* const* d_f, double* const* d_y);
+asg_status asg_batch_set_io_f32(asg_batch* batch, const float* const* d_f, float* const* d_y);
+/* Uploads the problem table for a precision (0 FP64, 1 FP32); call after set_io and before
+ * apply / graph capture. */
+asg_status asg_batch_prepare(asg_batch* batch, int precision);
+/* y_k = A_k f_k for every problem: one counter reset and one persistent launch (capturable). */
+asg_status asg_batch_apply(asg_batch* batch, int precision, void* stream);
+/* Times (warps per CTA, rows per work item) candidates and keeps the fastest. */
+asg_status asg_batch_tune(asg_batch* batch, int precision, void* stream, float* best_ms);
+asg_status asg_batch_info(const asg_batch* batch, int* warps_per_cta, int* rows_per_item, double* flops);
+
+/* ---------------------------------------------------------------------------------------
  * Time steppers on the operator application (time_advance.m)
  * ------------------------------------------------------------------------------------- */
 /* One RK3 step f <- f + dt (k1/6 + 2 k2/3 + k3/6), k_s = A y_s + src_s (RungeKutta3,
