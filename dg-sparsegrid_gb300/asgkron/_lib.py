@@ -126,6 +126,7 @@ SIGNATURES = {
     "asg_kron_plan_lists": (C.c_int, [C.c_void_p, C.POINTER(GemmDesc), C.c_int, _I]),
     "asg_kron_batch_f64": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), _P, _P, _P, C.c_size_t, _P]),
     "asg_kron_batch_f32": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), _P, _P, _P, C.c_size_t, _P]),
+    "asg_kron_batch_static_f64": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), _P, _P, _P]),
     "asg_krond_f64": (C.c_int, [C.c_int, _I, _I, C.POINTER(C.c_void_p), _P, _P]),
     "asg_batch_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int, C.POINTER(C.c_void_p)]),
     "asg_batch_destroy": (C.c_int, [C.c_void_p]),

@@ -5,6 +5,7 @@
 //   asg_krond_*           krond.m: the explicit Kronecker product
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -428,3 +429,107 @@ asg_status asg_krond_f64(int nkron, const int* nrow, const int* ncol, const doub
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free executor: asg_kron_batch_static_f64.
+//
+// For callers that may not allocate device memory at call time -- code running where
+// cudaMalloc is not allowed or not wanted (inside a host callback, under an allocator that
+// is being torn down, in a time-critical loop that must not synchronise the device), or a
+// caller that owns no allocator at all.  The recursion's temporaries live in one fixed
+// device array that this file declares; the GEMM descriptors travel in the launch
+// parameters, so nothing is uploaded and nothing is allocated.
+//
+// Contract:
+//  * the first call on each device (that device current) looks up the array's address once;
+//    make that first call before any stream capture;
+//  * plans whose workspace exceeds ASG_KRON_STATIC_SCRATCH_BYTES are rejected with
+//    ASG_ERR_CAPACITY before anything is launched;
+//  * every call on a device shares the one array and it keeps the previous call's values.
+//    Nothing in it has to start at zero: every temporary element is written (beta = 0
+//    GEMMs) before any GEMM reads it.  Calls whose launches overlap on the GPU (different
+//    streams, or host threads racing on one device) overwrite each other's temporaries:
+//    the caller must order them.
+// ---------------------------------------------------------------------------------------
+static __device__ __align__(256) double g_kron_scratch[ASG_KRON_STATIC_SCRATCH_BYTES / sizeof(double)];
+
+namespace asg {
+namespace {
+
+constexpr int kStaticChunk = 48;  // descriptors per launch, carried by value
+constexpr int kStaticMaxDevices = 64;
+
+struct KChunk {
+  KDev d[kStaticChunk];
+  int count;
+};
+static_assert(sizeof(KChunk) + sizeof(KBases<double>) <= 4096, "launch parameters exceed 4 KB");
+
+__global__ void k_kron_level_static(const KChunk chunk, KBases<double> b) {
+  for (int p = blockIdx.x; p < chunk.count; p += gridDim.x) {
+    const KDev e = chunk.d[p];
+    double* c = const_cast<double*>(kop(b, e.c_id, e.c_off));
+    cta_gemm<double>(e.ta, e.tb, e.m, e.n, e.k, 1.0, kop(b, e.a_id, e.a_off), e.lda, kop(b, e.b_id, e.b_off), e.ldb,
+                     0.0, c, e.ldc);
+  }
+}
+
+std::once_flag g_scratch_once[kStaticMaxDevices];
+double* g_scratch_ptr[kStaticMaxDevices];
+cudaError_t g_scratch_err[kStaticMaxDevices];
+
+// The array's device address for the current device, looked up once per device.
+asg_status static_scratch(double** out) {
+  int dev = 0;
+  ASG_CUDA(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kStaticMaxDevices)
+    return fail(ASG_ERR_UNSUPPORTED, "kron_batch_static: device %d beyond the %d supported", dev, kStaticMaxDevices);
+  std::call_once(g_scratch_once[dev], [dev] {
+    void* ptr = nullptr;
+    g_scratch_err[dev] = cudaGetSymbolAddress(&ptr, g_kron_scratch);
+    g_scratch_ptr[dev] = static_cast<double*>(ptr);
+  });
+  if (g_scratch_err[dev] != cudaSuccess) return cuda_fail(g_scratch_err[dev], "cudaGetSymbolAddress(kron scratch)");
+  *out = g_scratch_ptr[dev];
+  return ASG_OK;
+}
+
+}  // namespace
+}  // namespace asg
+
+extern "C" asg_status asg_kron_batch_static_f64(const asg_kron_plan* p, const double* const* A, const double* X,
+                                                double* Y, void* stream) {
+  if (!p || !A || !X || !Y) return fail(ASG_ERR_INVALID, "kron_batch_static: NULL argument");
+  const unsigned long long need = static_cast<unsigned long long>(p->work_elems) * sizeof(double);
+  if (need > ASG_KRON_STATIC_SCRATCH_BYTES)
+    return fail(ASG_ERR_CAPACITY,
+                "kron_batch_static: the plan needs %llu bytes of scratch, the static scratch holds %llu; "
+                "use asg_kron_batch_f64 with a caller workspace",
+                need, static_cast<unsigned long long>(ASG_KRON_STATIC_SCRATCH_BYTES));
+  double* work = nullptr;
+  asg_status st = asg::static_scratch(&work);
+  if (st) return st;
+  asg::KBases<double> b{};
+  for (int i = 0; i < p->nfac; ++i) {
+    if (!A[i]) return fail(ASG_ERR_INVALID, "kron_batch_static: factor %d is NULL", i);
+    b.fac[i] = A[i];
+  }
+  b.x = X;
+  b.y = Y;
+  b.work = work;
+  b.nfac = p->nfac;
+  for (size_t i = 0; i < p->tmp_off.size(); ++i) b.tmp_off[i] = p->tmp_off[i];
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  asg::KChunk chunk;
+  for (int l = 0; l < p->nfac; ++l) {  // level by level, each level in chunks of descriptors
+    for (int q = p->level_start[l]; q < p->level_start[l + 1]; q += asg::kStaticChunk) {
+      const int cnt = std::min(asg::kStaticChunk, p->level_start[l + 1] - q);
+      std::memcpy(chunk.d, p->dev.data() + q, cnt * sizeof(asg::KDev));
+      chunk.count = cnt;
+      asg::k_kron_level_static<<<cnt, 128, 0, s>>>(chunk, b);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return asg::cuda_fail(e, "kron_batch_static launch");
+    }
+  }
+  return ASG_OK;
+}

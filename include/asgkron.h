@@ -264,6 +264,22 @@ asg_status asg_kron_batch_f64(const asg_kron_plan* plan, const double* const* A,
                               void* work, size_t work_bytes, void* stream);
 asg_status asg_kron_batch_f32(const asg_kron_plan* plan, const float* const* A, const float* X, float* Y,
                               void* work, size_t work_bytes, void* stream);
+/* Size of the fixed device array asg_kron_batch_static_f64 keeps its temporaries in. */
+#define ASG_KRON_STATIC_SCRATCH_BYTES (8ull << 20)
+/* asg_kron_batch_f64 without any allocation (no counterpart in the reference, whose
+ * kronmultN_batch.m grows its temporaries at run time).  For callers that cannot call
+ * cudaMalloc when they execute -- allocation forbidden or unsafe at that point, or no
+ * allocator to hand: the recursion's temporaries live in one fixed device array of
+ * ASG_KRON_STATIC_SCRATCH_BYTES (8 MiB) inside the library and the plan's GEMM descriptors
+ * ride in the launch parameters.  Plans whose workspace (asg_kron_plan_workspace) exceeds
+ * the array are rejected with ASG_ERR_CAPACITY.  The first call on each device, made with
+ * that device current, looks the array up; make it before any stream capture.  All calls on
+ * a device share the array, which keeps the last call's values (nothing in it needs to
+ * start at zero: every temporary is written before it is read); calls that overlap on the
+ * GPU race on it, so order them (one stream, or events).  A: host array of nkron device
+ * pointers; X, Y: device. */
+asg_status asg_kron_batch_static_f64(const asg_kron_plan* plan, const double* const* A, const double* X, double* Y,
+                                     void* stream);
 /* out = kron(A1, kron(A2, ...)) (krond.m:7-17), column-major prod(nrow) x prod(ncol).
  * A: host array of nkron device pointers (each nrow_i x ncol_i, ld = nrow_i). */
 asg_status asg_krond_f64(int nkron, const int* nrow, const int* ncol, const double* const* A, double* out,
