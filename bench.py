@@ -44,6 +44,8 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-rows", type=int, default=48, help="rows in the bounded CPU sample")
     ap.add_argument("--skip-variants", action="store_true")
+    ap.add_argument("--workload", default="continuity6", choices=["continuity6", "batched"],
+                    help="batched: the 256-problem persistent-launch configuration (own JSON line)")
     return ap.parse_args()
 
 
@@ -227,11 +229,236 @@ def time_device(plan, f, y, flush, steps, warmup, stream):
     return [s.elapsed_time(e) for s, e in ev]
 
 
+def forward_backward(plan, f, ystar, flush, steps, stream, dof, n1d):
+    """Differentiation step on continuity6 (FP32): y = A f, r = y - y*, fbar = A^T r and the
+    gradients of L = 1/2 ||A f - y*||^2 with respect to the applied 1-D operators.  Four
+    launches per step (apply, subtract, adjoint, operator gradient), timed as one region."""
+    import ctypes as C
+
+    import torch
+    from asgkron._lib import check, lib
+
+    T, D = plan.T, plan.D
+    active = plan.active_factors()
+    ptrs, lds, keep = (C.c_void_p * (T * D))(), (C.c_int * (T * D))(), []
+    n_active = 0
+    for t in range(T):
+        for d in range(D):
+            if active[t][d]:
+                n = plan.term_mats[t][d].shape[0]
+                g = torch.zeros(n * n, dtype=f.dtype, device=f.device)
+                keep.append(g)
+                ptrs[t * D + d], lds[t * D + d] = g.data_ptr(), n
+                n_active += 1
+    y, r, fbar = torch.empty_like(f), torch.empty_like(f), torch.empty_like(f)
+    sp = C.c_void_p(stream.cuda_stream)
+
+    def step():
+        plan.apply(f, y, stream)
+        torch.sub(y, ystar, out=r)
+        plan.apply_T(r, fbar, stream)
+        check(lib().asg_grad_ops_f32(plan.handle, C.c_void_p(f.data_ptr()), C.c_void_p(r.data_ptr()), ptrs, lds, sp))
+
+    for _ in range(3):
+        flush()
+        step()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for s, e in ev:
+        flush()
+        s.record(stream)
+        step()
+        e.record(stream)
+    torch.cuda.synchronize()
+    ms = sum(s.elapsed_time(e) for s, e in ev) / steps
+    st = plan.stats()
+    # compulsory bytes: forward and adjoint as the forward model; the subtraction reads y, y*
+    # and writes r; the gradient reads f and r and writes the applied operators' gradients
+    fwd = algorithmic_bytes(4, dof, T, D, n1d, plan.N, st["num_pairs"])
+    alg = 2 * fwd + 4 * 3 * dof + 4 * (2 * dof + n_active * n1d * n1d)
+    return {"value": dof / (ms * 1e-3) / 1e9, "ms": ms, "launches_per_step": 4,
+            "algorithmic_bytes": alg, "achieved_gbs": alg / (ms * 1e-3) / 1e9}
+
+
+def implicit_steps(dev, nsteps=10):
+    """Implicit configuration: diffusion2 LDG (Dirichlet zero), SG level 8, degree 4 (20,480
+    DOF), dt = h^2 (CFL 1), f0 = projection of sin(pi x) sin(pi y) + 1e-3 N(0,1) (seed 2); ten
+    backward-Euler steps by GMRES(30) + iterative refinement to 1e-10 relative residual, once
+    with the FP32 matvec inside (mixed) and once all FP64.  Host-driven solver: wall-clock."""
+    import numpy as np
+    import torch
+
+    import asgkron
+    from asgkron import pdes
+    from asgkron.steppers import be_step
+
+    pde = pdes.diffusion2(8)
+    idx = asgkron.hash_table_sparse_nD(pde.levels, 8).idx1d()
+    plan = asgkron.Plan.create(pde.term_mats(4), idx, 4)
+    f0 = pde.initial_condition(4, idx) + 1e-3 * np.random.default_rng(2).standard_normal(plan.dof)
+    dt = pde.dt(1.0)
+    out = {}
+    finals = {}
+    for mode, mixed in (("mixed", True), ("fp64", False)):
+        f = torch.from_numpy(f0).to(dev)
+        be_step(plan, f.clone(), dt, mixed=mixed)  # warm-up (workspace, first launches)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        outer = inner = 0
+        worst = 0.0
+        for _ in range(nsteps):
+            f, info = be_step(plan, f, dt, mixed=mixed)
+            outer += info["outer_iters"]
+            inner += info["inner_iters"]
+            worst = max(worst, info["rel_residual"])
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) / nsteps * 1e3
+        out[mode] = {"ms_per_step": ms, "outer_iters": outer, "inner_iters": inner, "max_rel_residual": worst}
+        finals[mode] = f
+    out["mixed_speedup"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
+    out["rel_diff_mixed_vs_fp64"] = float(torch.linalg.norm(finals["mixed"] - finals["fp64"]) /
+                                          torch.linalg.norm(finals["fp64"]))
+    out["dof"] = plan.dof
+    plan.close()
+    return out
+
+
+def precision_continuity3(dev, flush, stream):
+    """Precision configuration: continuity3 SG level 6, degree 3 (18,576 DOF), f ~ N(0,1)
+    seed 1: FP64 and FP32 applies, FP32 relative 2-norm error against FP64."""
+    import numpy as np
+    import torch
+
+    import asgkron
+    from asgkron import pdes
+
+    pde = pdes.continuity3(6)
+    idx = asgkron.hash_table_sparse_nD(pde.levels, 8).idx1d()
+    plan = asgkron.Plan.create(pde.term_mats(3), idx, 3)
+    f64 = torch.from_numpy(np.random.default_rng(1).standard_normal(plan.dof)).to(dev)
+    f32 = f64.float()
+    y64, y32 = torch.empty_like(f64), torch.empty_like(f32)
+    m64 = time_device(plan, f64, y64, flush, 100, 5, stream)
+    m32 = time_device(plan, f32, y32, flush, 100, 5, stream)
+    err = float(torch.linalg.norm(y32.double() - y64) / torch.linalg.norm(y64))
+    t64, t32 = sum(m64) / len(m64), sum(m32) / len(m32)
+    out = {"dof": plan.dof, "fp64": {"value": plan.dof / (t64 * 1e-3) / 1e9, "ms": t64},
+           "fp32": {"value": plan.dof / (t32 * 1e-3) / 1e9, "ms": t32}, "fp32_rel_err_vs_fp64": err,
+           "kernel": asgkron._lib.KERNEL_NAMES[plan.stats()["kernel_kind"]]}
+    plan.close()
+    return out
+
+
+def run_batched(args, rank, local):
+    """Batching configuration: 256 independent problems, each d ~ U{2,3,4}, SG level ~ U{3..7},
+    degree ~ U{2..4} (seed 3), d terms of dense N(0, 1/deg) 1-D operators (no structure, so
+    every (pair, term) of all N^2 pairs is executed: the reference work model), f ~ N(0,1).
+    One step = one persistent launch over all problems (FP32, tuned, replayed from a CUDA
+    graph).  Baseline: 256 sequential FP64 single-problem launches.  The inputs (62 MB of f,
+    6.3 GB of work lists) exceed L2, so no flush is needed."""
+    import numpy as np
+    import torch
+
+    import asgkron
+    from asgkron.batch import Batch
+
+    if rank != 0:
+        return
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    rng = np.random.default_rng(3)
+    plans, f64s = [], []
+    flops = 0.0
+    for _ in range(256):
+        d = int(rng.choice([2, 3, 4]))
+        lev = int(rng.integers(3, 8))
+        deg = int(rng.integers(2, 5))
+        idx = asgkron.hash_table_sparse_nD([lev] * d, 8).idx1d()
+        n = deg * 2 ** lev
+        mats = [[rng.normal(0.0, 1.0 / np.sqrt(deg), (n, n)) for _ in range(d)] for _ in range(d)]
+        p = asgkron.Plan.create(mats, idx, deg, structure="none")
+        p.term_mats = None  # the plan holds its own packed copy; drop the host operators
+        flops += p.stats()["flops_executed"]
+        plans.append(p)
+        f64s.append(torch.from_numpy(rng.standard_normal(p.dof)).to(dev))
+    dof = sum(p.dof for p in plans)
+    f32s = [f.float() for f in f64s]
+    y32s = [torch.empty_like(f) for f in f32s]
+    y64s = [torch.empty_like(f) for f in f64s]
+    b = Batch(plans)
+    b.set_io(f32s, y32s)
+    b.tune()
+    g = b.capture()
+    stream = torch.cuda.current_stream(dev)
+    steps = max(1, min(args.steps, 20))
+    for _ in range(max(3, args.warmup)):
+        g.replay()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for s, e in ev:
+        s.record(stream)
+        g.replay()
+        e.record(stream)
+    torch.cuda.synchronize()
+    ms = sum(s.elapsed_time(e) for s, e in ev) / steps
+    # baseline: the same problems one FP64 launch after another
+    for p, f, y in zip(plans, f64s, y64s):
+        p.apply(f, y, stream)
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record(stream)
+    for p, f, y in zip(plans, f64s, y64s):
+        p.apply(f, y, stream)
+    e.record(stream)
+    torch.cuda.synchronize()
+    ms64 = s.elapsed_time(e)
+    errs = [float(torch.linalg.norm(a.double() - c) / torch.linalg.norm(c)) for a, c in zip(y32s, y64s)]
+    # end to end: pinned host f in, one batched launch, y back
+    fh = [f.cpu().pin_memory() for f in f32s]
+    yh = [torch.empty_like(t).pin_memory() for t in fh]
+    e2e_steps = max(1, min(steps, 5))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for h, d_ in zip(fh, f32s):
+            d_.copy_(h, non_blocking=True)
+        g.replay()
+        for h, d_ in zip(yh, y32s):
+            h.copy_(d_, non_blocking=True)
+        torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) / e2e_steps * 1e3
+    info = b.info()
+    line = {
+        "metric": METRIC, "value": dof / (ms * 1e-3) / 1e9, "unit": UNIT, "n_gpus": 1, "steps": steps,
+        "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (dense N(0,1/deg) operators, f ~ N(0,1), seed 3)",
+        "config": {"workload": "batched: 256 problems, d in {2,3,4}, SG lev 3..7, deg 2..4, all pairs",
+                   "dof": dof, "flops_per_step": flops, "l2": "inputs larger than L2 (6.3 GB work lists)",
+                   "launch": "one persistent launch replayed from a CUDA graph", "tuned": info},
+        "compute": {"gflops_per_s": flops / (ms * 1e-3) / 1e9},
+        "variants": {"fp64_sequential_256_launches": {"ms": ms64, "value": dof / (ms64 * 1e-3) / 1e9,
+                                                       "gflops_per_s": flops / (ms64 * 1e-3) / 1e9},
+                     "speedup_vs_fp64_sequential": ms64 / ms,
+                     "fp32_rel_err_vs_fp64": {"max": max(errs), "median": statistics.median(errs)}},
+        "e2e": {"value": dof / (e2e_ms * 1e-3) / 1e9, "unit": UNIT, "h2d_bytes_per_step": 4 * dof,
+                "d2h_bytes_per_step": 4 * dof, "ms_per_step": e2e_ms},
+        "gpu_launches": steps * 2,  # counter reset (memset node) + the persistent kernel per replay
+    }
+    print(json.dumps(line), flush=True)
+    b.close()
+    for p in plans:
+        p.close()
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_env()
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.workload == "batched":
+        run_batched(args, rank, local)
         return
     import numpy as np
     import torch
@@ -328,6 +555,11 @@ def main():
             "value": dof / (dms * 1e-3) / 1e9, "ms": dms, "entries": dst["num_entries"],
             "gflops_per_s": dst["flops_reference"] / (dms * 1e-3) / 1e9}
         dense.close()
+        ystar = torch.from_numpy(np.random.default_rng(5).standard_normal(dof).astype(np.float32)).to(dev)
+        variants["fp32_forward_backward"] = forward_backward(plan, f32, ystar, flush, max(5, min(args.steps, 200)),
+                                                             stream, dof, n1d)
+        variants["implicit_diffusion2_lev8_deg4"] = implicit_steps(dev)
+        variants["precision_continuity3_lev6_deg3"] = precision_continuity3(dev, flush, stream)
 
     # ---- roofline ------------------------------------------------------------------------
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -338,10 +570,13 @@ def main():
         peak, peak_src = FALLBACK_HBM_GBS, "of fallback"
     alg = algorithmic_bytes(4, dof, T, D, n1d, N, st["num_pairs"])
     achieved = alg / (apply_ms * 1e-3) / 1e9
+    if "fp32_forward_backward" in variants:
+        fb = variants["fp32_forward_backward"]
+        fb["frac_hbm"] = fb["achieved_gbs"] / peak
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
-        traffic = json.load(open(tpath)).get("k_single_mode_fp32_continuity6")
+        traffic = json.load(open(tpath)).get("k_single_tma_fp32_continuity6")
 
     cpu = None
     if rank == 0 and world == 1:

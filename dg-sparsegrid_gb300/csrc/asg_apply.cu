@@ -796,6 +796,233 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
   }
 }
 
+// Persistent variant of k_single_tma: one CTA per resident slot walks a static list of rows
+// (longest-processing-time assignment made at plan creation, cta_ptr/cta_rows).  The
+// producer streams entries across row boundaries, so only a CTA's first copy pays the
+// cold-start latency, and the lists balance work instead of leaving a short last wave.
+// Per row the consumers run exactly the k_single_tma algorithm (same group order, same
+// Kahan merges, one write of the row's y block), so results are bitwise those of kind 3.
+template <typename T, int S, int MINB>
+__global__ void __launch_bounds__(288, MINB) k_single_tma_rows(ApplyArgs<T> a) {
+  constexpr int P = 4;
+  constexpr bool F32 = sizeof(T) == 4;
+  constexpr int AB = F32 ? 32 : 16;  // operator block values per stage
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_abort;
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int B = a.B, D = a.D;
+  const int SST = B + AB;
+  T* stages = reinterpret_cast<T*>(smem_raw);
+  uint64_t* full = reinterpret_cast<uint64_t*>(stages + S * SST);
+  uint64_t* empty = full + S;
+  const int ri0 = a.cta_ptr[blockIdx.x], ri1 = a.cta_ptr[blockIdx.x + 1];
+  const uint32_t fbytes = static_cast<uint32_t>(B * sizeof(T)), abytes = AB * sizeof(T);
+  const T* opsrc = F32 ? reinterpret_cast<const T*>(a.ops_pair) : a.ops;
+
+  if (tid == 0) {
+    s_abort = 0;
+    for (int k = 0; k < S; ++k) {
+      mbar_init(&full[k], 1);
+      mbar_init(&empty[k], 8);
+    }
+    mbar_fence_init();
+  }
+  __syncthreads();
+  volatile int* abort_flag = &s_abort;
+
+  if (warp == 8) {
+    // ---------------- producer warp: one stage counter g across all rows ----------------
+    int g = 0;
+    bool stop = false;
+    for (int ri = ri0; ri < ri1 && !stop; ++ri) {
+      const int row = a.cta_rows[ri];
+      const long long q0 = a.row_ptr[row];
+      const int n = static_cast<int>(a.row_ptr[row + 1] - q0);
+      const EntryDesc* ed = a.ed + q0;
+      for (int k0 = 0; k0 < n && !stop; k0 += 32) {
+        EntryDesc mine{};
+        if (k0 + lane < n) mine = ed[k0 + lane];
+        const int cnt = min(32, n - k0);
+        for (int l = 0; l < cnt; ++l) {
+          const int j = __shfl_sync(0xffffffffu, mine.j, l);
+          const long long aoff = __shfl_sync(0xffffffffu, mine.aoff, l);
+          const int st = g % S;
+          bool ok = true;
+          if (g >= S) ok = mbar_wait_bounded(&empty[st], static_cast<uint32_t>(((g / S) - 1) & 1));
+          if (!__all_sync(0xffffffffu, ok)) {
+            if (lane == 0) *abort_flag = 1;
+            stop = true;
+            break;
+          }
+          if (lane == 0) {
+            T* dst = stages + st * SST;
+            fence_proxy_async();
+            mbar_expect_tx(&full[st], fbytes + abytes);
+            bulk_g2s(dst, a.f + static_cast<size_t>(j) * B, fbytes, &full[st]);
+            bulk_g2s(dst + B, opsrc + aoff * (AB / 16), abytes, &full[st]);
+          }
+          ++g;
+          __syncwarp();
+        }
+      }
+    }
+    if (lane == 0) {
+      if (*abort_flag) atomicExch(a.err, static_cast<int>(ASG_ERR_TIMEOUT));
+      // every issued copy lands before the CTA's shared memory is released (bounded)
+      for (int k = max(0, g - S); k < g; ++k) {
+        const long long t0 = clock64();
+        while (!mbar_test(&full[k % S], static_cast<uint32_t>((k / S) & 1)) && clock64() - t0 < (1LL << 28)) {
+        }
+      }
+    }
+    return;
+  }
+
+  // ---------------- consumer warps ----------------
+  int nat_base, nat_s;
+  tile_place(tid, D - 3, D, a.stride, nat_base, nat_s);
+  int g = 0;
+  bool gave_up = false;
+  for (int ri = ri0; ri < ri1; ++ri) {
+    const int row = a.cta_rows[ri];
+    const long long q0 = a.row_ptr[row];
+    const int n = static_cast<int>(a.row_ptr[row + 1] - q0);
+    const EntryDesc* ed = a.ed + q0;
+    int cur_m = -1, base_g = 0, s_g = 0, pend = -1, mlane = -1;
+    bool direct = false;
+    F32Tile g32, n32, c32;
+    T gg[P][P], nat[P][P];
+#pragma unroll
+    for (int r = 0; r < P; ++r) {
+#pragma unroll
+      for (int cp = 0; cp < 2; ++cp) g32.v[r][cp] = n32.v[r][cp] = c32.v[r][cp] = make_float2(0.f, 0.f);
+#pragma unroll
+      for (int c = 0; c < P; ++c) gg[r][c] = nat[r][c] = T(0);
+    }
+    for (int k = 0; k <= n; ++k) {
+      int m = -1;
+      const int st = g % S;
+      if (k < n) {
+        if ((k & 31) == 0) mlane = (k + lane < n) ? ed[k + lane].m : -1;
+        m = __shfl_sync(0xffffffffu, mlane, k & 31);
+        if (!gave_up) {
+          const bool ok = mbar_wait_bounded(&full[st], static_cast<uint32_t>((g / S) & 1));
+          if (!__all_sync(0xffffffffu, ok)) {
+            gave_up = true;
+            *abort_flag = 1;
+          }
+        }
+      }
+      if (m != cur_m) {
+        if (direct) {
+          if constexpr (F32) {
+#pragma unroll
+            for (int r = 0; r < P; ++r) {
+              kahan2(n32.v[r][0], c32.v[r][0], g32.v[r][0]);
+              kahan2(n32.v[r][1], c32.v[r][1], g32.v[r][1]);
+            }
+          } else {
+#pragma unroll
+            for (int r = 0; r < P; ++r)
+#pragma unroll
+              for (int c = 0; c < P; ++c) nat[r][c] += gg[r][c];
+          }
+        } else if (cur_m >= 0) {
+          // transpose the group's sums onto the natural tiles through the stage just consumed
+          consumer_sync();
+          T* scr = stages + pend * SST;
+#pragma unroll
+          for (int r = 0; r < P; ++r) {
+            if constexpr (F32) {
+              *reinterpret_cast<float4*>(scr + base_g + r * s_g) =
+                  make_float4(g32.v[r][0].x, g32.v[r][0].y, g32.v[r][1].x, g32.v[r][1].y);
+            } else {
+              Row<T, P> rr;
+#pragma unroll
+              for (int c = 0; c < P; ++c) rr.v[c] = gg[r][c];
+              rr.store(scr + base_g + r * s_g);
+            }
+          }
+          consumer_sync();
+#pragma unroll
+          for (int r = 0; r < P; ++r) {
+            if constexpr (F32) {
+              const float4 v = *reinterpret_cast<const float4*>(scr + nat_base + r * nat_s);
+              kahan2(n32.v[r][0], c32.v[r][0], make_float2(v.x, v.y));
+              kahan2(n32.v[r][1], c32.v[r][1], make_float2(v.z, v.w));
+            } else {
+              Row<T, P> rr;
+              rr.load(scr + nat_base + r * nat_s);
+#pragma unroll
+              for (int c = 0; c < P; ++c) nat[r][c] += rr.v[c];
+            }
+          }
+        }
+        cur_m = m;
+        if (m >= 0) {
+#pragma unroll
+          for (int r = 0; r < P; ++r) {
+#pragma unroll
+            for (int cp = 0; cp < 2; ++cp) g32.v[r][cp] = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int c = 0; c < P; ++c) gg[r][c] = T(0);
+          }
+          direct = (m == D - 1) || (m == D - 3);
+          if (m == D - 1) {
+            base_g = nat_base;
+            s_g = nat_s;
+          } else {
+            tile_place(tid, m, D, a.stride, base_g, s_g);
+          }
+        }
+      }
+      if (pend >= 0) {
+        __syncwarp();
+        if (lane == 0 && !gave_up) mbar_arrive(&empty[pend]);
+        pend = -1;
+      }
+      if (m < 0) break;
+      const T* sp = stages + st * SST;
+      if constexpr (F32) {
+        if (m == D - 1)
+          f32_cols(g32, reinterpret_cast<const float*>(sp + B), reinterpret_cast<const float*>(sp + base_g), s_g);
+        else
+          f32_rows(g32, reinterpret_cast<const float*>(sp + B), reinterpret_cast<const float*>(sp + base_g), s_g);
+      } else {
+        T A[P * P];
+#pragma unroll
+        for (int r = 0; r < P; ++r) {
+          Row<T, P> rr;
+          rr.load(sp + B + r * P);
+#pragma unroll
+          for (int c = 0; c < P; ++c) A[r * P + c] = rr.v[c];
+        }
+        if (m == D - 1)
+          tile_cols_s<T>(gg, A, sp + base_g, s_g);
+        else
+          tile_rows<T>(gg, A, sp + base_g, s_g);
+      }
+      pend = st;
+      ++g;
+    }
+    if (*abort_flag) continue;  // y is undefined; the plan's status word reports the timeout
+    T* yr = a.y + static_cast<size_t>(row) * B + nat_base;
+#pragma unroll
+    for (int r = 0; r < P; ++r) {
+      if constexpr (F32) {
+        *reinterpret_cast<float4*>(reinterpret_cast<float*>(yr) + r * nat_s) =
+            make_float4(n32.v[r][0].x, n32.v[r][0].y, n32.v[r][1].x, n32.v[r][1].y);
+      } else {
+        Row<T, P> rr;
+#pragma unroll
+        for (int c = 0; c < P; ++c) rr.v[c] = nat[r][c];
+        rr.store(yr + r * nat_s);
+      }
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------------------
 // Gradient with respect to the 1-D operators.  For a work entry (i, j, t) and an applied
 // factor k of term t, d L / d A_{t,k}[I_k(i), J_k(j)] (a P x P block) is the contraction of
@@ -915,6 +1142,13 @@ cudaError_t ensure_smem(K kernel, size_t bytes, size_t max_bytes, bool& done) {
   return e;
 }
 
+// Dynamic shared memory of k_single_tma_rows: S stages of (f block + operator block) and the
+// full/empty barriers.
+template <typename T>
+size_t rows_smem(int S, int B) {
+  return static_cast<size_t>(S) * (B + (sizeof(T) == 4 ? 32 : 16)) * sizeof(T) + 2 * S * sizeof(uint64_t);
+}
+
 template <typename T, int P>
 cudaError_t launch_p(const ApplyArgs<T>& a, int kind, cudaStream_t s) {
   constexpr bool K = sizeof(T) == 4;
@@ -972,6 +1206,20 @@ cudaError_t launch_p(const ApplyArgs<T>& a, int kind, cudaStream_t s) {
       return cudaGetLastError();
     }
   }
+  if constexpr (P == 4) {
+    if (kind == KK_SINGLE_TMA_ROWS) {
+      if (a.B != 256 * P * P || !a.cta_ptr || !a.cta_rows || a.nctas <= 0) return cudaErrorInvalidValue;
+      if (sizeof(T) == 4 && !a.ops_pair) return cudaErrorInvalidValue;
+      constexpr int S0 = sizeof(T) == 4 ? 4 : 3;
+      const size_t sm = rows_smem<T>(S0, a.B);
+      auto kern = k_single_tma_rows<T, S0, sizeof(T) == 4 ? 2 : 1>;
+      static bool done = false;
+      cudaError_t e = ensure_smem(kern, sm, sm, done);
+      if (e != cudaSuccess) return e;
+      kern<<<a.nctas, 288, sm, s>>>(a);
+      return cudaGetLastError();
+    }
+  }
   if constexpr (P == 3 || P == 4) {
     if (kind == KK_SINGLE_MODE) {
       const int nt = a.B / (P * P);
@@ -988,6 +1236,23 @@ cudaError_t launch_p(const ApplyArgs<T>& a, int kind, cudaStream_t s) {
 }
 
 }  // namespace
+
+int single_tma_rows_occupancy(int es) {
+  int nb = 0;
+  cudaError_t e;
+  if (es == 4) {
+    auto kern = k_single_tma_rows<float, 4, 2>;
+    const size_t sm = rows_smem<float>(4, 4096);
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 288, sm);
+  } else {
+    auto kern = k_single_tma_rows<double, 3, 1>;
+    const size_t sm = rows_smem<double>(3, 4096);
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(sm));
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, 288, sm);
+  }
+  return e == cudaSuccess ? nb : 0;
+}
 
 template <typename T>
 cudaError_t launch_apply(const ApplyArgs<T>& a, int P, int kind, cudaStream_t s) {

@@ -53,6 +53,9 @@ struct ApplyArgs {
   const float* ops_pair;     // FP32 blocks in paired-FMA order (32 values per block), single-mode plans
   const int* row_order;      // [N] launch order of rows (longest work first) or NULL
   int* err;                  // device status word (ASG_ERR_TIMEOUT after a bounded wait gave up)
+  const int* cta_ptr;        // [nctas+1] persistent single-mode kernel: rows of CTA c are
+  const int* cta_rows;       //   cta_rows[cta_ptr[c] .. cta_ptr[c+1]) (static LPT assignment)
+  int nctas;
 };
 
 template <typename T>
@@ -88,7 +91,12 @@ struct GradArgs {
 template <typename T>
 cudaError_t launch_grad(const GradArgs<T>& a, int P, cudaStream_t s);
 
-enum KernelKind { KK_CHAIN_WARP = 0, KK_CHAIN_CTA = 1, KK_SINGLE_MODE = 2, KK_SINGLE_TMA = 3, KK_SINGLE_TMA3 = 4 };
+enum KernelKind { KK_CHAIN_WARP = 0, KK_CHAIN_CTA = 1, KK_SINGLE_MODE = 2, KK_SINGLE_TMA = 3, KK_SINGLE_TMA3 = 4,
+                  KK_SINGLE_TMA_ROWS = 5 };
+
+// Resident CTAs per SM of the persistent single-mode kernel for element size es (4 or 8);
+// sets the kernel's dynamic shared-memory limit first.  0 on error.
+int single_tma_rows_occupancy(int es);
 
 }  // namespace asg
 
@@ -138,6 +146,10 @@ struct asg_plan {
   asg::EntryDesc* d_ed = nullptr;
   std::vector<int> row_order;
   int* d_row_order = nullptr;
+  // persistent single-mode kernel: per precision (0 FP64, 1 FP32) the rows of each CTA
+  std::vector<int> cta_ptr[2], cta_rows[2];
+  int* d_cta_ptr[2] = {nullptr, nullptr};
+  int* d_cta_rows[2] = {nullptr, nullptr};
   float* d_ops_pair = nullptr;
   int* d_err = nullptr;
   double* d_ops64 = nullptr;

@@ -66,6 +66,10 @@ void free_device(asg_plan* p) {
   cudaFree(p->d_ops32);
   cudaFree(p->d_ed);
   cudaFree(p->d_row_order);
+  for (int k = 0; k < 2; ++k) {
+    cudaFree(p->d_cta_ptr[k]);
+    cudaFree(p->d_cta_rows[k]);
+  }
   cudaFree(p->d_ops_pair);
   cudaFree(p->d_err);
   cudaFree(p->d_io);
@@ -178,7 +182,49 @@ asg_status finalize(asg_plan* p) {
                                          p->idx1d[j * D + m]) * P * P;
       }
   }
+  // persistent single-mode kernel: per precision, a longest-processing-time assignment of
+  // rows (cost = entries + 1) to the resident CTAs, each CTA's rows longest first
+  for (int k = 0; k < 2; ++k) {
+    p->cta_ptr[k].clear();
+    p->cta_rows[k].clear();
+  }
+  if (single && P == 4 && B == 4096 && N > 0) {
+    int dev = 0, nsm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return cuda_fail(e, "device attributes");
+    for (int k = 0; k < 2; ++k) {
+      const int occ = single_tma_rows_occupancy(k == 0 ? 8 : 4);
+      if (occ <= 0) return fail(ASG_ERR_CUDA, "persistent single-mode kernel cannot be resident");
+      const int G = std::max(1, std::min(N, occ * nsm));
+      std::vector<std::vector<int>> lists(G);
+      std::vector<std::pair<long long, int>> heap;  // (load, cta) min-heap
+      for (int c = 0; c < G; ++c) heap.push_back({0, c});
+      auto cmp = [](const std::pair<long long, int>& x, const std::pair<long long, int>& y) { return x > y; };
+      std::vector<int> by_cost(N);
+      for (int i = 0; i < N; ++i) by_cost[i] = i;
+      std::stable_sort(by_cost.begin(), by_cost.end(), [&](int x, int y) {
+        return p->row_ptr[x + 1] - p->row_ptr[x] > p->row_ptr[y + 1] - p->row_ptr[y];
+      });
+      for (int i : by_cost) {
+        std::pop_heap(heap.begin(), heap.end(), cmp);
+        auto& top = heap.back();
+        lists[top.second].push_back(i);
+        top.first += p->row_ptr[i + 1] - p->row_ptr[i] + 1;
+        std::push_heap(heap.begin(), heap.end(), cmp);
+      }
+      p->cta_ptr[k].push_back(0);
+      for (int c = 0; c < G; ++c) {
+        p->cta_rows[k].insert(p->cta_rows[k].end(), lists[c].begin(), lists[c].end());
+        p->cta_ptr[k].push_back(static_cast<int>(p->cta_rows[k].size()));
+      }
+    }
+  }
   asg_status st;
+  for (int k = 0; k < 2; ++k) {
+    if ((st = upload(&p->d_cta_ptr[k], p->cta_ptr[k]))) return st;
+    if ((st = upload(&p->d_cta_rows[k], p->cta_rows[k]))) return st;
+  }
   if ((st = upload(&p->d_row_order, p->row_order))) return st;
   if ((st = upload_ops(p))) return st;
   if ((st = upload(&p->d_idx1d, p->idx1d))) return st;
@@ -384,6 +430,10 @@ ApplyArgs<T> make_args(const asg_plan* p, const T* f, T* y, const T* ops) {
   a.err = p->d_err;
   a.ops_pair = p->d_ops_pair;
   a.row_order = p->d_row_order;
+  const int pk = sizeof(T) == 4 ? 1 : 0;
+  a.cta_ptr = p->d_cta_ptr[pk];
+  a.cta_rows = p->d_cta_rows[pk];
+  a.nctas = p->cta_ptr[pk].empty() ? 0 : static_cast<int>(p->cta_ptr[pk].size()) - 1;
   int s = 1;
   for (int m = p->D - 1; m >= 0; --m) {
     a.stride[m] = s;
@@ -688,14 +738,15 @@ asg_status asg_plan_update_ops(asg_plan* p, const double* const* ops, const int*
 asg_status asg_plan_set_kernel(asg_plan* p, int kind) {
   if (!p) return fail(ASG_ERR_INVALID, "plan_set_kernel: NULL plan");
   if (kind == asg::KK_CHAIN_WARP && p->B > 256) return fail(ASG_ERR_UNSUPPORTED, "warp chain kernel needs deg^d <= 256");
-  if (kind == asg::KK_SINGLE_MODE || kind == asg::KK_SINGLE_TMA || kind == asg::KK_SINGLE_TMA3) {
+  if (kind == asg::KK_SINGLE_MODE || kind == asg::KK_SINGLE_TMA || kind == asg::KK_SINGLE_TMA3 ||
+      kind == asg::KK_SINGLE_TMA_ROWS) {
     bool ok = kind != asg::KK_SINGLE_MODE ? (p->P == 4 && p->B == 4096)
                                          : ((p->P == 3 || p->P == 4) && p->B >= 32 * p->P * p->P);
     for (unsigned a : p->active) ok = ok && __builtin_popcount(a) == 1;
     if (!ok || p->ed.size() != p->ent.size())
       return fail(ASG_ERR_UNSUPPORTED, "single-mode kernels need one non-identity factor per term (deg 3/4)");
   }
-  if (kind < 0 || kind > 4) return fail(ASG_ERR_INVALID, "unknown kernel kind %d", kind);
+  if (kind < 0 || kind > 5) return fail(ASG_ERR_INVALID, "unknown kernel kind %d", kind);
   p->kernel_kind = kind;
   return ASG_OK;
 }

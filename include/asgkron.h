@@ -73,7 +73,7 @@ typedef struct {
   double flops_reference;      /* num_pairs * T * d * 2 * deg^(d+1): the reference's work */
   double flops_executed;       /* flops of the executed work model */
   long long op_bytes_f64;      /* packed operator bytes on the device (FP64 copy) */
-  int kernel_kind;             /* 0 warp chain, 1 CTA chain, 2/3 single-mode fiber kernels */
+  int kernel_kind;             /* 0 warp chain, 1 CTA chain, 2-5 single-mode fiber kernels */
   int active_modes_max;        /* max over terms of non-identity factors */
 } asg_plan_stats;
 
@@ -100,9 +100,10 @@ asg_status asg_plan_update_ops(asg_plan* plan, const double* const* ops, const i
 /* Force a kernel family for this plan: 0 warp chain (deg^d <= 256), 1 CTA chain,
  * 2 single-mode fiber kernel with direct loads, 3 single-mode fiber kernel with TMA bulk
  * copies (4 stages, 2 CTAs per SM), 4 the same with 3 stages, the FP32 compensation tile in
- * shared memory and 3 CTAs per SM (2-4 need one non-identity factor per term; 3-4 need deg 4,
- * d 6).  The default is chosen by asg_plan_create; this exists
- * for testing one family against another and for launch-shape tuning. */
+ * shared memory and 3 CTAs per SM, 5 the kind-3 pipeline in persistent CTAs that each walk
+ * a balanced list of rows (2-5 need one non-identity factor per term; 3-5 need deg 4, d 6).
+ * The default is chosen by asg_plan_create; this exists for testing one family against
+ * another and for launch-shape tuning. */
 asg_status asg_plan_set_kernel(asg_plan* plan, int kind);
 /* Synchronises and reads the plan's device status word: ASG_OK, or ASG_ERR_TIMEOUT when a
  * kernel's bounded shared-memory pipeline wait gave up (the y it wrote is then undefined).

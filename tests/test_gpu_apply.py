@@ -115,6 +115,11 @@ def test_continuity6_lev4_deg4_kernels_agree(dev):
     y32 = _apply(p, f, dev, torch.float32)
     assert p.device_status() == 0
     assert rel2(y32, y_single) <= FP32_TOL
+    # the persistent row-list kernel runs kind 3's arithmetic per row: bitwise equal
+    p.set_kernel(5)
+    assert np.array_equal(_apply(p, f, dev), y_single)
+    assert np.array_equal(_apply(p, f, dev, torch.float32), y32)
+    assert p.device_status() == 0
     for kind in (asgkron._lib.KERNEL_SINGLE_TMA3, asgkron._lib.KERNEL_SINGLE_MODE):
         p.set_kernel(kind)
         assert rel2(_apply(p, f, dev), y_single) <= FP64_TOL
@@ -128,6 +133,25 @@ def test_continuity6_lev4_deg4_kernels_agree(dev):
     assert pn.stats()["num_entries"] == 501 * 501 * 6
     y_none = _apply(pn, f, dev)
     assert rel2(y_none, y_single) <= FP64_TOL
+
+
+@pytest.mark.parametrize("lev", [2, 3])
+def test_continuity6_small_levels_row_lists(dev, lev):
+    """continuity6 deg 4 at levels with fewer elements than resident CTAs (one row per CTA)
+    and with several rows per CTA: kinds 3 and 5 agree bitwise, FP64 matches the oracle."""
+    pde, table, idx, mats = problem("continuity6", lev, 4)
+    N = idx.shape[0]
+    f = np.random.default_rng(lev).standard_normal(N * 4096)
+    p = _plan(mats, idx, 4, structure="detect")
+    y3 = _apply(p, f, dev)
+    y3s = _apply(p, f, dev, torch.float32)
+    p.set_kernel(5)
+    assert np.array_equal(_apply(p, f, dev), y3)
+    assert np.array_equal(_apply(p, f, dev, torch.float32), y3s)
+    assert p.device_status() == 0
+    rows = np.arange(0, N, max(1, N // 5))
+    want = O.apply_A_rows(mats, idx.astype(np.int64), 4, f, rows=rows)
+    assert rel2(y3.reshape(-1, 4096)[rows].ravel(), want) <= FP64_TOL
 
 
 @pytest.mark.parametrize("d,lev,deg", [(2, 3, 2), (2, 4, 4), (3, 3, 3), (3, 4, 2), (4, 3, 2), (4, 3, 3), (1, 5, 4),
