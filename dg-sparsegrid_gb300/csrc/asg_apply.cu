@@ -1115,6 +1115,116 @@ __global__ void __launch_bounds__(256) k_grad(GradArgs<T> a) {
   }
 }
 
+// Chunked gradient for plans whose terms have one applied factor (deg 4): no mode chain to
+// recompute, so a contributor is a pure contraction of two 4096-value blocks.  One CTA per
+// item of up to 8 contributors of one target, one warp per contributor reading both blocks
+// with 16-byte loads (fibers along k grouped 4 at a time along the fastest dimension).  The
+// item's 4 x 4 sum (warps added in a fixed order) goes to a partial slot; the CTA that
+// finishes a target's last item (atomic counter) adds the target's partials in item order and
+// writes G, so the result does not depend on which CTA arrives last.
+template <typename T>
+__device__ __forceinline__ void load4(const T* p, T (&v)[4]) {
+  if constexpr (sizeof(T) == 4) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+  } else {
+    const double2 q0 = *reinterpret_cast<const double2*>(p);
+    const double2 q1 = *reinterpret_cast<const double2*>(p + 2);
+    v[0] = q0.x; v[1] = q0.y; v[2] = q1.x; v[3] = q1.y;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_grad_items(GradArgs<T> a) {
+  constexpr int P = 4;
+  __shared__ T red[8][P * P];
+  __shared__ int s_last;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int B = a.B;
+  for (int it = blockIdx.x; it < a.nitems; it += gridDim.x) {
+    const GradItem item = a.items[it];
+    const GradTarget tg = a.tgt[item.tgt];
+    T* Gout = a.G[tg.tm];
+    if (Gout == nullptr) continue;  // uniform across the CTA
+    T acc[P][P];
+#pragma unroll
+    for (int x = 0; x < P; ++x)
+#pragma unroll
+      for (int y = 0; y < P; ++y) acc[x][y] = T(0);
+    const int c = item.c0 + warp;
+    if (c < item.c1) {
+      const GradContrib e = a.contrib[c];
+      const T* ri = a.r + static_cast<size_t>(e.i) * B;
+      const T* zj = a.f + static_cast<size_t>(e.j) * B;
+      const int s = a.stride[e.k];
+      if (s == 1) {
+        // fibers are 4 contiguous values: G[x][y] += r[x] z[y]
+        for (int fb = lane; fb < B / P; fb += 32) {
+          T rv[4], zv[4];
+          load4(ri + fb * P, rv);
+          load4(zj + fb * P, zv);
+#pragma unroll
+          for (int x = 0; x < P; ++x)
+#pragma unroll
+            for (int y = 0; y < P; ++y) acc[x][y] = fma(rv[x], zv[y], acc[x][y]);
+        }
+      } else {
+        // 4 fibers with consecutive fastest-dimension offsets per lane: one 16-byte load per
+        // (fiber position x) holds the 4 fibers' values
+        for (int grp = lane; grp < B / (P * 4); grp += 32) {
+          const int o = grp * 4;            // first of the 4 fibers (o = hi * s + lo)
+          const int hi = o / s, lo = o - hi * s;
+          const int base = hi * s * P + lo;
+          T rv[P][4], zv[P][4];
+#pragma unroll
+          for (int x = 0; x < P; ++x) {
+            load4(ri + base + x * s, rv[x]);
+            load4(zj + base + x * s, zv[x]);
+          }
+#pragma unroll
+          for (int x = 0; x < P; ++x)
+#pragma unroll
+            for (int y = 0; y < P; ++y)
+#pragma unroll
+              for (int q = 0; q < 4; ++q) acc[x][y] = fma(rv[x][q], zv[y][q], acc[x][y]);
+        }
+      }
+    }
+#pragma unroll
+    for (int x = 0; x < P; ++x)
+#pragma unroll
+      for (int y = 0; y < P; ++y) {
+        T v = acc[x][y];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if (lane == 0) red[warp][x * P + y] = v;
+      }
+    __syncthreads();
+    if (tid < P * P) {
+      T sum = T(0);
+#pragma unroll
+      for (int w = 0; w < 8; ++w) sum += red[w][tid];
+      a.partial[static_cast<size_t>(it) * P * P + tid] = sum;
+      __threadfence();
+    }
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(&a.counter[item.tgt], 1) == item.count - 1;
+    __syncthreads();
+    if (s_last) {
+      __threadfence();
+      if (tid < P * P) {
+        T sum = T(0);
+        for (int q = item.first; q < item.first + item.count; ++q)
+          sum += __ldcg(a.partial + static_cast<size_t>(q) * P * P + tid);
+        const int x = tid / P, y = tid % P;
+        Gout[static_cast<long long>(tg.beta * P + y) * a.ldg[tg.tm] + tg.alpha * P + x] = sum;
+      }
+      if (tid == 0) a.counter[item.tgt] = 0;  // ready for the next launch (stream order)
+    }
+    __syncthreads();
+  }
+}
+
 template <typename T, int P>
 cudaError_t launch_grad_p(const GradArgs<T>& a, cudaStream_t s) {
   const int Bpad = (a.B + 3) & ~3;
@@ -1129,6 +1239,13 @@ cudaError_t launch_grad_p(const GradArgs<T>& a, cudaStream_t s) {
   }
   const int grid = a.ntgt < 152 * 8 ? a.ntgt : 152 * 8;
   kern<<<grid, 256, sm, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_grad_items(const GradArgs<T>& a, cudaStream_t s) {
+  const int grid = a.nitems < 152 * 8 ? a.nitems : 152 * 8;
+  k_grad_items<T><<<grid, 256, 0, s>>>(a);
   return cudaGetLastError();
 }
 
@@ -1273,6 +1390,7 @@ cudaError_t launch_apply(const ApplyArgs<T>& a, int P, int kind, cudaStream_t s)
 template <typename T>
 cudaError_t launch_grad(const GradArgs<T>& a, int P, cudaStream_t s) {
   if (a.ntgt == 0) return cudaSuccess;
+  if (a.items) return P == 4 ? launch_grad_items<T>(a, s) : cudaErrorInvalidValue;
   switch (P) {
     case 1: return launch_grad_p<T, 1>(a, s);
     case 2: return launch_grad_p<T, 2>(a, s);

@@ -71,6 +71,11 @@ struct GradTarget {
   int alpha;  // block row (1-D index of the row element in dimension k)
   int beta;   // block column
 };
+// Work item of the chunked gradient kernel (terms with one applied factor, deg 4): up to 8
+// contributors [c0, c1) of target tgt, the items of one target being [first, first+count).
+struct GradItem {
+  int tgt, c0, c1, first, count;
+};
 template <typename T>
 struct GradArgs {
   const T* f;                   // forward input
@@ -87,6 +92,10 @@ struct GradArgs {
   const int* ldg;               // [T*D]
   int ntgt, D, B;
   int stride[kMaxDims];
+  const GradItem* items;        // chunked kernel: [nitems] (NULL: one CTA per target)
+  int nitems;
+  T* partial;                   // [nitems][P*P] item sums
+  int* counter;                 // [ntgt] items finished (last arriver sums and resets to 0)
 };
 template <typename T>
 cudaError_t launch_grad(const GradArgs<T>& a, int P, cudaStream_t s);
@@ -142,6 +151,10 @@ struct asg_plan {
   asg::GradTarget* d_g_tgt = nullptr;
   int* d_ldg = nullptr;
   void** d_gptrs = nullptr;
+  std::vector<asg::GradItem> g_items;  // chunked gradient (single-factor terms, deg 4)
+  asg::GradItem* d_g_items = nullptr;
+  void* d_g_partial = nullptr;         // nitems * 16 doubles
+  int* d_g_counter = nullptr;
   std::vector<asg::EntryDesc> ed;   // single-mode descriptors (empty unless every term has one factor)
   asg::EntryDesc* d_ed = nullptr;
   std::vector<int> row_order;

@@ -54,6 +54,9 @@ void free_device(asg_plan* p) {
   cudaFree(p->d_g_tgt);
   cudaFree(p->d_ldg);
   cudaFree(p->d_gptrs);
+  cudaFree(p->d_g_items);
+  cudaFree(p->d_g_partial);
+  cudaFree(p->d_g_counter);
   cudaFree(p->d_idx1d);
   cudaFree(p->d_op_nb);
   cudaFree(p->d_active);
@@ -358,10 +361,30 @@ asg_status build_grad(asg_plan* p) {
     p->g_contrib.insert(p->g_contrib.end(), kv.second.begin(), kv.second.end());
     p->g_ptr.push_back(static_cast<long long>(p->g_contrib.size()));
   }
+  // terms with one applied factor at deg 4: chunked kernel (items of up to 8 contributors)
+  bool single = p->P == 4;
+  for (int t = 0; t < p->T; ++t) single = single && __builtin_popcount(p->active[t]) == 1;
+  p->g_items.clear();
+  if (single) {
+    for (size_t g = 0; g < p->g_tgt.size(); ++g) {
+      const int first = static_cast<int>(p->g_items.size());
+      const long long c0 = p->g_ptr[g], c1 = p->g_ptr[g + 1];
+      const int count = static_cast<int>((c1 - c0 + 7) / 8);
+      for (long long c = c0; c < c1; c += 8)
+        p->g_items.push_back({static_cast<int>(g), static_cast<int>(c), static_cast<int>(std::min(c + 8, c1)), first,
+                              count});
+    }
+  }
   asg_status st;
   if ((st = upload(&p->d_g_ptr, p->g_ptr))) return st;
   if ((st = upload(&p->d_g_contrib, p->g_contrib))) return st;
   if ((st = upload(&p->d_g_tgt, p->g_tgt))) return st;
+  if (!p->g_items.empty()) {
+    if ((st = upload(&p->d_g_items, p->g_items))) return st;
+    ASG_CUDA(cudaMalloc(&p->d_g_partial, p->g_items.size() * 16 * sizeof(double)));
+    ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_g_counter), p->g_tgt.size() * sizeof(int)));
+    ASG_CUDA(cudaMemset(p->d_g_counter, 0, p->g_tgt.size() * sizeof(int)));
+  }
   ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_ldg), sizeof(int) * p->T * D));
   ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_gptrs), sizeof(void*) * p->T * D));
   return ASG_OK;
@@ -398,6 +421,12 @@ asg_status grad_ops(asg_plan* p, const T* f, const T* r, T* const* G, const int*
   a.ntgt = static_cast<int>(p->g_tgt.size());
   a.D = p->D;
   a.B = p->B;
+  if (!p->g_items.empty()) {
+    a.items = p->d_g_items;
+    a.nitems = static_cast<int>(p->g_items.size());
+    a.partial = static_cast<T*>(p->d_g_partial);
+    a.counter = p->d_g_counter;
+  }
   int sd = 1;
   for (int m = p->D - 1; m >= 0; --m) {
     a.stride[m] = sd;
