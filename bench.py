@@ -316,6 +316,12 @@ def implicit_steps(dev, nsteps=10):
         out[mode] = {"ms_per_step": ms, "outer_iters": outer, "inner_iters": inner, "max_rel_residual": worst}
         finals[mode] = f
     out["mixed_speedup"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
+    # the operator application alone, both precisions (L2-resident, as inside the solver)
+    stream = torch.cuda.current_stream(dev)
+    x64 = torch.from_numpy(f0).to(dev)
+    for name, x in (("apply_fp64_us", x64), ("apply_fp32_us", x64.float())):
+        ms = time_device(plan, x, torch.empty_like(x), lambda: None, 200, 10, stream)
+        out[name] = 1e3 * sum(ms) / len(ms)
     out["rel_diff_mixed_vs_fp64"] = float(torch.linalg.norm(finals["mixed"] - finals["fp64"]) /
                                           torch.linalg.norm(finals["fp64"]))
     out["dof"] = plan.dof

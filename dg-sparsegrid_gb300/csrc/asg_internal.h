@@ -101,7 +101,7 @@ template <typename T>
 cudaError_t launch_grad(const GradArgs<T>& a, int P, cudaStream_t s);
 
 enum KernelKind { KK_CHAIN_WARP = 0, KK_CHAIN_CTA = 1, KK_SINGLE_MODE = 2, KK_SINGLE_TMA = 3, KK_SINGLE_TMA3 = 4,
-                  KK_SINGLE_TMA_ROWS = 5 };
+                  KK_SINGLE_TMA_ROWS = 5, KK_SINGLE_SMALL = 6 };
 
 // Resident CTAs per SM of the persistent single-mode kernel for element size es (4 or 8);
 // sets the kernel's dynamic shared-memory limit first.  0 on error.

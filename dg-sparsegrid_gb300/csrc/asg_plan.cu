@@ -158,11 +158,14 @@ asg_status finalize(asg_plan* p) {
   for (int i = 0; i < N; ++i)
     for (long long q = p->row_ptr[i]; q < p->row_ptr[i + 1]; ++q)
       p->flops_exec += 2.0 * pd1 * __builtin_popcount(p->active[ent[q] & 15]);
-  bool single = detect && (P == 3 || P == 4) && B >= 32LL * P * P;
+  // single_terms: every term has exactly one applied factor (advection/diffusion terms once
+  // the mass factors are the identity); single: additionally a large block for the fiber kernels
+  bool single_terms = detect && N > 0;
   for (int t = 0; t < T; ++t)
-    if (__builtin_popcount(p->active[t]) != 1) single = false;
+    if (__builtin_popcount(p->active[t]) != 1) single_terms = false;
+  const bool single = single_terms && (P == 3 || P == 4) && B >= 32LL * P * P;
   p->kernel_kind = single ? ((P == 4 && B == 4096) ? KK_SINGLE_TMA : KK_SINGLE_MODE)
-                          : (B <= 256 ? KK_CHAIN_WARP : KK_CHAIN_CTA);
+                          : (B <= 256 ? (single_terms ? KK_SINGLE_SMALL : KK_CHAIN_WARP) : KK_CHAIN_CTA);
   p->row_order.clear();
   p->ed.clear();
   if (single) {
@@ -172,6 +175,8 @@ asg_status finalize(asg_plan* p) {
     std::stable_sort(p->row_order.begin(), p->row_order.end(), [&](int x, int y) {
       return p->row_ptr[x + 1] - p->row_ptr[x] > p->row_ptr[y + 1] - p->row_ptr[y];
     });
+  }
+  if (single_terms) {
     // per-entry descriptors of the single-mode kernels: column, dimension, block offset
     p->ed.resize(ent.size());
     for (int i = 0; i < N; ++i)
@@ -775,7 +780,12 @@ asg_status asg_plan_set_kernel(asg_plan* p, int kind) {
     if (!ok || p->ed.size() != p->ent.size())
       return fail(ASG_ERR_UNSUPPORTED, "single-mode kernels need one non-identity factor per term (deg 3/4)");
   }
-  if (kind < 0 || kind > 5) return fail(ASG_ERR_INVALID, "unknown kernel kind %d", kind);
+  if (kind == asg::KK_SINGLE_SMALL) {
+    bool ok = p->B <= 256 && p->ed.size() == p->ent.size();
+    for (unsigned a : p->active) ok = ok && __builtin_popcount(a) == 1;
+    if (!ok) return fail(ASG_ERR_UNSUPPORTED, "small single-mode kernel needs one applied factor per term, deg^d <= 256");
+  }
+  if (kind < 0 || kind > 6) return fail(ASG_ERR_INVALID, "unknown kernel kind %d", kind);
   p->kernel_kind = kind;
   return ASG_OK;
 }

@@ -15,8 +15,21 @@
 namespace asg {
 namespace {
 
-constexpr int kRedBlocks = 304;  // partial sums per reduction (2 per SM)
+constexpr int kRedBlocks = 304;  // most partial sums per reduction (2 per SM)
+constexpr int kMaxRestart = 64;  // largest GMRES restart length (Hessenberg staged in shared memory)
 constexpr int kRedThreads = 256;
+// partial sums for a reduction over n values: one block per 4096 values, at most kRedBlocks
+inline int red_blocks(long long n) {
+  const long long b = (n + 4095) / 4096;
+  return static_cast<int>(b < 1 ? 1 : (b > kRedBlocks ? kRedBlocks : b));
+}
+// sum of nb partials by one warp: lane-strided sums, then a fixed shuffle tree (lane 0 has it)
+__device__ __forceinline__ double warp_sum_partials(const double* __restrict__ p, int nb, int lane) {
+  double s = 0.0;
+  for (int b = lane; b < nb; b += 32) s += p[b];
+  for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+  return s;
+}
 
 // ---------------------------------------------------------------------------------------
 // RK3 stage updates (time_advance.m:177-204):
@@ -60,36 +73,6 @@ __global__ void k_lincomb(long long n, int ns, const T* __restrict__ c, const T*
 // ---------------------------------------------------------------------------------------
 // GMRES helpers.  Basis vectors V (FP32 in mixed mode, FP64 otherwise), FP64 work vectors.
 // ---------------------------------------------------------------------------------------
-// partial[j * kRedBlocks + b] = sum over block b's slice of w * V_j, j < k (FP64 sums)
-template <typename TV>
-__global__ void __launch_bounds__(kRedThreads) k_dots(long long n, int k, const double* __restrict__ w,
-                                                      const TV* __restrict__ V, long long ldv,
-                                                      double* __restrict__ partial) {
-  __shared__ double red[kRedThreads / 32];
-  const int j = blockIdx.y;
-  const TV* v = V + j * ldv;
-  double acc = 0.0;
-  for (long long i = blockIdx.x * static_cast<long long>(kRedThreads) + threadIdx.x; i < n;
-       i += static_cast<long long>(gridDim.x) * kRedThreads)
-    acc = fma(w[i], static_cast<double>(v[i]), acc);
-  for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (int q = 0; q < kRedThreads / 32; ++q) s += red[q];
-    partial[j * static_cast<long long>(gridDim.x) + blockIdx.x] = s;
-  }
-  (void)k;
-}
-// out[j] = sum_b partial[j * nb + b] in block order (deterministic second pass)
-__global__ void k_dots_final(int k, int nb, const double* __restrict__ partial, double* __restrict__ out) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= k) return;
-  double s = 0.0;
-  for (int b = 0; b < nb; ++b) s += partial[j * static_cast<long long>(nb) + b];
-  out[j] = s;
-}
 // partial[b] = sum of x^2 over block b's slice
 __global__ void __launch_bounds__(kRedThreads) k_norm2(long long n, const double* __restrict__ x,
                                                        double* __restrict__ partial) {
@@ -107,42 +90,12 @@ __global__ void __launch_bounds__(kRedThreads) k_norm2(long long n, const double
     partial[blockIdx.x] = s;
   }
 }
-// w -= sum_{j<k} h[j] V_j   (h on the device)
-template <typename TV>
-__global__ void k_orth_update(long long n, int k, const double* __restrict__ h, const TV* __restrict__ V, long long ldv,
-                              double* __restrict__ w) {
-  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<long long>(gridDim.x) * blockDim.x) {
-    double acc = w[i];
-    for (int j = 0; j < k; ++j) acc = fma(-h[j], static_cast<double>(V[j * ldv + i]), acc);
-    w[i] = acc;
-  }
-}
 // V_j = w * inv  (stored in the basis precision)
 template <typename TV>
 __global__ void k_store_basis(long long n, double inv, const double* __restrict__ w, TV* __restrict__ vj) {
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<long long>(gridDim.x) * blockDim.x)
     vj[i] = static_cast<TV>(w[i] * inv);
-}
-// w = x - dt * ax   (the operator I - dt A applied, ax = A x in the matvec precision)
-template <typename TV, typename TA>
-__global__ void k_shift(long long n, double dt, const TV* __restrict__ x, const TA* __restrict__ ax,
-                        double* __restrict__ w) {
-  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<long long>(gridDim.x) * blockDim.x)
-    w[i] = static_cast<double>(x[i]) - dt * static_cast<double>(ax[i]);
-}
-// x += sum_j y[j] V_j  (FP64 solution update; y on the device)
-template <typename TV>
-__global__ void k_sol_update(long long n, int k, const double* __restrict__ y, const TV* __restrict__ V, long long ldv,
-                             double* __restrict__ x) {
-  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<long long>(gridDim.x) * blockDim.x) {
-    double acc = x[i];
-    for (int j = 0; j < k; ++j) acc = fma(y[j], static_cast<double>(V[j * ldv + i]), acc);
-    x[i] = acc;
-  }
 }
 // r = b - (x - dt * ax)   (FP64 outer residual)
 __global__ void k_residual(long long n, double dt, const double* __restrict__ b, const double* __restrict__ x,
@@ -151,10 +104,166 @@ __global__ void k_residual(long long n, double dt, const double* __restrict__ b,
        i += static_cast<long long>(gridDim.x) * blockDim.x)
     r[i] = b[i] - (x[i] - dt * ax[i]);
 }
-__global__ void k_copy_f64(long long n, const double* __restrict__ a, double* __restrict__ b) {
+// ---- device-side Arnoldi/Givens state: a cycle runs without a host round trip per step ----
+struct GmresState {
+  int done;      // cycle finished (converged, breakdown or m steps): later kernels return
+  int kdone;     // Arnoldi steps taken
+  double resid;  // |g[kdone]|, the residual estimate
+  double inv;    // 1 / ||w|| of the last step (scales the next basis vector)
+};
+// w = V_j - dt * (A V_j), skipped once the cycle is done
+template <typename TV>
+__global__ void k_shift_g(long long n, double dt, const TV* __restrict__ x, const TV* __restrict__ ax,
+                          double* __restrict__ w, const GmresState* __restrict__ st) {
+  if (st->done) return;
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<long long>(gridDim.x) * blockDim.x)
-    b[i] = a[i];
+    w[i] = static_cast<double>(x[i]) - dt * static_cast<double>(ax[i]);
+}
+// partial[j * gridDim.x + b] = block b's share of <w, V_j> (FP64), j = blockIdx.y
+template <typename TV>
+__global__ void __launch_bounds__(kRedThreads) k_dots_g(long long n, const double* __restrict__ w,
+                                                        const TV* __restrict__ V, long long ldv,
+                                                        double* __restrict__ partial,
+                                                        const GmresState* __restrict__ st) {
+  if (st->done) return;
+  __shared__ double red[kRedThreads / 32];
+  const int j = blockIdx.y;
+  const TV* v = V + j * ldv;
+  double acc = 0.0;
+  for (long long i = blockIdx.x * static_cast<long long>(kRedThreads) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * kRedThreads)
+    acc = fma(w[i], static_cast<double>(v[i]), acc);
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int q = 0; q < kRedThreads / 32; ++q) s += red[q];
+    partial[j * static_cast<long long>(gridDim.x) + blockIdx.x] = s;
+  }
+}
+// h[j] = sum_b partial (one warp per j, fixed order); the Hessenberg column accumulates both
+// CGS passes
+__global__ void k_dots_final_g(int k, int nb, const double* __restrict__ partial, double* __restrict__ h,
+                               double* __restrict__ hcol, int pass, const GmresState* __restrict__ st) {
+  if (st->done) return;
+  const int j = blockIdx.x;
+  if (j >= k) return;
+  const double s = warp_sum_partials(partial + j * static_cast<long long>(nb), nb, threadIdx.x);
+  if (threadIdx.x == 0) {
+    h[j] = s;
+    hcol[j] = pass ? hcol[j] + s : s;
+  }
+}
+// w -= sum_{j<k} h[j] V_j
+template <typename TV>
+__global__ void k_orth_update_g(long long n, int k, const double* __restrict__ h, const TV* __restrict__ V,
+                                long long ldv, double* __restrict__ w, const GmresState* __restrict__ st) {
+  if (st->done) return;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    double acc = w[i];
+    for (int j = 0; j < k; ++j) acc = fma(-h[j], static_cast<double>(V[j * ldv + i]), acc);
+    w[i] = acc;
+  }
+}
+__global__ void __launch_bounds__(kRedThreads) k_norm2_g(long long n, const double* __restrict__ x,
+                                                         double* __restrict__ partial,
+                                                         const GmresState* __restrict__ st) {
+  if (st->done) return;
+  __shared__ double red[kRedThreads / 32];
+  double acc = 0.0;
+  for (long long i = blockIdx.x * static_cast<long long>(kRedThreads) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * kRedThreads)
+    acc = fma(x[i], x[i], acc);
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int q = 0; q < kRedThreads / 32; ++q) s += red[q];
+    partial[blockIdx.x] = s;
+  }
+}
+// Step j of the Givens QR of the Hessenberg matrix (one thread): ||w|| from the partials,
+// the previous rotations on the new column, a new rotation, the residual estimate and the
+// stopping decision.
+__global__ void k_givens(int j, int m, double target, int nb, const double* __restrict__ partial,
+                         double* __restrict__ hcol, double* __restrict__ H, double* __restrict__ cs,
+                         double* __restrict__ sn, double* __restrict__ g, GmresState* __restrict__ st) {
+  if (st->done) return;
+  __shared__ double hc[kMaxRestart + 1], c_s[kMaxRestart], s_s[kMaxRestart];
+  const int lane = threadIdx.x;
+  const double acc = warp_sum_partials(partial, nb, lane);
+  for (int i = lane; i <= j; i += 32) hc[i] = hcol[i];  // the column and rotations, staged once
+  for (int i = lane; i < j; i += 32) {
+    c_s[i] = cs[i];
+    s_s[i] = sn[i];
+  }
+  __syncwarp();
+  if (lane == 0) {
+    const double hn = sqrt(acc);
+    hc[j + 1] = hn;
+    for (int i = 0; i < j; ++i) {
+      const double a = c_s[i] * hc[i] + s_s[i] * hc[i + 1];
+      hc[i + 1] = -s_s[i] * hc[i] + c_s[i] * hc[i + 1];
+      hc[i] = a;
+    }
+    const double den = hypot(hc[j], hc[j + 1]);
+    const double c = den > 0 ? hc[j] / den : 1.0, sv = den > 0 ? hc[j + 1] / den : 0.0;
+    cs[j] = c;
+    sn[j] = sv;
+    hc[j] = den;
+    const double gj = g[j];
+    g[j + 1] = -sv * gj;
+    g[j] = c * gj;
+    st->resid = fabs(sv * gj);
+    st->inv = hn > 0 ? 1.0 / hn : 0.0;
+    st->kdone = j + 1;
+    st->done = (st->resid <= target || hn == 0.0 || j + 1 == m) ? 1 : 0;
+  }
+  __syncwarp();
+  for (int i = lane; i <= j; i += 32) H[static_cast<long long>(i) * m + j] = hc[i];
+}
+// V_{j+1} = w / ||w|| (skipped once the cycle is done)
+template <typename TV>
+__global__ void k_store_basis_g(long long n, const double* __restrict__ w, TV* __restrict__ vj,
+                                const GmresState* __restrict__ st) {
+  if (st->done) return;
+  const double inv = st->inv;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x)
+    vj[i] = static_cast<TV>(w[i] * inv);
+}
+// y = H(1:k,1:k) \ g(1:k), k = kdone (one thread, upper triangular)
+__global__ void k_backsolve(int m, const double* __restrict__ H, const double* __restrict__ g, double* __restrict__ y,
+                            const GmresState* __restrict__ st) {
+  __shared__ double hs[kMaxRestart * kMaxRestart], ys[kMaxRestart];
+  const int k = st->kdone;
+  for (int q = threadIdx.x; q < k * k; q += blockDim.x) hs[q] = H[static_cast<long long>(q / k) * m + q % k];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = k - 1; i >= 0; --i) {
+      double acc = g[i];
+      for (int q = i + 1; q < k; ++q) acc -= hs[i * k + q] * ys[q];
+      ys[i] = acc / hs[i * k + i];
+    }
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < k; q += blockDim.x) y[q] = ys[q];
+}
+// x += sum_{j < kdone} y[j] V_j  (FP64 solution update)
+template <typename TV>
+__global__ void k_sol_update_g(long long n, const double* __restrict__ y, const TV* __restrict__ V, long long ldv,
+                               double* __restrict__ x, const GmresState* __restrict__ st) {
+  const int k = st->kdone;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x) {
+    double acc = x[i];
+    for (int j = 0; j < k; ++j) acc = fma(y[j], static_cast<double>(V[j * ldv + i]), acc);
+    x[i] = acc;
+  }
 }
 
 inline int grid_for(long long n) {
@@ -175,7 +284,7 @@ namespace {
 size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 
 struct GmresLayout {
-  size_t v, w, r, ax64, axmv, h, y, partial, total;
+  size_t v, w, r, ax64, axmv, h, y, partial, hcol, hh, cs, sn, g, state, total;
 };
 
 GmresLayout gmres_layout(long long n, int m, bool mixed) {
@@ -194,12 +303,18 @@ GmresLayout gmres_layout(long long n, int m, bool mixed) {
   L.h = take((m + 1) * sizeof(double));
   L.y = take((m + 1) * sizeof(double));
   L.partial = take(static_cast<size_t>(m + 1) * asg::kRedBlocks * sizeof(double));
+  L.hcol = take((m + 1) * sizeof(double));
+  L.hh = take(static_cast<size_t>(m + 1) * m * sizeof(double));
+  L.cs = take(m * sizeof(double));
+  L.sn = take(m * sizeof(double));
+  L.g = take((m + 1) * sizeof(double));
+  L.state = take(sizeof(asg::GmresState));
   L.total = off;
   return L;
 }
 
-double host_norm(const double* d_partial, cudaStream_t s, asg_status* st) {
-  std::vector<double> p(asg::kRedBlocks);
+double host_norm(const double* d_partial, int nb, cudaStream_t s, asg_status* st) {
+  std::vector<double> p(nb);
   cudaError_t e = cudaMemcpyAsync(p.data(), d_partial, p.size() * sizeof(double), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) {
@@ -226,65 +341,55 @@ asg_status gmres_cycle(asg_plan* plan, long long n, double dt, const double* r0,
   const int gr = asg::grid_for(n);
   asg_status st = ASG_OK;
   *iters = 0;
-  asg::k_norm2<<<asg::kRedBlocks, asg::kRedThreads, 0, s>>>(n, r0, partial);
-  const double beta = host_norm(partial, s, &st);
+  const int nb = asg::red_blocks(n);
+  asg::k_norm2<<<nb, asg::kRedThreads, 0, s>>>(n, r0, partial);
+  const double beta = host_norm(partial, nb, s, &st);
   if (st) return st;
   *resid = beta;
   if (beta <= rtol_abs || beta == 0.0) return ASG_OK;
   asg::k_store_basis<TV><<<gr, 256, 0, s>>>(n, 1.0 / beta, r0, V);
-  std::vector<double> H(static_cast<size_t>(m + 1) * m, 0.0), cs(m), sn(m), g(m + 1, 0.0), hcol(m + 1), yv(m);
-  g[0] = beta;
-  int kdone = 0;
-  for (int j = 0; j < m; ++j) {
-    // w = V_j - dt * A V_j
-    asg_status ast = sizeof(TV) == 4 ? asg_apply_f32(plan, reinterpret_cast<const float*>(V + j * n),
-                                                     reinterpret_cast<float*>(axmv), s)
-                                     : asg_apply_f64(plan, reinterpret_cast<const double*>(V + j * n),
-                                                     reinterpret_cast<double*>(axmv), s);
-    if (ast) return ast;
-    asg::k_shift<TV, TV><<<gr, 256, 0, s>>>(n, dt, V + j * n, axmv, w);
-    std::fill(hcol.begin(), hcol.end(), 0.0);
-    std::vector<double> hp(j + 1);
-    for (int pass = 0; pass < 2; ++pass) {  // classical Gram-Schmidt, reorthogonalised (FP64)
-      asg::k_dots<TV><<<dim3(asg::kRedBlocks, j + 1), asg::kRedThreads, 0, s>>>(n, j + 1, w, V, n, partial);
-      asg::k_dots_final<<<1, 64, 0, s>>>(j + 1, asg::kRedBlocks, partial, h_dev);
-      asg::k_orth_update<TV><<<gr, 256, 0, s>>>(n, j + 1, h_dev, V, n, w);
-      ASG_CUDA(cudaMemcpyAsync(hp.data(), h_dev, (j + 1) * sizeof(double), cudaMemcpyDeviceToHost, s));
-      ASG_CUDA(cudaStreamSynchronize(s));
-      for (int i = 0; i <= j; ++i) hcol[i] += hp[i];
+  double* hcol = reinterpret_cast<double*>(base + L.hcol);
+  double* H = reinterpret_cast<double*>(base + L.hh);
+  double* cs = reinterpret_cast<double*>(base + L.cs);
+  double* sn = reinterpret_cast<double*>(base + L.sn);
+  double* g = reinterpret_cast<double*>(base + L.g);
+  asg::GmresState* state = reinterpret_cast<asg::GmresState*>(base + L.state);
+  // g = (beta, 0, ...), state cleared: the Arnoldi steps below run without host round trips;
+  // the host looks at the state every kChunk steps (steps after the stop are no-ops, except
+  // the operator application, which is why the host checks at all)
+  std::vector<double> g0(m + 1, 0.0);
+  g0[0] = beta;
+  ASG_CUDA(cudaMemcpyAsync(g, g0.data(), (m + 1) * sizeof(double), cudaMemcpyHostToDevice, s));
+  ASG_CUDA(cudaMemsetAsync(state, 0, sizeof(asg::GmresState), s));
+  constexpr int kChunk = 4;
+  asg::GmresState hs{};
+  for (int j0 = 0; j0 < m; j0 += kChunk) {
+    for (int j = j0; j < std::min(m, j0 + kChunk); ++j) {
+      // w = V_j - dt * A V_j
+      asg_status ast = sizeof(TV) == 4 ? asg_apply_f32(plan, reinterpret_cast<const float*>(V + j * n),
+                                                       reinterpret_cast<float*>(axmv), s)
+                                       : asg_apply_f64(plan, reinterpret_cast<const double*>(V + j * n),
+                                                       reinterpret_cast<double*>(axmv), s);
+      if (ast) return ast;
+      asg::k_shift_g<TV><<<gr, 256, 0, s>>>(n, dt, V + j * n, axmv, w, state);
+      for (int pass = 0; pass < 2; ++pass) {  // classical Gram-Schmidt, reorthogonalised (FP64)
+        asg::k_dots_g<TV><<<dim3(nb, j + 1), asg::kRedThreads, 0, s>>>(n, w, V, n, partial, state);
+        asg::k_dots_final_g<<<j + 1, 32, 0, s>>>(j + 1, nb, partial, h_dev, hcol, pass, state);
+        asg::k_orth_update_g<TV><<<gr, 256, 0, s>>>(n, j + 1, h_dev, V, n, w, state);
+      }
+      asg::k_norm2_g<<<nb, asg::kRedThreads, 0, s>>>(n, w, partial, state);
+      asg::k_givens<<<1, 32, 0, s>>>(j, m, rtol_abs, nb, partial, hcol, H, cs, sn, g, state);
+      asg::k_store_basis_g<TV><<<gr, 256, 0, s>>>(n, w, V + (j + 1) * n, state);
     }
-    asg::k_norm2<<<asg::kRedBlocks, asg::kRedThreads, 0, s>>>(n, w, partial);
-    const double hn = host_norm(partial, s, &st);
-    if (st) return st;
-    hcol[j + 1] = hn;
-    // previous Givens rotations, then a new one (FP64, host)
-    for (int i = 0; i < j; ++i) {
-      const double a = cs[i] * hcol[i] + sn[i] * hcol[i + 1];
-      hcol[i + 1] = -sn[i] * hcol[i] + cs[i] * hcol[i + 1];
-      hcol[i] = a;
-    }
-    const double den = std::hypot(hcol[j], hcol[j + 1]);
-    cs[j] = den > 0 ? hcol[j] / den : 1.0;
-    sn[j] = den > 0 ? hcol[j + 1] / den : 0.0;
-    hcol[j] = den;
-    g[j + 1] = -sn[j] * g[j];
-    g[j] = cs[j] * g[j];
-    for (int i = 0; i <= j; ++i) H[static_cast<size_t>(i) * m + j] = hcol[i];
-    kdone = j + 1;
-    *resid = std::fabs(g[j + 1]);
-    if (*resid <= rtol_abs || hn == 0.0) break;
-    if (j + 1 < m) asg::k_store_basis<TV><<<gr, 256, 0, s>>>(n, 1.0 / hn, w, V + (j + 1) * n);
+    ASG_CUDA(cudaMemcpyAsync(&hs, state, sizeof(hs), cudaMemcpyDeviceToHost, s));
+    ASG_CUDA(cudaStreamSynchronize(s));
+    if (hs.done) break;
   }
-  // back substitution H y = g, then x += V y (FP64 update)
-  for (int i = kdone - 1; i >= 0; --i) {
-    double acc = g[i];
-    for (int k = i + 1; k < kdone; ++k) acc -= H[static_cast<size_t>(i) * m + k] * yv[k];
-    yv[i] = acc / H[static_cast<size_t>(i) * m + i];
-  }
-  ASG_CUDA(cudaMemcpyAsync(y_dev, yv.data(), kdone * sizeof(double), cudaMemcpyHostToDevice, s));
-  asg::k_sol_update<TV><<<gr, 256, 0, s>>>(n, kdone, y_dev, V, n, x64);
-  ASG_CUDA(cudaStreamSynchronize(s));  // yv is host memory read by the copy above
-  *iters = kdone;
+  // back substitution H y = g and x += V y (FP64 update), on the device
+  asg::k_backsolve<<<1, 256, 0, s>>>(m, H, g, y_dev, state);
+  asg::k_sol_update_g<TV><<<gr, 256, 0, s>>>(n, y_dev, V, n, x64, state);
+  *iters = hs.kdone;
+  *resid = hs.resid;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return asg::cuda_fail(e, "gmres kernels");
   return ASG_OK;
@@ -306,8 +411,9 @@ asg_status be_solve(asg_plan* p, double dt, const double* b, double* x, const as
   double* partial = reinterpret_cast<double*>(base + L.partial);
   const int gr = asg::grid_for(n);
   asg_status st = ASG_OK;
-  asg::k_norm2<<<asg::kRedBlocks, asg::kRedThreads, 0, s>>>(n, b, partial);
-  const double bnorm = host_norm(partial, s, &st);
+  const int nb = asg::red_blocks(n);
+  asg::k_norm2<<<nb, asg::kRedThreads, 0, s>>>(n, b, partial);
+  const double bnorm = host_norm(partial, nb, s, &st);
   if (st) return st;
   asg_gmres_info inf{};
   inf.rel_residual = 1.0;
@@ -315,8 +421,8 @@ asg_status be_solve(asg_plan* p, double dt, const double* b, double* x, const as
     // FP64 outer residual r = b - (I - dt A) x
     if ((st = asg_apply_f64(p, x, ax64, s))) return st;
     asg::k_residual<<<gr, 256, 0, s>>>(n, dt, b, x, ax64, r);
-    asg::k_norm2<<<asg::kRedBlocks, asg::kRedThreads, 0, s>>>(n, r, partial);
-    const double rn = host_norm(partial, s, &st);
+    asg::k_norm2<<<nb, asg::kRedThreads, 0, s>>>(n, r, partial);
+    const double rn = host_norm(partial, nb, s, &st);
     if (st) return st;
     inf.rel_residual = bnorm > 0 ? rn / bnorm : rn;
     inf.outer_iters = outer;
@@ -392,7 +498,7 @@ asg_status asg_lincomb_f64(long long n, int ns, const double* d_coef, const doub
 
 asg_status asg_be_workspace(const asg_plan* plan, const asg_gmres_opts* opts, size_t* bytes) {
   if (!plan || !opts || !bytes) return fail(ASG_ERR_INVALID, "be_workspace: NULL argument");
-  if (opts->restart < 1 || opts->restart > 200) return fail(ASG_ERR_INVALID, "be_workspace: restart=%d", opts->restart);
+  if (opts->restart < 1 || opts->restart > asg::kMaxRestart) return fail(ASG_ERR_INVALID, "be_workspace: restart=%d", opts->restart);
   asg_plan_stats ps{};
   asg_plan_stats_get(plan, &ps);
   *bytes = gmres_layout(ps.dof, opts->restart, opts->mixed != 0).total;
@@ -402,7 +508,7 @@ asg_status asg_be_workspace(const asg_plan* plan, const asg_gmres_opts* opts, si
 asg_status asg_be_solve(asg_plan* plan, double dt, const double* d_b, double* d_x, const asg_gmres_opts* opts,
                         asg_gmres_info* info, void* d_work, size_t work_bytes, void* stream) {
   if (!plan || !d_b || !d_x || !opts || !d_work) return fail(ASG_ERR_INVALID, "be_solve: NULL argument");
-  if (opts->restart < 1 || opts->restart > 200 || opts->max_outer < 0 || !(opts->tol > 0) ||
+  if (opts->restart < 1 || opts->restart > asg::kMaxRestart || opts->max_outer < 0 || !(opts->tol > 0) ||
       !(opts->inner_reduction > 0 && opts->inner_reduction < 1))
     return fail(ASG_ERR_INVALID, "be_solve: bad options");
   return opts->mixed ? be_solve<float>(plan, dt, d_b, d_x, opts, info, d_work, work_bytes, stream)

@@ -198,7 +198,7 @@ asg_status asg_lincomb_f64(long long n, int ns, const double* d_coef, const doub
                            void* stream);
 
 typedef struct {
-  int restart;             /* GMRES(m) Krylov dimension per cycle */
+  int restart;             /* GMRES(m) Krylov dimension per cycle, 1..64 */
   int max_outer;           /* refinement steps (each one GMRES cycle on the FP64 residual) */
   double tol;              /* stop when ||b - (I - dt A) x|| <= tol * ||b|| */
   double inner_reduction;  /* each cycle stops once its residual drops by this factor */

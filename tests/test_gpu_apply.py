@@ -135,6 +135,31 @@ def test_continuity6_lev4_deg4_kernels_agree(dev):
     assert rel2(y_none, y_single) <= FP64_TOL
 
 
+@pytest.mark.parametrize("name,lev,deg", [("continuity2", 4, 2), ("continuity2", 3, 4), ("continuity3", 4, 3),
+                                          ("continuity3", 3, 4), ("diffusion2", 5, 4), ("continuity6", 2, 2),
+                                          ("continuity3", 2, 6)])
+def test_small_block_single_mode_kernel(dev, name, lev, deg):
+    """Small blocks (deg^d <= 256) with one applied factor per term run the grouped-lane kernel
+    by default: FP64 against the oracle, against the warp chain kernel, FP32 against FP64,
+    and bitwise repeatable."""
+    import asgkron
+
+    pde, table, idx, mats = problem(name, lev, deg)
+    N, D = idx.shape
+    B = deg ** D
+    f = np.random.default_rng(lev * 10 + deg).standard_normal(N * B)
+    p = _plan(mats, idx, deg)
+    assert p.stats()["kernel_kind"] == 6
+    y = _apply(p, f, dev)
+    assert np.array_equal(_apply(p, f, dev), y)
+    rows = np.arange(0, N, max(1, N // 6))
+    want = O.apply_A_rows(mats, idx.astype(np.int64), deg, f, rows=rows)
+    assert rel2(y.reshape(-1, B)[rows].ravel(), want) <= FP64_TOL
+    assert rel2(_apply(p, f, dev, torch.float32), y) <= FP32_TOL
+    p.set_kernel(asgkron._lib.KERNEL_CHAIN_WARP)
+    assert rel2(_apply(p, f, dev), y) <= FP64_TOL
+
+
 @pytest.mark.parametrize("lev", [2, 3])
 def test_continuity6_small_levels_row_lists(dev, lev):
     """continuity6 deg 4 at levels with fewer elements than resident CTAs (one row per CTA)
