@@ -1,0 +1,107 @@
+"""Row-sharded apply over ranks: partitioning, per-rank pair lists and the f all-gather,
+exercised with world_size 2 over gloo on CPU.  The per-rank compute is the oracle restricted
+to the rank's rows (stand-in for the GPU plan, which needs a device)."""
+import os
+import socket
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_partition_rows_balances_prefix_sums():
+    from asgkron.shard import partition_rows
+
+    cost = np.array([5, 1, 1, 1, 1, 1, 10, 1, 1, 1, 1, 1])
+    parts = partition_rows(cost, 3)
+    assert parts[0][0] == 0 and parts[-1][1] == cost.size
+    assert all(a[1] == b[0] for a, b in zip(parts, parts[1:]))
+    loads = [cost[r0:r1].sum() for r0, r1 in parts]
+    assert sum(loads) == cost.sum() and max(loads) <= 13
+    assert partition_rows(np.ones(7), 1) == [(0, 7)]
+    p = partition_rows(np.ones(3), 5)  # more ranks than rows: some ranges are empty
+    assert p[0][0] == 0 and p[-1][1] == 3 and all(r0 <= r1 for r0, r1 in p)
+
+
+def test_row_pairs_keeps_only_the_range():
+    from asgkron.shard import row_pairs
+
+    N = 6
+    rp, cl = row_pairs(N, (2, 4))
+    assert list(np.diff(rp)) == [0, 0, N, N, 0, 0] and list(cl) == list(range(N)) * 2
+    full_rp = np.array([0, 2, 3, 6, 6, 8, 9])
+    full_cl = np.array([0, 1, 2, 0, 3, 5, 1, 4, 5])
+    rp, cl = row_pairs(N, (1, 5), (full_rp, full_cl))
+    assert list(np.diff(rp)) == [0, 1, 3, 0, 2, 0]
+    assert list(cl) == [2, 0, 3, 5, 1, 4]
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _worker(rank, world, port, out_path):
+    sys.path[:0] = [ROOT, os.path.join(ROOT, "dg-sparsegrid_gb300"), os.path.join(ROOT, "tests")]
+    import torch
+    import torch.distributed as dist
+
+    from cases import problem
+    from oracle import asgard_oracle as O
+    from asgkron.shard import ShardedApply, partition_rows
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        _, _, idx, mats = problem("continuity2", 4, 2)
+        deg = 2
+        N, D = idx.shape
+        B = deg ** D
+        idx64 = idx.astype(np.int64)
+        f = np.random.default_rng(0).standard_normal(N * B)
+        ranges = partition_rows(np.full(N, N), world)
+
+        class OracleRows:  # the rank's plan: rows of its range, zeros elsewhere
+            def __init__(self, r0, r1):
+                self.rows = np.arange(r0, r1)
+
+            def apply(self, ft):
+                y = np.zeros(N * B)
+                if self.rows.size:
+                    vals = O.apply_A_rows(mats, idx64, deg, ft.numpy(), rows=self.rows)
+                    y.reshape(N, B)[self.rows] = vals.reshape(-1, B)
+                return torch.from_numpy(y)
+
+        r0, r1 = ranges[rank]
+        sharded = ShardedApply(OracleRows(r0, r1), ranges, B)
+        f_local = torch.from_numpy(f.reshape(N, B)[r0:r1].ravel().copy())
+        # the gathered f is the full vector on every rank
+        assert torch.equal(sharded.gather_f(f_local), torch.from_numpy(f))
+        y_local = sharded.apply(f_local)
+        parts = [torch.zeros(max(sharded.counts), dtype=torch.float64) for _ in range(world)]
+        buf = torch.zeros(max(sharded.counts), dtype=torch.float64)
+        buf[:y_local.numel()] = y_local
+        dist.all_gather(parts, buf)
+        if rank == 0:
+            y = torch.cat([p[:c] for p, c in zip(parts, sharded.counts)]).numpy()
+            want = O.apply_A_rows(mats, idx64, deg, f)
+            err = np.linalg.norm(y - want) / np.linalg.norm(want)
+            with open(out_path, "w") as fh:
+                fh.write("%.17g %r" % (float(err), [[int(a), int(b)] for a, b in ranges]))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_sharded_apply_two_gloo_ranks(tmp_path):
+    torch = pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+
+    out = str(tmp_path / "res.txt")
+    mp.start_processes(_worker, args=(2, _free_port(), out), nprocs=2, join=True, start_method="spawn")
+    err, ranges = open(out).read().split(" ", 1)
+    assert float(err) <= 1e-14, (err, ranges)
+    assert "[0," in ranges
