@@ -457,6 +457,52 @@ def run_batched(args, rank, local):
         p.close()
 
 
+def graph_replay(plan, f, y, stream, n_apply=100, reps=10):
+    """n_apply back-to-back applies captured in one CUDA graph (no flush between them: the
+    operands stay in L2), replayed reps times; returns microseconds per apply."""
+    import torch
+
+    for _ in range(3):
+        plan.apply(f, y, stream)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=stream):
+        for _ in range(n_apply):
+            plan.apply(f, y, stream)
+    with torch.cuda.stream(stream):  # replay on the stream the events are recorded on
+        g.replay()
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        for _ in range(reps):
+            g.replay()
+        e.record(stream)
+    torch.cuda.synchronize()
+    return 1e3 * s.elapsed_time(e) / (reps * n_apply)
+
+
+def small_config_graph(dev):
+    """CPU-runnable configuration: continuity2 SG 4, deg 2 (48 elements, 192 DOF), FP64, f ~
+    N(0,1) seed 0; 100 applies per CUDA graph (a single apply lasts microseconds)."""
+    import numpy as np
+    import torch
+
+    import asgkron
+    from asgkron import pdes
+
+    pde = pdes.continuity2(4)
+    idx = asgkron.hash_table_sparse_nD(pde.levels, 8).idx1d()
+    plan = asgkron.Plan.create(pde.term_mats(2), idx, 2)
+    f = torch.from_numpy(np.random.default_rng(0).standard_normal(plan.dof)).to(dev)
+    y = torch.empty_like(f)
+    stream = torch.cuda.Stream(dev)
+    us = graph_replay(plan, f, y, stream)
+    out = {"dof": plan.dof, "us_per_apply": us, "value": plan.dof / (us * 1e-6) / 1e9,
+           "kernel": asgkron._lib.KERNEL_NAMES[plan.stats()["kernel_kind"]]}
+    plan.close()
+    return out
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_env()
@@ -564,6 +610,12 @@ def main():
         ystar = torch.from_numpy(np.random.default_rng(5).standard_normal(dof).astype(np.float32)).to(dev)
         variants["fp32_forward_backward"] = forward_backward(plan, f32, ystar, flush, max(5, min(args.steps, 200)),
                                                              stream, dof, n1d)
+        gstream = torch.cuda.Stream(dev)
+        variants["fp32_graph_100_applies_l2_resident"] = {
+            "us_per_apply": graph_replay(plan, f32, y32, gstream)}
+        variants["fp32_graph_100_applies_l2_resident"]["value"] = (
+            dof / (variants["fp32_graph_100_applies_l2_resident"]["us_per_apply"] * 1e-6) / 1e9)
+        variants["continuity2_lev4_deg2_fp64_graph"] = small_config_graph(dev)
         variants["implicit_diffusion2_lev8_deg4"] = implicit_steps(dev)
         variants["precision_continuity3_lev6_deg3"] = precision_continuity3(dev, flush, stream)
 

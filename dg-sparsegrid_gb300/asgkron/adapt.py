@@ -1,0 +1,115 @@
+"""Adaptive element tables (adapt.m) and the plan rebuild that follows them.
+
+``adapt`` restates adapt.m's element rules on the dense table arrays:
+
+* thresholds (adapt.m:15-18): refine where max|f_e| >= max|f| * rel, coarsen where
+  max|f_e| <= 0.1 * that (and nothing happens when max|f| is zero);
+* coarsening (adapt.m:92-200): every element below the coarsening threshold is removed
+  with its coefficients; the others keep their order;
+* refinement (adapt.m:252-340): for each remaining element at or above the refinement
+  threshold, its daughters (get_child_elements.m, methods 1 and 2) that are not in the
+  table yet are appended, in discovery order, with coefficient value 1e-15.
+
+``rebuild_plan`` then builds the plan for the new table with the same 1-D operators (built
+at the maximum level, so every new 1-D index has its rows; adapt.m:417-437 rebuilds the
+coefficient matrices only when they were not).  Plan creation is the whole cost of an
+adaptation step on the device side: structure analysis, work list, uploads.
+"""
+import numpy as np
+
+from .grid import ElementTable, element_idx1d
+
+NEW_ELEMENT_VALUE = 1e-15  # adapt.m:20
+
+
+def child_elements(lev, pos, max_lev, method=1):
+    """Daughters of one element (get_child_elements.m): per dimension d, (lev+1, 2 pos) and,
+    when lev_d >= 1, (lev+1, 2 pos + 1), each only while lev_d + 1 < max_lev; method 2 adds the
+    combinations of the 1-D daughters across dimensions.  Returns [(lev tuple, pos tuple)]."""
+    lev = [int(v) for v in lev]
+    pos = [int(v) for v in pos]
+    d = len(lev)
+    out = []
+    new_1d = [[] for _ in range(d)]
+    for k in range(d):
+        if lev[k] + 1 < max_lev:
+            l2, p2 = list(lev), list(pos)
+            l2[k] += 1
+            p2[k] = 2 * pos[k]
+            out.append((tuple(l2), tuple(p2)))
+            new_1d[k].append((l2[k], p2[k]))
+            if lev[k] >= 1:
+                l3, p3 = list(lev), list(pos)
+                l3[k] += 1
+                p3[k] = 2 * pos[k] + 1
+                out.append((tuple(l3), tuple(p3)))
+                new_1d[k].append((l3[k], p3[k]))
+    if method == 2 and all(new_1d):
+        # every combination of the 1-D daughters (the tensor-product children)
+        combos = [[]]
+        for k in range(d):
+            combos = [c + [v] for c in combos for v in new_1d[k]]
+        for c in combos:
+            out.append((tuple(v[0] for v in c), tuple(v[1] for v in c)))
+    return out
+
+
+def md_keys(levels, cells, max_lev):
+    """0-based md keys (md_lev_pos_to_idx.m minus one): sum_d (idx1d_d - 1) * 2^(max_lev d)."""
+    idx = element_idx1d(levels, cells).astype(np.uint64) - 1
+    key = np.zeros(idx.shape[0], dtype=np.uint64)
+    for k in range(idx.shape[1]):
+        key += idx[:, k] << np.uint64(max_lev * k)
+    return key
+
+
+class AdaptResult:
+    def __init__(self, table, fval, removed, added):
+        self.table = table        # the new ElementTable
+        self.fval = fval          # coefficients on the new table
+        self.removed = removed    # indices (into the old table) of removed elements
+        self.added = added        # number of appended elements
+
+
+def adapt(table, fval, deg, max_lev, rel_threshold, coarsen=True, refine=True, method=1):
+    """One adaptation step of adapt.m on an element table and its coefficient vector."""
+    levels = np.asarray(table.levels, dtype=np.int32)
+    cells = np.asarray(table.cells, dtype=np.int32)
+    N, d = levels.shape
+    B = deg ** d
+    f = np.asarray(fval, dtype=np.float64).reshape(N, B)
+    if levels.size and int(levels.max()) > max_lev:
+        raise ValueError("adapt: element level above max_lev=%d" % max_lev)
+    refine_thr = float(np.abs(f).max()) * rel_threshold if N else 0.0
+    coarsen_thr = 0.1 * refine_thr
+    if refine_thr <= 0:
+        coarsen = refine = False
+    emax = np.abs(f).max(axis=1) if N else np.zeros(0)
+    removed = np.nonzero(emax <= coarsen_thr)[0] if coarsen else np.zeros(0, dtype=np.int64)
+    keep = np.ones(N, dtype=bool)
+    keep[removed] = False
+    levels, cells, f, emax = levels[keep], cells[keep], f[keep], emax[keep]
+    added_lev, added_pos = [], []
+    if refine:
+        present = {(tuple(l), tuple(c)) for l, c in zip(levels.tolist(), cells.tolist())}
+        for n in np.nonzero(emax >= refine_thr)[0]:
+            for child in child_elements(levels[n], cells[n], max_lev, method):
+                if child not in present:
+                    present.add(child)
+                    added_lev.append(child[0])
+                    added_pos.append(child[1])
+    if added_lev:
+        levels = np.vstack([levels, np.array(added_lev, dtype=np.int32)])
+        cells = np.vstack([cells, np.array(added_pos, dtype=np.int32)])
+        f = np.vstack([f, np.full((len(added_lev), B), NEW_ELEMENT_VALUE)])
+    new = ElementTable(np.ascontiguousarray(levels), np.ascontiguousarray(cells),
+                       md_keys(levels, cells, max_lev) if levels.shape[0] else np.zeros(0, dtype=np.uint64))
+    return AdaptResult(new, f.reshape(-1), removed, len(added_lev))
+
+
+def rebuild_plan(plan, table, pairs=None, **kw):
+    """A plan for the adapted table with the operators and work model of ``plan``."""
+    from .api import Plan
+
+    structure = kw.pop("structure", plan.structure)
+    return Plan.create(plan.term_mats, table.idx1d(), plan.deg, pairs=pairs, structure=structure, **kw)

@@ -47,6 +47,7 @@ class Plan:
             raise ValueError("term_mats must hold num_terms lists of num_dims operators")
         deg = None
         self.term_mats = mats
+        self.structure = structure
         self.N, self.D, self.T = N, D, T
         self._keep = [mats, idx]
         ptrs = (C.POINTER(C.c_double) * (T * D))()
