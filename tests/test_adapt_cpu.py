@@ -70,7 +70,7 @@ def test_rebuilt_plan_matches_oracle_after_adapt():
     table = asgkron.hash_table_sparse_nD(pde.levels, max_lev)
     mats = pde.term_mats(deg, construction_level=max_lev)  # rows for every level up to max_lev
     plan = asgkron.Plan.create(mats, table.idx1d(), deg)
-    f = np.random.default_rng(11).standard_normal(plan.dof) * np.repeat(np.linspace(0.01, 1.0, table.num_elems), 4)
+    f = np.random.default_rng(11).standard_normal(plan.dof) * np.repeat(np.linspace(1.0, 0.01, table.num_elems), 4)
     res = adapt(table, f, deg, max_lev, 0.6)
     assert res.added > 0 and res.removed.size > 0
     p2 = rebuild_plan(plan, res.table)
