@@ -52,6 +52,33 @@ def test_rk3_matches_gold_trajectory(dev, name, pdename, lev, deg, graph):
         assert rel2(f.cpu().numpy(), g) <= 1e-13, i
 
 
+@pytest.mark.parametrize("name,lev,deg,grid", [("continuity2_implicit_l2_d2", 2, 2, "SG"),
+                                               ("continuity2_implicit_l4_d3", 4, 3, "SG"),
+                                               ("continuity2_implicit_fg_l3_4_d3", [3, 4], 3, "FG")])
+@pytest.mark.parametrize("mixed", [True, False])
+def test_backward_euler_matches_gold_trajectory(dev, name, lev, deg, grid, mixed):
+    """5 backward-Euler steps at CFL 0.01 (source at t + dt) by GMRES + refinement on the GPU
+    reproduce the reference's direct-solve gold trajectories."""
+    import asgkron
+    from asgkron import pdes
+    from asgkron.steppers import be_step
+
+    pde = pdes.continuity2(lev, 0.0)
+    table = asgkron.hash_table_sparse_nD(pde.levels, 8, grid)
+    idx = table.idx1d()
+    plan = asgkron.Plan.create(pde.term_mats(deg, construction_level=8), idx, deg)
+    f = torch.from_numpy(pde.initial_condition(deg, idx)).to(dev)
+    dt = pde.dt(0.01)
+    gold = np.load(os.path.join(G, "time_advance.npz"))
+    for i in range(5):
+        s = torch.from_numpy(pde.source_vector(deg, idx, (i + 1) * dt)).to(dev)
+        f, info = be_step(plan, f, dt, source=s, mixed=mixed, tol=1e-13)
+        torch.cuda.synchronize()
+        assert info["converged"], (i, info)
+        g = gold["%s_t%d" % (name, i)]
+        assert rel2(f.cpu().numpy(), g) <= 1e-11, (i, info)
+
+
 def test_rk3_cfg1_lf_upwind_vs_oracle(dev):
     """The CPU-runnable configuration: continuity2 lev 4 deg 2 (current PDE file, LF = -1),
     5 RK3 steps at CFL 0.01: GPU FP64 vs the oracle's RK3; FP32 within 1e-6."""

@@ -205,6 +205,39 @@ def test_rk3_trajectory_gold(name, pdefn, lev, deg, grid):
     assert _replay(name, pdefn, lev, deg, grid) < 1e-14
 
 
+def _replay_be(name, pdefn, lev, deg, grid="SG"):
+    """Backward Euler (time_advance.m:267-349: (I - dt A) f1 = f0 + dt s(t + dt), direct
+    solve) from the projected initial condition, against the gold trajectory."""
+    pde = pdefn(lev, LF=0.0)
+    lev_vec = [d.lev for d in pde.dims]
+    max_lev = 4 if len(lev_vec) > 3 else 8
+    lv, cl, _ = O.hash_table_sparse_nd(lev_vec, max_lev, grid)
+    idx = O.element_idx1d(lv, cl)
+    _, blocks = O.operator_two_scale(deg, max_lev)
+    mats = O.build_term_mats(pde, deg, coeff_level=max_lev)
+    f = O.md_eval(pde, deg, pde.ic, idx, blocks, 0.0)
+    _, A = O.apply_A_loop(mats, idx, deg, f, build_A=True)
+    dt = pde.dt_fn(pde, 0.01)
+    ta = _npz("time_advance.npz")
+    worst = 0.0
+    for i in range(5):
+        f = O.backward_euler_step(A, f, dt, O.md_eval(pde, deg, pde.sources, idx, blocks, (i + 1) * dt))
+        g = ta["%s_t%d" % (name, i)]
+        worst = max(worst, np.linalg.norm(f - g) / np.linalg.norm(g))
+    return worst
+
+
+@pytest.mark.parametrize("name,pdefn,lev,deg,grid", [
+    ("continuity1_implicit_l2_d2", O.continuity1, 2, 2, "SG"),
+    ("continuity1_implicit_l4_d3", O.continuity1, 4, 3, "SG"),
+    ("continuity2_implicit_l2_d2", O.continuity2, 2, 2, "SG"),
+    ("continuity2_implicit_l4_d3", O.continuity2, 4, 3, "SG"),
+    ("continuity2_implicit_fg_l3_4_d3", O.continuity2, [3, 4], 3, "FG"),
+])
+def test_backward_euler_trajectory_gold(name, pdefn, lev, deg, grid):
+    assert _replay_be(name, pdefn, lev, deg, grid) < 1e-13
+
+
 def test_apply_A_loop_equals_vectorised_and_krond():
     """The faithful loop, the vectorised restatement and the assembled krond matrix agree
     (apply_A.m:170-201), with and without a connectivity list."""
