@@ -171,6 +171,7 @@ class PartialTerm:
         swap = {"D": "N", "N": "D"}
         self.bcl = swap.get(BCL, BCL) if kind == "grad" else BCL
         self.bcr = swap.get(BCR, BCR) if kind == "grad" else BCR
+        self.BCL, self.BCR = BCL, BCR  # as given: the boundary-data sides (boundary_condition_vector.m:57-60)
 
 
 def mass_term(g=None):
@@ -245,6 +246,29 @@ def realspace_matrix(deg, lo, hi, lev, pt):
         if pt.kind == "grad":
             M = -M.T
     return M
+
+
+def pterm_matrix(deg, lo, hi, lev, pt):
+    """One partial term in wavelet space, LHS mass solved: M \\ L (pterm_coeff_matrix.m:6-20)."""
+    F = fmwt_matrix(deg, lev)
+    Mw = F @ realspace_matrix(deg, lo, hi, lev, mass_term()) @ F.T
+    return np.linalg.solve(Mw, F @ realspace_matrix(deg, lo, hi, lev, pt) @ F.T)
+
+
+def boundary_trace(deg, lo, hi, lev, pt, fn, t, side):
+    """Wavelet coefficients of the boundary flux of a Dirichlet side (compute_boundary_condition.m
+    + apply_FMWT_blocks): -g(lo) f(lo) v(lo) on the first cell, +g(hi) f(hi) v(hi) on the last."""
+    N = 2 ** lev
+    h = (hi - lo) / N
+    c = np.zeros(deg * N)
+    x = np.array([lo if side == "L" else hi])
+    gval = float(np.asarray(pt.g(x)).reshape(-1)[0])
+    fval = float(np.asarray(fn(x, t)).reshape(-1)[0])
+    if side == "L":
+        c[:deg] = -gval * fval * legendre_values(-1.0, deg)[0] / np.sqrt(h)
+    else:
+        c[deg * (N - 1):] = gval * fval * legendre_values(1.0, deg)[0] / np.sqrt(h)
+    return fmwt_matrix(deg, lev) @ c
 
 
 def term_matrix(deg, lo, hi, lev, pterms):

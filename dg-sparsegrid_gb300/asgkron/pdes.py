@@ -7,11 +7,15 @@ Each follows the reference's pdes/*.m file it names: domains, per-dimension part
 import numpy as np
 
 from . import grid as _grid
-from .operators import combine_dimensions, div_term, grad_term, mass_term, project_1d, term_matrix
+from .operators import (boundary_trace, combine_dimensions, div_term, grad_term, mass_term, project_1d, pterm_matrix,
+                        term_matrix)
 
 
 class PDE:
-    def __init__(self, name, bounds, lev, terms, sources=(), ic=(), dt_rule=None):
+    """bc: separable Dirichlet boundary data [f_1(x, t), ..., f_d(x, t), c(t)] used on every
+    'D' side of every partial term (BCL_fList = BCR_fList, as the configurations' PDEs have it)."""
+
+    def __init__(self, name, bounds, lev, terms, sources=(), ic=(), dt_rule=None, bc=None):
         self.name = name
         self.bounds = list(bounds)
         d = len(self.bounds)
@@ -20,6 +24,7 @@ class PDE:
         self.sources = list(sources)
         self.ic = list(ic)
         self.dt_rule = dt_rule
+        self.bc = bc
 
     @property
     def num_dims(self):
@@ -77,6 +82,67 @@ class PDE:
     def initial_condition(self, deg, idx1d, t=0.0):
         return self._md(deg, self.ic, idx1d, t)
 
+    def boundary_parts(self, deg, idx1d, t=0.0):
+        """boundary_condition_vector.m:29-193 as (vectors, time factors): for every partial term
+        p of dimension d1 with a Dirichlet side, the d1 factor is the boundary flux passed
+        through d1's preceding partial terms; each other dimension d2 carries the projection of
+        its boundary function times the g of its own p-th partial term, passed through its
+        preceding partial terms (the LHS mass matrices are the identity for these terms).  The
+        spatial parts are evaluated at t; bc(t) = sum_k c_k(t) v_k."""
+        if self.bc is None:
+            return [], []
+        D = self.num_dims
+        vecs, facs = [], []
+        pm = {}
+
+        def pmat(d, tt, q):
+            key = (d, tt, q)
+            if key not in pm:
+                lo, hi = self.bounds[d]
+                pm[key] = pterm_matrix(deg, lo, hi, self.levels[d], self.terms[tt][d][q])
+            return pm[key]
+
+        for tt, term in enumerate(self.terms):
+            for d1 in range(D):
+                lo1, hi1 = self.bounds[d1]
+                for p, pt in enumerate(term[d1]):
+                    if pt.kind not in ("div", "grad"):
+                        continue
+                    for side, kind in (("L", pt.BCL), ("R", pt.BCR)):
+                        if kind != "D":
+                            continue
+                        parts = []
+                        for d2 in range(D):
+                            if d2 == d1:
+                                v = boundary_trace(deg, lo1, hi1, self.levels[d1], pt, self.bc[d1], t, side)
+                                for q in range(p - 1, -1, -1):
+                                    v = pmat(d1, tt, q) @ v
+                            else:
+                                lo2, hi2 = self.bounds[d2]
+                                g2 = term[d2][p].g
+                                f2 = self.bc[d2]
+                                v = project_1d(deg, self.levels[d2], lo2, hi2,
+                                               lambda x, tt_, f2=f2, g2=g2: f2(x, tt_) * g2(x), t)
+                                for q in range(p):
+                                    v = pmat(d2, tt, q) @ v
+                            parts.append(v)
+                        vecs.append(combine_dimensions(deg, parts, 1.0, idx1d))
+                        facs.append(self.bc[D])
+        return vecs, facs
+
+    def boundary_vector(self, deg, idx1d, t):
+        vecs, facs = self.boundary_parts(deg, idx1d, t)
+        out = np.zeros(idx1d.shape[0] * deg ** self.num_dims)
+        for v, c in zip(vecs, facs):
+            out += c(t) * v
+        return out
+
+    def forcing_parts(self, deg, idx1d):
+        """Sources and boundary data together (the rhs time_advance.m adds to A f each stage)."""
+        sv, sf = self.source_parts(deg, idx1d)
+        bv, bf = self.boundary_parts(deg, idx1d)
+        return sv + bv, sf + bf
+
 
 def _neg(v):
     return lambda x: 0 * x - v
@@ -124,12 +190,24 @@ def continuity6(lev, LF=-1.0):
                lambda p, cfl: (p.bounds[0][1] - p.bounds[0][0]) / 2 ** p.levels[0] * cfl)
 
 
-def diffusion2(lev):
-    """pdes/diffusion2.m: LDG d2/dx2 + d2/dy2 on [0,1]^2: DIV(+1, N, N) then GRAD(-1, D, D)."""
+def diffusion2(lev, case="zero_dirichlet"):
+    """pdes/diffusion2.m: LDG d2/dx2 + d2/dy2 on [0,1]^2: DIV(+1, N, N) then GRAD(-1, D, D).
+
+    case "reference": the reference file's data -- initial condition and Dirichlet data from
+    the solution cos(pi x) cos(pi y) exp(-2 pi^2 t) (diffusion2.m:41-55).
+    case "zero_dirichlet": the implicit benchmark configuration -- homogeneous Dirichlet data
+    and sin(pi x) sin(pi y) initially.  The operators are the same in both cases (they depend
+    on the boundary types only, coeff_matrix.m:212-263)."""
     one = lambda x: 0 * x + 1
     ldg = [div_term(one, 1.0, "N", "N"), grad_term(one, -1.0, "D", "D")]
     terms = [[ldg, [mass_term(), mass_term()]], [[mass_term(), mass_term()], ldg]]
     pi = np.pi
-    ic = [[lambda x, t: np.sin(pi * x), lambda y, t: np.sin(pi * y), lambda t: 1.0]]
+    if case == "reference":
+        soln = [lambda x, t: np.cos(pi * x), lambda y, t: np.cos(pi * y), lambda t: np.exp(-2 * pi ** 2 * t)]
+        ic, bc = [soln], soln
+    elif case == "zero_dirichlet":
+        ic, bc = [[lambda x, t: np.sin(pi * x), lambda y, t: np.sin(pi * y), lambda t: 1.0]], None
+    else:
+        raise ValueError("diffusion2: case must be 'reference' or 'zero_dirichlet'")
     return PDE("diffusion2", [(0.0, 1.0), (0.0, 1.0)], lev, terms, (), ic,
-               lambda p, cfl: cfl * (1.0 / 2 ** p.levels[0]) ** 2)
+               lambda p, cfl: cfl * (1.0 / 2 ** p.levels[0]) ** 2, bc=bc)

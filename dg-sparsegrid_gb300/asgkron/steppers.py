@@ -24,8 +24,9 @@ class RK3Stepper:
         self.torch_dtype = torch.float64 if dtype in ("float64", torch.float64) else torch.float32
         self.n = plan.dof
         dev = torch.device("cuda")
-        if source_parts is None and pde is not None and pde.sources:
-            source_parts, time_factors = pde.source_parts(plan.deg, np.asarray(idx1d))
+        if source_parts is None and pde is not None:
+            # sources and boundary data: both enter each stage as rhs (time_advance.m:158-190)
+            source_parts, time_factors = pde.forcing_parts(plan.deg, np.asarray(idx1d))
         self.tfac = list(time_factors or [])
         ns = len(self.tfac)
         self.ns = ns

@@ -982,10 +982,75 @@ def continuity6(lev, LF=-1.0):
 
 
 def diffusion2(lev):
-    """pdes/diffusion2.m:33-108: LDG d2/dx2 + d2/dy2 on [0,1]^2 (DIV(+1,N,N) then GRAD(-1,D,D))."""
+    """pdes/diffusion2.m:33-108: LDG d2/dx2 + d2/dy2 on [0,1]^2 (DIV(+1,N,N) then GRAD(-1,D,D)),
+    analytic solution cos(pi x) cos(pi y) exp(-2 pi^2 t) as initial and Dirichlet boundary
+    data (diffusion2.m:41-55)."""
+    pi = np.pi
     lv = [lev] * 2 if np.isscalar(lev) else list(lev)
     dims = [Dim(0.0, 1.0, lv[0]), Dim(0.0, 1.0, lv[1])]
     one = lambda x: 0 * x + 1
     ldg = [DIV(one, +1.0, "N", "N"), GRAD(one, -1.0, "D", "D")]
     terms = [[ldg, [MASS(), MASS()]], [[MASS(), MASS()], ldg]]
-    return PDESpec(dims, terms, [], [], lambda p, cfl: cfl * (1.0 / 2 ** p.dims[0].lev) ** 2)
+    soln = [lambda x, t: np.cos(pi * x), lambda y, t: np.cos(pi * y), lambda t: np.exp(-2 * pi ** 2 * t)]
+    spec = PDESpec(dims, terms, [], [soln], lambda p, cfl: cfl * (1.0 / 2 ** p.dims[0].lev) ** 2)
+    spec.bc = soln  # BCL = BCR = the solution (diffusion2.m:49-52)
+    return spec
+
+
+def compute_boundary_condition(g, lev, deg, lo, hi, fn, t, side):
+    """compute_boundary_condition.m:1-55 (dV = 1): the boundary trace -g f v|_lo on the first
+    cell or +g f v|_hi on the last, in the Legendre basis."""
+    n = 2 ** lev
+    h = (hi - lo) / n
+    bc = np.zeros(deg * n)
+    if side == "L":
+        p_L = lin_legendre(-1.0, deg)[0] / np.sqrt(h)
+        bc[:deg] = -float(g(np.array([lo]))[0]) * p_L * float(fn(np.array([lo]), t)[0])
+    else:
+        p_R = lin_legendre(1.0, deg)[0] / np.sqrt(h)
+        bc[deg * (n - 1):] = float(g(np.array([hi]))[0]) * p_R * float(fn(np.array([hi]), t)[0])
+    return bc
+
+
+def boundary_condition_vector(pde, deg, idx1d, blocks, t, coeff_level=None):
+    """boundary_condition_vector.m:1-197 for Dirichlet partial terms (dV = 1, so every LHS
+    mass matrix is the identity).  For partial term p of dimension d1 with a 'D' side: the
+    other dimensions carry the projection of the boundary function times the p-th partial
+    term's g of that dimension, passed through that dimension's preceding partial terms; d1
+    carries the FMWT of the boundary trace passed through d1's preceding partial terms;
+    combine_dimensions_D then forms the Kronecker product on the element table, scaled by the
+    boundary function's time factor."""
+    D = len(pde.dims)
+    out = np.zeros(idx1d.shape[0] * deg ** D)
+    lv = [d.lev if coeff_level is None else coeff_level for d in pde.dims]
+    pmats = [[[pterm_matrix(deg, pde.dims[d], pt, lv[d]) for pt in pde.terms[tt][d]] for d in range(D)]
+             for tt in range(len(pde.terms))]
+    for tt, term in enumerate(pde.terms):
+        for d1 in range(D):
+            dim = pde.dims[d1]
+            dof = deg * 2 ** dim.lev
+            for p, pt in enumerate(term[d1]):
+                if pt.type not in ("grad", "div"):
+                    continue
+                for side, kind in (("L", pt.BCL), ("R", pt.BCR)):
+                    if kind != "D":
+                        continue
+                    fl = []
+                    for d2 in range(D):
+                        oth = term[d2]
+                        n2 = deg * 2 ** pde.dims[d2].lev
+                        if d2 == d1:
+                            v = compute_boundary_condition(pt.g, dim.lev, deg, dim.min, dim.max, pde.bc[d1], t, side)
+                            v = apply_fmwt_blocks(dim.lev, blocks, v, "LN")
+                            for q in range(p - 1, -1, -1):
+                                v = pmats[tt][d1][q][:dof, :dof] @ v
+                        else:
+                            mp = oth[p]
+                            fn = (lambda f2, g2: (lambda x, tt_: f2(x, tt_) * g2(x)))(pde.bc[d2], mp.g)
+                            v = forward_wavelet_transform(deg, pde.dims[d2].lev, pde.dims[d2].min, pde.dims[d2].max,
+                                                          fn, blocks, t)
+                            for q in range(p):
+                                v = pmats[tt][d2][q][:n2, :n2] @ v
+                        fl.append(v)
+                    out += combine_dimensions(deg, fl, pde.bc[D](t), idx1d)
+    return out

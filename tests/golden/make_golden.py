@@ -14,7 +14,7 @@ once, in the container that has the reference checked out, and packs the subset 
 * ``permutations.npz``    -- ``gold/generated-inputs/permutations/*`` (``gold/gold_permute.m``)
 * ``quadrature.npz``      -- ``gold/generated-inputs/quadrature/*`` (``gold/gold_quadrature.m``)
 * ``transformations.npz`` -- ``operator_two_scale_*.dat``, ``multiwavelet_*.dat``, ``combine_dim_*.dat``
-* ``time_advance.npz``    -- RK3 and backward-Euler trajectories ``continuity{1,2,3}_*_t{0..4}.dat``
+* ``time_advance.npz``    -- RK3 and backward-Euler trajectories ``continuity{1,2,3}_*``, ``diffusion2_*`` ``_t{0..4}.dat``
                              (``gold/gold_time_advance.m:252-364``)
 
 Run:  python tests/golden/make_golden.py [reference_root]
@@ -99,7 +99,11 @@ def main(ref_root):
                  "continuity3_sg_l2_d2", "continuity3_sg_l4_d3",
                  # backward Euler (gold/gold_time_advance.m:156-173, 237-240)
                  "continuity1_implicit_l2_d2", "continuity1_implicit_l4_d3", "continuity2_implicit_l2_d2",
-                 "continuity2_implicit_l4_d3", "continuity2_implicit_fg_l3_4_d3"):
+                 "continuity2_implicit_l4_d3", "continuity2_implicit_fg_l3_4_d3",
+                 # LDG diffusion with inhomogeneous Dirichlet data (gold_time_advance.m:40-51, 179-193, 203-234)
+                 "diffusion2_sg_l2_d2", "diffusion2_sg_l3_d3", "diffusion2_sg_l4_d4", "diffusion2_sg_l4_5_d2",
+                 "diffusion2_implicit_sg_l3_d3", "diffusion2_implicit_sg_l4_d3", "diffusion2_implicit_sg_l5_d3",
+                 "diffusion2_implicit_sg_l4_5_d2"):
         for t in range(5):
             path = os.path.join(gold, "time_advance", "%s_t%d.dat" % (stem, t))
             out["%s_t%d" % (stem, t)] = read_octave_text(path).reshape(-1)

@@ -79,6 +79,36 @@ def test_backward_euler_matches_gold_trajectory(dev, name, lev, deg, grid, mixed
         assert rel2(f.cpu().numpy(), g) <= 1e-11, (i, info)
 
 
+@pytest.mark.parametrize("name,lev,deg,method", [("diffusion2_sg_l3_d3", 3, 3, "RK3"),
+                                                 ("diffusion2_sg_l4_5_d2", [4, 5], 2, "RK3"),
+                                                 ("diffusion2_implicit_sg_l4_d3", 4, 3, "BE"),
+                                                 ("diffusion2_implicit_sg_l4_5_d2", [4, 5], 2, "BE")])
+def test_diffusion2_matches_gold_trajectory(dev, name, lev, deg, method):
+    """diffusion2.m with its Dirichlet data on the GPU: LDG operators, the boundary vector as
+    rhs (RK3 stages on the device from its spatial parts; BE at t + dt), against the gold."""
+    import asgkron
+    from asgkron import pdes
+    from asgkron.steppers import RK3Stepper, be_step
+
+    pde = pdes.diffusion2(lev, case="reference")
+    idx = asgkron.hash_table_sparse_nD(pde.levels, 8).idx1d()
+    plan = asgkron.Plan.create(pde.term_mats(deg), idx, deg)
+    f = torch.from_numpy(pde.initial_condition(deg, idx)).to(dev)
+    dt = pde.dt(0.01)
+    gold = np.load(os.path.join(G, "time_advance.npz"))
+    st = RK3Stepper(plan, pde, idx) if method == "RK3" else None
+    for i in range(5):
+        if method == "RK3":
+            st.step(f, i * dt, dt)
+        else:
+            bc = torch.from_numpy(pde.boundary_vector(deg, idx, (i + 1) * dt)).to(dev)
+            f, info = be_step(plan, f, dt, source=bc, mixed=True, tol=1e-13)
+            assert info["converged"], (i, info)
+        torch.cuda.synchronize()
+        g = gold["%s_t%d" % (name, i)]
+        assert rel2(f.cpu().numpy(), g) <= 1e-11, i
+
+
 def test_rk3_cfg1_lf_upwind_vs_oracle(dev):
     """The CPU-runnable configuration: continuity2 lev 4 deg 2 (current PDE file, LF = -1),
     5 RK3 steps at CFL 0.01: GPU FP64 vs the oracle's RK3; FP32 within 1e-6."""

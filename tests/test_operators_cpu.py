@@ -57,3 +57,18 @@ def test_projection_matches_oracle():
         a = prod.source_vector(3, idx, tt)
         b = O.md_eval(orac, 3, orac.sources, idx.astype(np.int64), blocks, tt)
         np.testing.assert_allclose(a, b, rtol=0, atol=1e-13 * np.abs(b).max())
+
+
+@pytest.mark.parametrize("lev,deg", [(2, 2), (3, 3), ([4, 5], 2), (4, 4)])
+def test_boundary_vector_matches_oracle(lev, deg):
+    """boundary_condition_vector.m for diffusion2's Dirichlet data: product vs oracle."""
+    import asgkron
+    from asgkron import pdes
+
+    pde = pdes.diffusion2(lev, case="reference")
+    idx = asgkron.hash_table_sparse_nD(pde.levels, 8).idx1d()
+    _, blocks = O.operator_two_scale(deg, 8)
+    for t in (0.0, 0.0137):
+        got = pde.boundary_vector(deg, idx, t)
+        want = O.boundary_condition_vector(O.diffusion2(lev), deg, idx.astype(np.int64), blocks, t)
+        assert np.linalg.norm(got - want) <= 1e-14 * np.linalg.norm(want)
