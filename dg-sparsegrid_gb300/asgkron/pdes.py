@@ -182,11 +182,33 @@ def continuity3(lev, LF=-1.0):
 
 
 def continuity6(lev, LF=-1.0):
-    """pdes/continuity6.m: six dimensions, d/dx_k with speeds (1,1,3,4,3,2), periodic."""
+    """pdes/continuity6.m: six dimensions, d/dx_k with speeds (1,1,3,4,3,2), periodic; the
+    manufactured solution cos(pi x) sin(pi y/2) cos(pi z/3) cos(pi vx/10) sin(pi vy/20)
+    cos(pi vz/30) sin(2t) gives seven separable sources (continuity6.m:142-221), zero start."""
     bounds = [(-1.0, 1.0), (-2.0, 2.0), (-3.0, 3.0), (-10.0, 10.0), (-20.0, 20.0), (-30.0, 30.0)]
     speeds = [1.0, 1.0, 3.0, 4.0, 3.0, 2.0]
     terms = [[[div_term(_neg(speeds[k]), LF, "P", "P")] if k == d else None for d in range(6)] for k in range(6)]
-    return PDE("continuity6", bounds, lev, terms, (), (),
+    pi = np.pi
+    freq = [pi, pi / 2, pi / 3, pi / 10, pi / 20, pi / 30]
+    sol_is_cos = [True, False, True, True, False, True]
+
+    def factors(swap):  # the solution's spatial factors, dimension ``swap`` cos <-> sin
+        out = []
+        for k in range(6):
+            use_cos = sol_is_cos[k] != (k == swap)
+            out.append((lambda a: (lambda x, t: np.cos(a * x)))(freq[k]) if use_cos else
+                       (lambda a: (lambda x, t: np.sin(a * x)))(freq[k]))
+        return out
+
+    sources = [factors(-1) + [lambda t: 2 * np.cos(2 * t)],
+               factors(1) + [lambda t: 0.5 * pi * np.sin(2 * t)],
+               factors(0) + [lambda t: -pi * np.sin(2 * t)],
+               factors(2) + [lambda t: -pi * np.sin(2 * t)],
+               factors(4) + [lambda t: 3.0 / 20.0 * pi * np.sin(2 * t)],
+               factors(3) + [lambda t: -2.0 / 5.0 * pi * np.sin(2 * t)],
+               factors(5) + [lambda t: -1.0 / 15.0 * pi * np.sin(2 * t)]]
+    ic = [[lambda x, t: 0 * x] * 6 + [lambda t: 1.0]]
+    return PDE("continuity6", bounds, lev, terms, sources, ic,
                lambda p, cfl: (p.bounds[0][1] - p.bounds[0][0]) / 2 ** p.levels[0] * cfl)
 
 

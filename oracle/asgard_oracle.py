@@ -968,7 +968,8 @@ def continuity3(lev, LF=-1.0):
 
 
 def continuity6(lev, LF=-1.0):
-    """pdes/continuity6.m:28-130 (terms only; sources are not needed for apply_A)."""
+    """pdes/continuity6.m:28-221: six advection terms, the seven separable sources, zero
+    initial condition."""
     lv = [lev] * 6 if np.isscalar(lev) else list(lev)
     bounds = [(-1.0, 1.0), (-2.0, 2.0), (-3.0, 3.0), (-10.0, 10.0), (-20.0, 20.0), (-30.0, 30.0)]
     dims = [Dim(lo, hi, l) for (lo, hi), l in zip(bounds, lv)]
@@ -978,7 +979,25 @@ def continuity6(lev, LF=-1.0):
         row = [None] * 6
         row[k] = [DIV((lambda s: (lambda x: 0 * x - s))(speeds[k]), LF, "P", "P")]
         terms.append(row)
-    return PDESpec(dims, terms, [], [], lambda p, cfl: (p.dims[0].max - p.dims[0].min) / 2 ** p.dims[0].lev * cfl)
+    pi = np.pi
+    args = [pi, pi / 2, pi / 3, pi / 10, pi / 20, pi / 30]
+    cos_ = lambda a: (lambda x, t: np.cos(a * x))
+    sin_ = lambda a: (lambda x, t: np.sin(a * x))
+    base = ["c", "s", "c", "c", "s", "c"]  # the solution's factors (continuity6.m:214-221)
+
+    def src(flip, tf):  # the solution's factors with dimension ``flip`` differentiated
+        fs = []
+        for k in range(6):
+            kind = base[k] if k != flip else ("s" if base[k] == "c" else "c")
+            fs.append(cos_(args[k]) if kind == "c" else sin_(args[k]))
+        return fs + [tf]
+
+    sources = [src(-1, lambda t: 2 * np.cos(2 * t)), src(1, lambda t: 0.5 * pi * np.sin(2 * t)),
+               src(0, lambda t: -pi * np.sin(2 * t)), src(2, lambda t: -pi * np.sin(2 * t)),
+               src(4, lambda t: 3 / 20 * pi * np.sin(2 * t)), src(3, lambda t: -2 / 5 * pi * np.sin(2 * t)),
+               src(5, lambda t: -1 / 15 * pi * np.sin(2 * t))]
+    ic = [[(lambda x, t: 0 * x)] * 6 + [lambda t: 1.0]]
+    return PDESpec(dims, terms, sources, ic, lambda p, cfl: (p.dims[0].max - p.dims[0].min) / 2 ** p.dims[0].lev * cfl)
 
 
 def diffusion2(lev):

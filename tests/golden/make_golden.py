@@ -14,7 +14,7 @@ once, in the container that has the reference checked out, and packs the subset 
 * ``permutations.npz``    -- ``gold/generated-inputs/permutations/*`` (``gold/gold_permute.m``)
 * ``quadrature.npz``      -- ``gold/generated-inputs/quadrature/*`` (``gold/gold_quadrature.m``)
 * ``transformations.npz`` -- ``operator_two_scale_*.dat``, ``multiwavelet_*.dat``, ``combine_dim_*.dat``
-* ``time_advance.npz``    -- RK3 and backward-Euler trajectories ``continuity{1,2,3}_*``, ``diffusion2_*`` ``_t{0..4}.dat``
+* ``time_advance.npz``    -- RK3 and backward-Euler trajectories ``continuity{1,2,3,6}_*``, ``diffusion2_*`` ``_t{0..4}.dat``
                              (``gold/gold_time_advance.m:252-364``)
 
 Run:  python tests/golden/make_golden.py [reference_root]
@@ -97,6 +97,7 @@ def main(ref_root):
     for stem in ("continuity1_sg_l2_d2", "continuity1_sg_l4_d3", "continuity1_fg_l2_d2",
                  "continuity2_sg_l2_d2", "continuity2_sg_l4_d3", "continuity2_fg_l2_d2",
                  "continuity3_sg_l2_d2", "continuity3_sg_l4_d3",
+                 "continuity6_sg_l2_d2", "continuity6_sg_l2_d3", "continuity6_sg_l2_3_2_3_3_2_d2",
                  # backward Euler (gold/gold_time_advance.m:156-173, 237-240)
                  "continuity1_implicit_l2_d2", "continuity1_implicit_l4_d3", "continuity2_implicit_l2_d2",
                  "continuity2_implicit_l4_d3", "continuity2_implicit_fg_l3_4_d3",

@@ -79,6 +79,31 @@ def test_backward_euler_matches_gold_trajectory(dev, name, lev, deg, grid, mixed
         assert rel2(f.cpu().numpy(), g) <= 1e-11, (i, info)
 
 
+@pytest.mark.parametrize("name,lev,deg", [("continuity6_sg_l2_d3", 2, 3),
+                                          ("continuity6_sg_l2_3_2_3_3_2_d2", [2, 3, 2, 3, 3, 2], 2)])
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_rk3_continuity6_matches_gold_trajectory(dev, name, lev, deg, dtype):
+    """continuity6 (the six-dimensional configuration's PDE, with its seven sources): 5 RK3
+    steps on the GPU against gold/generated-inputs/time_advance (max_lev 4 for d > 3)."""
+    import asgkron
+    from asgkron import pdes
+    from asgkron.steppers import RK3Stepper
+
+    pde = pdes.continuity6(lev, 0.0)
+    idx = asgkron.hash_table_sparse_nD(pde.levels, 4).idx1d()
+    plan = asgkron.Plan.create(pde.term_mats(deg, construction_level=4), idx, deg)
+    st = RK3Stepper(plan, pde, idx, dtype=dtype)
+    tdt = torch.float64 if dtype == "float64" else torch.float32
+    f = torch.from_numpy(pde.initial_condition(deg, idx)).to(dev, tdt)
+    dt = pde.dt(0.01)
+    gold = np.load(os.path.join(G, "time_advance.npz"))
+    for i in range(5):
+        st.step(f, i * dt, dt)
+        torch.cuda.synchronize()
+        g = gold["%s_t%d" % (name, i)]
+        assert rel2(f.double().cpu().numpy(), g) <= (1e-13 if dtype == "float64" else 1e-6), i
+
+
 @pytest.mark.parametrize("name,lev,deg,method", [("diffusion2_sg_l3_d3", 3, 3, "RK3"),
                                                  ("diffusion2_sg_l4_5_d2", [4, 5], 2, "RK3"),
                                                  ("diffusion2_implicit_sg_l4_d3", 4, 3, "BE"),
