@@ -37,7 +37,8 @@ class RK3Stepper:
         self.src64 = [torch.zeros(self.n, dtype=torch.float64, device=dev) for _ in range(3)]
         self.src = self.src64 if self.torch_dtype == torch.float64 else [
             torch.zeros(self.n, dtype=torch.float32, device=dev) for _ in range(3)]
-        self.work = torch.empty(4 * self.n, dtype=self.torch_dtype, device=dev)
+        per = 16 // (8 if self.torch_dtype == torch.float64 else 4)  # values per 16 bytes
+        self.work = torch.empty(4 * ((self.n + per - 1) // per * per), dtype=self.torch_dtype, device=dev)
         self.graph = None
         self._f_static = None
 

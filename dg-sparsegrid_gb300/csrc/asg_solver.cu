@@ -287,6 +287,10 @@ struct GmresLayout {
   size_t v, w, r, ax64, axmv, h, y, partial, hcol, hh, cs, sn, g, state, total;
 };
 
+// Leading dimension of the Krylov basis: every basis vector starts on a 32-byte boundary (the
+// operator application reads it with 16-byte loads, in either precision).
+long long basis_ld(long long n) { return (n + 3) / 4 * 4; }
+
 GmresLayout gmres_layout(long long n, int m, bool mixed) {
   GmresLayout L{};
   size_t off = 0;
@@ -295,7 +299,7 @@ GmresLayout gmres_layout(long long n, int m, bool mixed) {
     off += align256(bytes);
     return o;
   };
-  L.v = take(static_cast<size_t>(m + 1) * n * (mixed ? sizeof(float) : sizeof(double)));
+  L.v = take(static_cast<size_t>(m + 1) * basis_ld(n) * (mixed ? sizeof(float) : sizeof(double)));
   L.w = take(n * sizeof(double));
   L.r = take(n * sizeof(double));
   L.ax64 = take(n * sizeof(double));
@@ -333,6 +337,7 @@ template <typename TV>
 asg_status gmres_cycle(asg_plan* plan, long long n, double dt, const double* r0, double* x64, int m, double rtol_abs,
                        unsigned char* base, const GmresLayout& L, cudaStream_t s, int* iters, double* resid) {
   TV* V = reinterpret_cast<TV*>(base + L.v);
+  const long long ldv = basis_ld(n);
   double* w = reinterpret_cast<double*>(base + L.w);
   TV* axmv = reinterpret_cast<TV*>(base + L.axmv);
   double* h_dev = reinterpret_cast<double*>(base + L.h);
@@ -366,20 +371,20 @@ asg_status gmres_cycle(asg_plan* plan, long long n, double dt, const double* r0,
   for (int j0 = 0; j0 < m; j0 += kChunk) {
     for (int j = j0; j < std::min(m, j0 + kChunk); ++j) {
       // w = V_j - dt * A V_j
-      asg_status ast = sizeof(TV) == 4 ? asg_apply_f32(plan, reinterpret_cast<const float*>(V + j * n),
+      asg_status ast = sizeof(TV) == 4 ? asg_apply_f32(plan, reinterpret_cast<const float*>(V + j * ldv),
                                                        reinterpret_cast<float*>(axmv), s)
-                                       : asg_apply_f64(plan, reinterpret_cast<const double*>(V + j * n),
+                                       : asg_apply_f64(plan, reinterpret_cast<const double*>(V + j * ldv),
                                                        reinterpret_cast<double*>(axmv), s);
       if (ast) return ast;
-      asg::k_shift_g<TV><<<gr, 256, 0, s>>>(n, dt, V + j * n, axmv, w, state);
+      asg::k_shift_g<TV><<<gr, 256, 0, s>>>(n, dt, V + j * ldv, axmv, w, state);
       for (int pass = 0; pass < 2; ++pass) {  // classical Gram-Schmidt, reorthogonalised (FP64)
-        asg::k_dots_g<TV><<<dim3(nb, j + 1), asg::kRedThreads, 0, s>>>(n, w, V, n, partial, state);
+        asg::k_dots_g<TV><<<dim3(nb, j + 1), asg::kRedThreads, 0, s>>>(n, w, V, ldv, partial, state);
         asg::k_dots_final_g<<<j + 1, 32, 0, s>>>(j + 1, nb, partial, h_dev, hcol, pass, state);
-        asg::k_orth_update_g<TV><<<gr, 256, 0, s>>>(n, j + 1, h_dev, V, n, w, state);
+        asg::k_orth_update_g<TV><<<gr, 256, 0, s>>>(n, j + 1, h_dev, V, ldv, w, state);
       }
       asg::k_norm2_g<<<nb, asg::kRedThreads, 0, s>>>(n, w, partial, state);
       asg::k_givens<<<1, 32, 0, s>>>(j, m, rtol_abs, nb, partial, hcol, H, cs, sn, g, state);
-      asg::k_store_basis_g<TV><<<gr, 256, 0, s>>>(n, w, V + (j + 1) * n, state);
+      asg::k_store_basis_g<TV><<<gr, 256, 0, s>>>(n, w, V + (j + 1) * ldv, state);
     }
     ASG_CUDA(cudaMemcpyAsync(&hs, state, sizeof(hs), cudaMemcpyDeviceToHost, s));
     ASG_CUDA(cudaStreamSynchronize(s));
@@ -387,7 +392,7 @@ asg_status gmres_cycle(asg_plan* plan, long long n, double dt, const double* r0,
   }
   // back substitution H y = g and x += V y (FP64 update), on the device
   asg::k_backsolve<<<1, 256, 0, s>>>(m, H, g, y_dev, state);
-  asg::k_sol_update_g<TV><<<gr, 256, 0, s>>>(n, y_dev, V, n, x64, state);
+  asg::k_sol_update_g<TV><<<gr, 256, 0, s>>>(n, y_dev, V, ldv, x64, state);
   *iters = hs.kdone;
   *resid = hs.resid;
   cudaError_t e = cudaGetLastError();
@@ -448,13 +453,16 @@ asg_status rk3(asg_plan* p, T* f, double dt, const T* const* src, T* work, size_
   asg_plan_stats st{};
   asg_plan_stats_get(p, &st);
   const long long n = st.dof;
-  if (work_bytes < static_cast<size_t>(4 * n) * sizeof(T))
-    return fail(ASG_ERR_CAPACITY, "rk3_step: workspace needs %lld bytes", 4 * n * (long long)sizeof(T));
+  // four vectors, each starting on a 16-byte boundary (the operator application needs it)
+  const long long per = 16 / static_cast<long long>(sizeof(T));
+  const long long np = (n + per - 1) / per * per;
+  if (work_bytes < static_cast<size_t>(4 * np) * sizeof(T))
+    return fail(ASG_ERR_CAPACITY, "rk3_step: workspace needs %lld bytes", 4 * np * (long long)sizeof(T));
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   T* k1 = work;
-  T* k2 = work + n;
-  T* k3 = work + 2 * n;
-  T* y = work + 3 * n;
+  T* k2 = work + np;
+  T* k3 = work + 2 * np;
+  T* y = work + 3 * np;
   auto apply = [&](const T* in, T* out) {
     return sizeof(T) == 8 ? asg_apply_f64(p, reinterpret_cast<const double*>(in), reinterpret_cast<double*>(out), s)
                           : asg_apply_f32(p, reinterpret_cast<const float*>(in), reinterpret_cast<float*>(out), s);

@@ -73,7 +73,7 @@ typedef struct {
   double flops_reference;      /* num_pairs * T * d * 2 * deg^(d+1): the reference's work */
   double flops_executed;       /* flops of the executed work model */
   long long op_bytes_f64;      /* packed operator bytes on the device (FP64 copy) */
-  int kernel_kind;             /* 0 warp chain, 1 CTA chain, 2-5 single-mode fiber kernels */
+  int kernel_kind;             /* 0 warp chain, 1 CTA chain, 2-6 single-mode fiber kernels */
   int active_modes_max;        /* max over terms of non-identity factors */
 } asg_plan_stats;
 
@@ -101,7 +101,9 @@ asg_status asg_plan_update_ops(asg_plan* plan, const double* const* ops, const i
  * 2 single-mode fiber kernel with direct loads, 3 single-mode fiber kernel with TMA bulk
  * copies (4 stages, 2 CTAs per SM), 4 the same with 3 stages, the FP32 compensation tile in
  * shared memory and 3 CTAs per SM, 5 the kind-3 pipeline in persistent CTAs that each walk
- * a balanced list of rows (2-5 need one non-identity factor per term; 3-5 need deg 4, d 6).
+ * a balanced list of rows, 6 the small-block single-mode kernel (deg^d <= 256; grouped lanes
+ * per row, no shared-memory staging) (2-6 need one non-identity factor per term; 3-5 need
+ * deg 4, d 6).
  * The default is chosen by asg_plan_create; this exists for testing one family against
  * another and for launch-shape tuning. */
 asg_status asg_plan_set_kernel(asg_plan* plan, int kind);
@@ -186,8 +188,9 @@ asg_status asg_batch_info(const asg_batch* batch, int* warps_per_cta, int* rows_
 /* One RK3 step f <- f + dt (k1/6 + 2 k2/3 + k3/6), k_s = A y_s + src_s (RungeKutta3,
  * time_advance.m:151-204, without LHS mass or boundary vectors).  d_src: host array of the
  * three device source vectors at t, t+dt/2, t+dt (NULL array or entries = zero sources).
- * d_work: device workspace of 4*dof values.  Asynchronous, allocation-free, capturable into a
- * CUDA graph. */
+ * d_work: 16-byte aligned device workspace of 4 * round_up(dof, 16 / sizeof(value)) values
+ * (four vectors, each on a 16-byte boundary).  Asynchronous, allocation-free, capturable into
+ * a CUDA graph. */
 asg_status asg_rk3_step_f64(asg_plan* plan, double* d_f, double dt, const double* const* d_src, double* d_work,
                             size_t work_bytes, void* stream);
 asg_status asg_rk3_step_f32(asg_plan* plan, float* d_f, double dt, const float* const* d_src, float* d_work,

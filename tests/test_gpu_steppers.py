@@ -134,6 +134,29 @@ def test_diffusion2_matches_gold_trajectory(dev, name, lev, deg, method):
         assert rel2(f.cpu().numpy(), g) <= 1e-11, i
 
 
+@pytest.mark.parametrize("mixed", [True, False])
+def test_be_odd_block_size_vs_direct(dev, mixed):
+    """deg 3 in 3-D (27-value blocks, so dof is not a multiple of 4): the Krylov basis vectors
+    keep their 16-byte alignment; (I - dt A) x = b against a dense direct solve."""
+    import asgkron
+    from asgkron import pdes
+    from asgkron.steppers import be_step
+
+    pde = pdes.continuity3(3)
+    idx = asgkron.hash_table_sparse_nD(pde.levels, 8).idx1d()
+    mats = pde.term_mats(3)
+    plan = asgkron.Plan.create(mats, idx, 3)
+    assert plan.dof % 4 != 0
+    f0 = np.random.default_rng(12).standard_normal(plan.dof)
+    dt = 0.05
+    _, A = O.apply_A_loop(mats, idx.astype(np.int64), 3, f0, build_A=True)
+    want = O.backward_euler_step(A, f0, dt, np.zeros_like(f0))
+    x, info = be_step(plan, torch.from_numpy(f0).to(dev), dt, mixed=mixed, tol=1e-12)
+    torch.cuda.synchronize()
+    assert info["converged"]
+    assert rel2(x.cpu().numpy(), want) <= 1e-10
+
+
 def test_rk3_cfg1_lf_upwind_vs_oracle(dev):
     """The CPU-runnable configuration: continuity2 lev 4 deg 2 (current PDE file, LF = -1),
     5 RK3 steps at CFL 0.01: GPU FP64 vs the oracle's RK3; FP32 within 1e-6."""
