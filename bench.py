@@ -46,6 +46,10 @@ def parse_args():
     ap.add_argument("--skip-variants", action="store_true")
     ap.add_argument("--workload", default="continuity6", choices=["continuity6", "batched"],
                     help="batched: the 256-problem persistent-launch configuration (own JSON line)")
+    ap.add_argument("--batch-problems", type=int, default=256,
+                    help="batched workload: number of problems drawn (the configuration has 256)")
+    ap.add_argument("--batch-max-level", type=int, default=7,
+                    help="batched workload: highest SG level drawn (the configuration has 7)")
     return ap.parse_args()
 
 
@@ -360,7 +364,7 @@ def run_batched(args, rank, local):
     degree ~ U{2..4} (seed 3), d terms of dense N(0, 1/deg) 1-D operators (no structure, so
     every (pair, term) of all N^2 pairs is executed: the reference work model), f ~ N(0,1).
     One step = one persistent launch over all problems (FP32, tuned, replayed from a CUDA
-    graph).  Baseline: 256 sequential FP64 single-problem launches.  The inputs (62 MB of f,
+    graph).  Baseline: the same problems as sequential FP64 single-problem launches.  The inputs (62 MB of f,
     6.3 GB of work lists) exceed L2, so no flush is needed."""
     import numpy as np
     import torch
@@ -375,9 +379,9 @@ def run_batched(args, rank, local):
     rng = np.random.default_rng(3)
     plans, f64s = [], []
     flops = 0.0
-    for _ in range(256):
+    for _ in range(args.batch_problems):
         d = int(rng.choice([2, 3, 4]))
-        lev = int(rng.integers(3, 8))
+        lev = int(rng.integers(3, args.batch_max_level + 1))
         deg = int(rng.integers(2, 5))
         idx = asgkron.hash_table_sparse_nD([lev] * d, 8).idx1d()
         n = deg * 2 ** lev
@@ -439,11 +443,12 @@ def run_batched(args, rank, local):
         "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (dense N(0,1/deg) operators, f ~ N(0,1), seed 3)",
-        "config": {"workload": "batched: 256 problems, d in {2,3,4}, SG lev 3..7, deg 2..4, all pairs",
+        "config": {"workload": "batched: %d problems, d in {2,3,4}, SG lev 3..%d, deg 2..4, all pairs"
+                               % (args.batch_problems, args.batch_max_level),
                    "dof": dof, "flops_per_step": flops, "l2": "inputs larger than L2 (6.3 GB work lists)",
                    "launch": "one persistent launch replayed from a CUDA graph", "tuned": info},
         "compute": {"gflops_per_s": flops / (ms * 1e-3) / 1e9},
-        "variants": {"fp64_sequential_256_launches": {"ms": ms64, "value": dof / (ms64 * 1e-3) / 1e9,
+        "variants": {"fp64_sequential_launches": {"count": len(plans), "ms": ms64, "value": dof / (ms64 * 1e-3) / 1e9,
                                                        "gflops_per_s": flops / (ms64 * 1e-3) / 1e9},
                      "speedup_vs_fp64_sequential": ms64 / ms,
                      "fp32_rel_err_vs_fp64": {"max": max(errs), "median": statistics.median(errs)}},
