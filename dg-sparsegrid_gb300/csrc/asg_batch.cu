@@ -4,7 +4,8 @@
 // packed work list holds (problem, first row) items of `rows_per_item` rows, sorted by
 // descending cost (chain flops); persistent warps take items from a device counter (reset
 // by a memset in the same stream, so the launch is graph-capturable) and run the warp chain
-// algorithm of the single-problem kernel for each row, dispatching on the problem's degree.
+// algorithm of the single-problem kernel for each row, dispatching on the problem's degree,
+// with the next entry's operands prefetched by asynchronous copies.
 // Each row is still computed by one warp in a fixed order: results do not depend on which
 // warp took the item.  A tuner times (warps per CTA, rows per item) candidates.
 #include <algorithm>
@@ -27,7 +28,7 @@ struct BatchProblem {
   const long long* row_ptr;
   const int* ent;
   const unsigned* active;
-  int N, D, B, P;
+  int N, D, B, P, T;
   int stride[kMaxDims];
 };
 
@@ -36,42 +37,109 @@ struct BatchItem {
   int row;
 };
 
+// Asynchronous 4- or 8-byte global -> shared copy (cp.async, completion tracked per thread by
+// commit/wait groups).
 template <typename T>
-__device__ __forceinline__ void team_copy_w(T* dst, const T* src, int n, int lane) {
-  for (int k = lane; k < n; k += 32) dst[k] = src[k];
+__device__ __forceinline__ void cp_async_elem(T* dst, const T* src) {
+  const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
+  if constexpr (sizeof(T) == 8)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
+// Per-warp shared memory of the row kernel: the row's block-base table (8-byte entries), then
+// in elements of T two stages of (column block), two chain buffers and two stages of factor
+// blocks.
+constexpr int kStageVals = 256;           // one element block (deg^d <= 256)
+constexpr int kAmatVals = kMaxDims * 16;  // every factor block of one entry (deg <= 4)
+constexpr int kWarpVals = 2 * kStageVals + 2 * kStageVals + 2 * kAmatVals;
+template <typename T>
+__host__ __device__ constexpr size_t warp_smem_bytes() {
+  return kMaxTerms * kMaxDims * sizeof(long long) + kWarpVals * sizeof(T);
 }
 
+// One row of a problem, computed by one warp: for each work entry (column j, term t) the
+// column's block goes through the term's mode-product chain (fastest dimension first,
+// kronmult method 1, identity factors skipped) and is added to the row's accumulators
+// (Kahan-compensated in FP32), entries in list order -- the single-plan warp chain kernel's
+// arithmetic, so results equal it bitwise.  Entries are software-pipelined: while entry q is
+// computed, the warp's asynchronous copies bring entry q+1's column block and all its factor
+// blocks into the other shared-memory stage, so the global-memory latency of an entry is
+// paid once instead of once per mode and overlaps the previous entry's arithmetic.  The row's
+// per-(term, dimension) block bases sit in a shared table; for deg 2 and 4 the fiber indexing
+// uses shifts instead of divisions.
 template <typename T, int P>
-__device__ __forceinline__ void warp_row(const BatchProblem& pb, int row, T* buf0, T* buf1, int lane) {
+__device__ __forceinline__ void warp_row(const BatchProblem& pb, int row, unsigned char* wsm, int lane) {
   constexpr int MAXE = 8;
   constexpr bool KAHAN = sizeof(T) == 4;
+  constexpr int LG = P == 2 ? 1 : (P == 4 ? 2 : 0);  // log2(P) when P is a power of two
+  long long* abase = reinterpret_cast<long long*>(wsm);
+  T* stage = reinterpret_cast<T*>(wsm + kMaxTerms * kMaxDims * sizeof(long long));  // [2][256]
+  T* work = stage + 2 * kStageVals;                                                  // [2][256]
+  T* amat = work + 2 * kStageVals;                                                   // [2][kAmatVals]
   const T* f = static_cast<const T*>(pb.f);
   T* y = static_cast<T*>(pb.y);
   const T* ops = sizeof(T) == 8 ? reinterpret_cast<const T*>(pb.ops64) : reinterpret_cast<const T*>(pb.ops32);
-  const int B = pb.B, D = pb.D;
-  T acc[MAXE], cmp[MAXE];
-#pragma unroll
-  for (int k = 0; k < MAXE; ++k) acc[k] = cmp[k] = T(0);
-  const long long q1 = pb.row_ptr[row + 1];
-  for (long long q = pb.row_ptr[row]; q < q1; ++q) {
+  const int B = pb.B, D = pb.D, nt = pb.T;
+  // block base of operator (t, m) at this row's 1-D index: op_off + I_m(row) * nb * P^2
+  for (int k = lane; k < nt * D; k += 32) {
+    const long long off = pb.op_off[k];
+    abase[k] = off < 0 ? 0 : off + static_cast<long long>(pb.idx1d[row * D + k % D]) * pb.op_nb[k] * (P * P);
+  }
+  __syncwarp();
+  // issue the copies of entry q into stage st: the column block and every applied factor block
+  auto issue = [&](long long q, int st) {
     const int e = pb.ent[q];
     const int j = e >> 4, t = e & 15;
     const unsigned act = pb.active[t];
-    team_copy_w(buf0, f + static_cast<size_t>(j) * B, B, lane);
-    __syncwarp();
-    T* in = buf0;
-    T* out = buf1;
-    for (int m = D - 1; m >= 0; --m) {
+    const T* src = f + static_cast<size_t>(j) * B;
+    T* dst = stage + st * kStageVals;
+    for (int k = lane; k < B; k += 32) cp_async_elem(dst + k, src + k);
+    T* ad = amat + st * kAmatVals;
+    for (int k = lane; k < D * P * P; k += 32) {
+      const int m = k / (P * P), r = k - m * (P * P);
+      if ((act >> m) & 1u)
+        cp_async_elem(ad + m * 16 + r,
+                      ops + abase[t * D + m] + static_cast<long long>(pb.idx1d[j * D + m]) * (P * P) + r);
+    }
+    return act;
+  };
+  T acc[MAXE], cmp[MAXE];
+#pragma unroll
+  for (int k = 0; k < MAXE; ++k) acc[k] = cmp[k] = T(0);
+  const long long q0 = pb.row_ptr[row], q1 = pb.row_ptr[row + 1];
+  unsigned act_next = 0;
+  if (q0 < q1) act_next = issue(q0, 0);
+  cp_async_commit();
+  for (long long q = q0; q < q1; ++q) {
+    const int cur = static_cast<int>((q - q0) & 1);
+    const unsigned act = act_next;
+    if (q + 1 < q1) act_next = issue(q + 1, cur ^ 1);
+    cp_async_commit();
+    cp_async_wait_prev();  // this lane's copies of entry q have landed
+    __syncwarp();          // ... and every lane's
+    const T* in = stage + cur * kStageVals;
+    const T* Am = amat + cur * kAmatVals;
+    int wsel = 0;
+    int s = 1, sh = 0;  // stride P^(D-1-m) of dimension m; for P = 2, 4: s = 1 << sh
+    for (int m = D - 1; m >= 0; --m, s *= P, sh += LG) {
       if (!((act >> m) & 1u)) continue;
-      const int tm = t * D + m;
-      const T* Ag = ops + pb.op_off[tm] +
-                    (static_cast<long long>(pb.idx1d[row * D + m]) * pb.op_nb[tm] + pb.idx1d[j * D + m]) * (P * P);
       T A[P * P];
 #pragma unroll
-      for (int r = 0; r < P * P; ++r) A[r] = Ag[r];
-      const int s = pb.stride[m];
+      for (int r = 0; r < P * P; ++r) A[r] = Am[m * 16 + r];
+      T* out = work + wsel * kStageVals;
       for (int fi = lane; fi < B / P; fi += 32) {
-        const int hi = fi / s, lo = fi - hi * s;
+        int hi, lo;
+        if constexpr (LG > 0) {
+          hi = fi >> sh;
+          lo = fi & (s - 1);
+        } else {
+          hi = fi / s;
+          lo = fi - hi * s;
+        }
         const int base = hi * s * P + lo;
         T x[P];
 #pragma unroll
@@ -85,9 +153,8 @@ __device__ __forceinline__ void warp_row(const BatchProblem& pb, int row, T* buf
         }
       }
       __syncwarp();
-      T* tmp = in;
       in = out;
-      out = tmp;
+      wsel ^= 1;
     }
 #pragma unroll
     for (int k = 0; k < MAXE; ++k) {
@@ -103,7 +170,7 @@ __device__ __forceinline__ void warp_row(const BatchProblem& pb, int row, T* buf
         }
       }
     }
-    __syncwarp();
+    __syncwarp();  // stage cur is refilled by the next iteration's copies
   }
   T* yr = y + static_cast<size_t>(row) * B;
 #pragma unroll
@@ -116,10 +183,9 @@ __device__ __forceinline__ void warp_row(const BatchProblem& pb, int row, T* buf
 template <typename T>
 __global__ void k_batch(const BatchProblem* __restrict__ probs, const BatchItem* __restrict__ items, int nitems,
                         int rows_per_item, int* counter) {
-  __shared__ __align__(16) T sbuf[8][2][256];
+  extern __shared__ __align__(16) unsigned char batch_smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  T* buf0 = sbuf[warp][0];
-  T* buf1 = sbuf[warp][1];
+  unsigned char* wsm = batch_smem + warp * warp_smem_bytes<T>();
   while (true) {
     int it = 0;
     if (lane == 0) it = atomicAdd(counter, 1);
@@ -130,10 +196,10 @@ __global__ void k_batch(const BatchProblem* __restrict__ probs, const BatchItem*
     const int r1 = min(pb.N, w.row + rows_per_item);
     for (int row = w.row; row < r1; ++row) {
       switch (pb.P) {
-        case 1: warp_row<T, 1>(pb, row, buf0, buf1, lane); break;
-        case 2: warp_row<T, 2>(pb, row, buf0, buf1, lane); break;
-        case 3: warp_row<T, 3>(pb, row, buf0, buf1, lane); break;
-        case 4: warp_row<T, 4>(pb, row, buf0, buf1, lane); break;
+        case 1: warp_row<T, 1>(pb, row, wsm, lane); break;
+        case 2: warp_row<T, 2>(pb, row, wsm, lane); break;
+        case 3: warp_row<T, 3>(pb, row, wsm, lane); break;
+        case 4: warp_row<T, 4>(pb, row, wsm, lane); break;
         default: break;  // rejected at batch creation
       }
     }
@@ -210,6 +276,7 @@ asg_status asg_batch_create(asg_plan* const* plans, int count, asg_batch** out) 
     pb.D = p->D;
     pb.B = p->B;
     pb.P = p->P;
+    pb.T = p->T;
     int sd = 1;
     for (int m = p->D - 1; m >= 0; --m) {
       pb.stride[m] = sd;
@@ -308,12 +375,25 @@ asg_status asg_batch_apply(asg_batch* b, int precision, void* stream) {
   ASG_CUDA(cudaMemsetAsync(b->d_counter, 0, sizeof(int), s));
   const int c = b->rpi_choice;
   const int grid = 152 * (b->wpb == 4 ? 8 : 4);
-  if (precision == 1)
-    asg::k_batch<float><<<grid, b->wpb * 32, 0, s>>>(b->d_probs, b->d_items[c], b->nitems[c], kRowsPerItem[c],
-                                                     b->d_counter);
-  else
-    asg::k_batch<double><<<grid, b->wpb * 32, 0, s>>>(b->d_probs, b->d_items[c], b->nitems[c], kRowsPerItem[c],
-                                                      b->d_counter);
+  if (precision == 1) {
+    static bool done = false;  // opt in once to the largest request (8 warps per CTA)
+    if (!done) {
+      ASG_CUDA(cudaFuncSetAttribute(asg::k_batch<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(8 * asg::warp_smem_bytes<float>())));
+      done = true;
+    }
+    asg::k_batch<float><<<grid, b->wpb * 32, b->wpb * asg::warp_smem_bytes<float>(), s>>>(
+        b->d_probs, b->d_items[c], b->nitems[c], kRowsPerItem[c], b->d_counter);
+  } else {
+    static bool done = false;
+    if (!done) {
+      ASG_CUDA(cudaFuncSetAttribute(asg::k_batch<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    static_cast<int>(8 * asg::warp_smem_bytes<double>())));
+      done = true;
+    }
+    asg::k_batch<double><<<grid, b->wpb * 32, b->wpb * asg::warp_smem_bytes<double>(), s>>>(
+        b->d_probs, b->d_items[c], b->nitems[c], kRowsPerItem[c], b->d_counter);
+  }
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? ASG_OK : asg::cuda_fail(e, "batch launch");
 }
