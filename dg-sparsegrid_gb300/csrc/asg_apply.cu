@@ -9,21 +9,10 @@
 #include <cstdio>
 
 #include "asg_internal.h"
+#include "asg_rows.cuh"
 
 namespace asg {
 namespace {
-
-template <typename T>
-__device__ __forceinline__ void acc_add(T& s, T& c, T v, bool kahan) {
-  if (kahan) {
-    const T yv = v - c;
-    const T t = s + yv;
-    c = (t - s) - yv;
-    s = t;
-  } else {
-    s += v;
-  }
-}
 
 // P contiguous values with the widest aligned vector access the element type allows.
 template <typename T, int P>
@@ -177,86 +166,12 @@ __global__ void __launch_bounds__(128) k_chain_warp(ApplyArgs<T> a) {
   }
 }
 
-// ---------------------------------------------------------------------------------------
-// Small-block single-mode kernel: every term has one applied factor and deg^d <= 256 (the
-// 2-D/3-D configurations).  One warp per output element; the warp's lanes form G groups of
-// L lanes (L = min(32, next power of two >= deg^d)), group g taking the row's entries
-// g, g+G, ...; lane r of a group owns outputs r, r+L, ...  An entry adds, for each owned
-// output o (digit a along the entry's dimension m, stride s), sum_b A[a][b] f_j[o + (b-a) s]:
-// P strided loads of f_j and one row of the P x P block, straight from global memory (no
-// shared-memory round trip, no barrier per entry), two entries in flight per group.  Group
-// sums (Kahan-compensated in FP32) are added across groups by a fixed shuffle tree, so the
-// result is deterministic.
-// ---------------------------------------------------------------------------------------
-template <typename T, int P, int MAXO>
-__device__ __forceinline__ void small_entry(const ApplyArgs<T>& a, const EntryDesc& e, int r, int L, int B,
-                                            T (&v)[MAXO]) {
-  const int s = a.stride[e.m];
-  const T* fj = a.f + static_cast<size_t>(e.j) * B;
-  const T* Ab = a.ops + e.aoff;
-#pragma unroll
-  for (int q = 0; q < MAXO; ++q) {
-    const int o = r + L * q;
-    v[q] = T(0);
-    if (o < B) {
-      const int ad = (o / s) % P;
-      const int base = o - ad * s;
-      T acc = T(0);
-#pragma unroll
-      for (int b = 0; b < P; ++b) acc = fma(Ab[ad * P + b], fj[base + b * s], acc);
-      v[q] = acc;
-    }
-  }
-}
-
 template <typename T, int P, int MAXO, bool KAHAN>
 __global__ void __launch_bounds__(128) k_single_small(ApplyArgs<T> a) {
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
-  const int B = a.B;
-  int L = 1;
-  while (L < B && L < 32) L <<= 1;
-  const int G = 32 / L;
-  const int g = lane / L, r = lane - g * L;
-  for (int row = blockIdx.x * wpb + warp; row < a.N; row += gridDim.x * wpb) {
-    T acc[MAXO], cmp[MAXO];
-#pragma unroll
-    for (int q = 0; q < MAXO; ++q) acc[q] = cmp[q] = T(0);
-    const long long q0 = a.row_ptr[row], q1 = a.row_ptr[row + 1];
-    long long q = q0 + g;
-    for (; q + G < q1; q += 2 * G) {  // two entries of this group in flight
-      const EntryDesc e0 = a.ed[q], e1 = a.ed[q + G];
-      T v0[MAXO], v1[MAXO];
-      small_entry<T, P, MAXO>(a, e0, r, L, B, v0);
-      small_entry<T, P, MAXO>(a, e1, r, L, B, v1);
-#pragma unroll
-      for (int k = 0; k < MAXO; ++k) {
-        acc_add(acc[k], cmp[k], v0[k], KAHAN);
-        acc_add(acc[k], cmp[k], v1[k], KAHAN);
-      }
-    }
-    if (q < q1) {
-      const EntryDesc e0 = a.ed[q];
-      T v0[MAXO];
-      small_entry<T, P, MAXO>(a, e0, r, L, B, v0);
-#pragma unroll
-      for (int k = 0; k < MAXO; ++k) acc_add(acc[k], cmp[k], v0[k], KAHAN);
-    }
-    // fixed-order tree across the G groups (lane r of group 0 ends with the total)
-    for (int off = L; off < 32; off <<= 1) {
-#pragma unroll
-      for (int k = 0; k < MAXO; ++k) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], off);
-    }
-    if (g == 0) {
-      T* yr = a.y + static_cast<size_t>(row) * B;
-#pragma unroll
-      for (int k = 0; k < MAXO; ++k) {
-        const int o = r + L * k;
-        if (o < B) yr[o] = acc[k];
-      }
-    }
-  }
+  for (int row = blockIdx.x * wpb + warp; row < a.N; row += gridDim.x * wpb) small_row<T, P, MAXO, KAHAN>(a, row, lane);
 }
 
 // ---------------------------------------------------------------------------------------

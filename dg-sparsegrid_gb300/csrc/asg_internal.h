@@ -33,6 +33,14 @@ struct EntryDesc {
   long long aoff;
 };
 
+// One warp's share of a row in the fused GMRES cycle: entries [q0, q0 + len) of a row, summed
+// into partial-sum slot `slot` (a row's slots are added in slot order).
+struct FzItem {
+  long long q0;
+  int len;
+  int slot;
+};
+
 // Arguments of the operator-application kernels.  One work entry is one
 // (column element, term) product contributing to a row element; entries of a row are
 // contiguous (CSR by row), packed as (col << 4) | term.
@@ -103,6 +111,11 @@ cudaError_t launch_grad(const GradArgs<T>& a, int P, cudaStream_t s);
 enum KernelKind { KK_CHAIN_WARP = 0, KK_CHAIN_CTA = 1, KK_SINGLE_MODE = 2, KK_SINGLE_TMA = 3, KK_SINGLE_TMA3 = 4,
                   KK_SINGLE_TMA_ROWS = 5, KK_SINGLE_SMALL = 6 };
 
+// Apply arguments (f and y unset) of a plan that runs the small-block single-mode kernel, for
+// kernels that call its row routine themselves (the fused GMRES cycle); false for other plans.
+template <typename T>
+bool small_plan_args(const asg_plan* p, ApplyArgs<T>* out);
+
 // Resident CTAs per SM of the persistent single-mode kernel for element size es (4 or 8);
 // sets the kernel's dynamic shared-memory limit first.  0 on error.
 int single_tma_rows_occupancy(int es);
@@ -164,6 +177,11 @@ struct asg_plan {
   int* d_cta_ptr[2] = {nullptr, nullptr};
   int* d_cta_rows[2] = {nullptr, nullptr};
   float* d_ops_pair = nullptr;
+  // fused GMRES cycle (small-block plans, built on first use): contiguous row ranges per CTA
+  // and chunks of their rows' entries per warp
+  int fz_G = 0, fz_max_rows = 0, fz_max_slots = 0;
+  int* d_fz_int = nullptr;           // blk_row[G+1], blk_slot[G+1], row_slot[N+1], warp_item[G*W+1]
+  asg::FzItem* d_fz_items = nullptr;
   int* d_err = nullptr;
   double* d_ops64 = nullptr;
   float* d_ops32 = nullptr;

@@ -74,6 +74,8 @@ void free_device(asg_plan* p) {
     cudaFree(p->d_cta_rows[k]);
   }
   cudaFree(p->d_ops_pair);
+  cudaFree(p->d_fz_int);
+  cudaFree(p->d_fz_items);
   cudaFree(p->d_err);
   cudaFree(p->d_io);
   if (p->stream) cudaStreamDestroy(p->stream);
@@ -522,6 +524,17 @@ asg_status apply_host(asg_plan* p, const T* hf, T* hy) {
 }
 
 }  // namespace
+
+template <typename T>
+bool small_plan_args(const asg_plan* p, ApplyArgs<T>* out) {
+  if (!p || p->kernel_kind != KK_SINGLE_SMALL || p->ed.size() != p->ent.size() || p->N == 0) return false;
+  const T* ops = sizeof(T) == 8 ? reinterpret_cast<const T*>(p->d_ops64) : reinterpret_cast<const T*>(p->d_ops32);
+  *out = make_args<T>(p, nullptr, nullptr, ops);
+  return true;
+}
+template bool small_plan_args<float>(const asg_plan*, ApplyArgs<float>*);
+template bool small_plan_args<double>(const asg_plan*, ApplyArgs<double>*);
+
 }  // namespace asg
 
 using asg::fail;

@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "asg_internal.h"
+#include "asg_rows.cuh"
 
 namespace asg {
 namespace {
@@ -110,6 +111,7 @@ struct GmresState {
   int kdone;     // Arnoldi steps taken
   double resid;  // |g[kdone]|, the residual estimate
   double inv;    // 1 / ||w|| of the last step (scales the next basis vector)
+  unsigned bar[3];  // fused cycle's grid barrier: arrivals, generation, timeout flag
 };
 // w = V_j - dt * (A V_j), skipped once the cycle is done
 template <typename TV>
@@ -266,6 +268,301 @@ __global__ void k_sol_update_g(long long n, const double* __restrict__ y, const 
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Fused GMRES cycle for plans on the small-block single-mode kernel: one cooperative launch
+// runs a whole GMRES(m) cycle.  CTA b owns a contiguous range of element rows (balanced by
+// work entries) and keeps its slice of the Krylov basis and of w in shared memory, so
+// everything but the operator application and the grid-wide sums stays on chip:
+//   1. A v_j for the CTA's own rows (the rows' entries split into chunks over the warps,
+//      chunk sums added per row in a fixed order; v_j read from the global basis copy),
+//      w = v_j - dt A v_j, first Gram-Schmidt pass's partial dots          -> grid barrier
+//   2. h = grid sums, w -= V h, second pass's partial dots and ||w||^2    -> grid barrier
+//   3. h2 = grid sums, w -= V h2, ||w||^2 = ||w_before||^2 - ||h2||^2 (an explicit sum, with
+//      one more barrier, when ||h2||^2 > 1e-2 ||w_before||^2), the Givens step, v_{j+1} =
+//      w / ||w|| into shared memory and the global copy                    -> grid barrier
+// Every CTA reduces the same partials in the same order and runs the same Givens
+// recurrence, so all take the same stopping decision; CTA 0 keeps the Hessenberg matrix for
+// the back substitution.  Fixed-order reductions: bitwise reproducible.  The grid barrier's
+// wait is bounded (~2^31 cycles): on expiry the kernel records the timeout and returns.
+// ---------------------------------------------------------------------------------------
+constexpr int kFzThreads = 512;
+constexpr int kFzWarps = kFzThreads / 32;
+
+template <typename TV>
+struct FusedArgs {
+  ApplyArgs<TV> a;             // the plan's apply arguments (a.f, a.y unused)
+  long long n, ldv;
+  double dt, target, beta;
+  int m;
+  TV* V;                       // global basis copy, read by the operator application
+  double* partial;             // (2m + 2) rows of gridDim.x CTA partials
+  double* H;                   // [(m+1) x m] Hessenberg (CTA 0)
+  double* yv;
+  const double* r0;
+  double* x64;
+  GmresState* state;           // zeroed before the launch; bar[] is the grid barrier
+  const int* blk_row;          // [G+1] row range of CTA b
+  const int* blk_slot;         // [G+1] its partial-sum slots
+  const int* row_slot;         // [N+1] slots of each row
+  const int* warp_item;        // [G*W+1] items of warp w of CTA b
+  const FzItem* items;
+  int max_rows, max_slots;
+};
+
+__host__ __device__ constexpr size_t align16(size_t x) { return (x + 15) / 16 * 16; }
+
+// Dynamic shared memory of the fused cycle: basis slice [m+1][S], w [S] (FP64), partial-sum
+// slots [slots][B].
+template <typename TV>
+__host__ __device__ constexpr size_t fused_smem(int m, int max_rows, int max_slots, int B) {
+  return align16(static_cast<size_t>(m + 1) * max_rows * B * sizeof(TV)) +
+         align16(static_cast<size_t>(max_rows) * B * sizeof(double)) +
+         static_cast<size_t>(max_slots) * B * sizeof(TV);
+}
+
+// Grid-wide barrier for a cooperative launch (all CTAs resident): arrival counter plus a
+// generation word; bounded wait.  Returns false once any CTA has timed out.
+__device__ bool grid_sync(unsigned* bar) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* gen = bar + 1;
+    volatile unsigned* flag = bar + 2;
+    int ok = *flag == 0u;
+    if (ok) {
+      const unsigned g0 = *gen;
+      __threadfence();
+      if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+        atomicExch(bar, 0u);
+        __threadfence();
+        atomicAdd(bar + 1, 1u);
+      } else {
+        const long long t0 = clock64();
+        while (*gen == g0) {
+          if (*flag != 0u || clock64() - t0 > (1LL << 31)) {
+            atomicExch(bar + 2, 1u);
+            ok = 0;
+            break;
+          }
+        }
+      }
+      __threadfence();
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// Sum over the CTA of one value per thread, fixed order; the result goes to every thread.
+__device__ double fz_block_sum(double v) {
+  __shared__ double red[kFzWarps];
+  __shared__ double total;
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int q = 0; q < kFzWarps; ++q) s += red[q];
+    total = s;
+  }
+  __syncthreads();
+  const double r = total;
+  __syncthreads();
+  return r;
+}
+
+// Warp sum, fixed order (every lane gets the total).
+__device__ __forceinline__ double fz_warp_sum(double v) {
+  for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+  return v;
+}
+
+// s_out[k] = sum over the grid's CTAs of partial[k * G + q], k < nk: one warp per row k, its
+// lanes adding q = lane, lane + 32, ...; every CTA computes the same values in the same order.
+__device__ void sum_partials(const double* partial, int nk, double* s_out) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, G = gridDim.x;
+  for (int k = warp; k < nk; k += kFzWarps) {
+    double acc = 0.0;
+    for (int q = lane; q < G; q += 32) acc += __ldcg(partial + static_cast<long long>(k) * G + q);
+    acc = fz_warp_sum(acc);
+    if (lane == 0) s_out[k] = acc;
+  }
+  __syncthreads();
+}
+
+template <typename TV, int P, int MAXO>
+__global__ void __launch_bounds__(kFzThreads, 1) k_gmres_fused(const __grid_constant__ FusedArgs<TV> c) {
+  constexpr bool KAHAN = sizeof(TV) == 4;
+  extern __shared__ __align__(16) unsigned char fz_smem[];
+  __shared__ double s_h[kMaxRestart], s_h2[kMaxRestart + 1], s_cs[kMaxRestart], s_sn[kMaxRestart],
+      s_g[kMaxRestart + 1], s_hc[kMaxRestart + 1];
+  __shared__ double s_hn2, s_inv, s_resid;
+  __shared__ int s_done, s_need;
+  const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int B = c.a.B, m = c.m;
+  const long long ldv = c.ldv;
+  const int r0 = c.blk_row[b], r1 = c.blk_row[b + 1];
+  const int S = (r1 - r0) * B;                      // this CTA's elements
+  const long long i0 = static_cast<long long>(r0) * B;
+  const int Smax = c.max_rows * B;
+  TV* Vs = reinterpret_cast<TV*>(fz_smem);          // [m+1][Smax]
+  double* ws = reinterpret_cast<double*>(fz_smem + align16(static_cast<size_t>(m + 1) * Smax * sizeof(TV)));
+  TV* slots = reinterpret_cast<TV*>(reinterpret_cast<unsigned char*>(ws) + align16(static_cast<size_t>(Smax) * sizeof(double)));
+  const int slot0 = c.blk_slot[b];
+  double* part1 = c.partial;
+  double* part2 = c.partial + static_cast<long long>(m) * G;
+  double* partn = c.partial + (2LL * m + 1) * G;
+  unsigned* bar = c.state->bar;
+  {  // v_0 = r0 / beta
+    const double ib = 1.0 / c.beta;
+    for (int e = tid; e < S; e += kFzThreads) {
+      const TV v = static_cast<TV>(c.r0[i0 + e] * ib);
+      Vs[e] = v;
+      c.V[i0 + e] = v;
+    }
+  }
+  if (tid == 0) {
+    for (int k = 0; k <= m; ++k) s_g[k] = 0.0;
+    s_g[0] = c.beta;
+  }
+  const int it0 = c.warp_item[b * kFzWarps + warp], it1 = c.warp_item[b * kFzWarps + warp + 1];
+  int kdone = 0;
+  double resid = c.beta;
+  bool ok = grid_sync(bar);
+  for (int j = 0; j < m && ok; ++j) {
+    const TV* Vj = Vs + j * Smax;
+    // 1. A v_j for the CTA's rows, w = v_j - dt A v_j, pass-1 partial dots
+    {
+      const TV* f = c.V + j * ldv;
+      for (int it = it0; it < it1; ++it) {
+        const FzItem t = c.items[it];
+        small_chunk<TV, P, MAXO, KAHAN>(c.a, f, t.q0, t.q0 + t.len, lane, slots + (t.slot - slot0) * B);
+      }
+    }
+    __syncthreads();
+    for (int e = tid; e < S; e += kFzThreads) {
+      const int r = e / B, o = e - r * B;
+      const int s0 = c.row_slot[r0 + r] - slot0, s1 = c.row_slot[r0 + r + 1] - slot0;
+      TV ax = TV(0);
+      for (int q = s0; q < s1; ++q) ax += slots[q * B + o];
+      ws[e] = static_cast<double>(Vj[e]) - c.dt * static_cast<double>(ax);
+    }
+    __syncthreads();
+    for (int k = warp; k <= j; k += kFzWarps) {
+      const TV* vk = Vs + k * Smax;
+      double acc = 0.0;
+      for (int e = lane; e < S; e += 32) acc = fma(ws[e], static_cast<double>(vk[e]), acc);
+      acc = fz_warp_sum(acc);
+      if (lane == 0) part1[static_cast<long long>(k) * G + b] = acc;
+    }
+    if (!(ok = grid_sync(bar))) break;
+    // 2. h; w -= V h; pass-2 partial dots and ||w||^2
+    sum_partials(part1, j + 1, s_h);
+    for (int e = tid; e < S; e += kFzThreads) {
+      double acc = ws[e];
+      for (int k = 0; k <= j; ++k) acc = fma(-s_h[k], static_cast<double>(Vs[k * Smax + e]), acc);
+      ws[e] = acc;
+    }
+    __syncthreads();
+    for (int k = warp; k <= j + 1; k += kFzWarps) {
+      double acc = 0.0;
+      if (k <= j) {
+        const TV* vk = Vs + k * Smax;
+        for (int e = lane; e < S; e += 32) acc = fma(ws[e], static_cast<double>(vk[e]), acc);
+      } else {
+        for (int e = lane; e < S; e += 32) acc = fma(ws[e], ws[e], acc);
+      }
+      acc = fz_warp_sum(acc);
+      if (lane == 0) part2[static_cast<long long>(k) * G + b] = acc;
+    }
+    if (!(ok = grid_sync(bar))) break;
+    // 3. h2; w -= V h2; ||w||; Givens; v_{j+1}
+    sum_partials(part2, j + 2, s_h2);
+    for (int e = tid; e < S; e += kFzThreads) {
+      double acc = ws[e];
+      for (int k = 0; k <= j; ++k) acc = fma(-s_h2[k], static_cast<double>(Vs[k * Smax + e]), acc);
+      ws[e] = acc;
+    }
+    if (tid == 0) {
+      double h2sq = 0.0;
+      for (int k = 0; k <= j; ++k) h2sq = fma(s_h2[k], s_h2[k], h2sq);
+      const double nw2 = s_h2[j + 1];
+      s_hn2 = nw2 - h2sq;
+      s_need = h2sq <= 1e-2 * nw2 ? 0 : 1;
+    }
+    __syncthreads();
+    if (s_need) {  // the same decision in every CTA: explicit ||w||^2
+      double acc = 0.0;
+      for (int e = tid; e < S; e += kFzThreads) acc = fma(ws[e], ws[e], acc);
+      acc = fz_block_sum(acc);
+      if (tid == 0) partn[b] = acc;
+      if (!(ok = grid_sync(bar))) break;
+      sum_partials(partn, 1, &s_hn2);
+    }
+    if (tid == 0) {
+      const double hn = sqrt(fmax(s_hn2, 0.0));
+      for (int k = 0; k <= j; ++k) s_hc[k] = s_h[k] + s_h2[k];
+      s_hc[j + 1] = hn;
+      for (int i = 0; i < j; ++i) {
+        const double t = s_cs[i] * s_hc[i] + s_sn[i] * s_hc[i + 1];
+        s_hc[i + 1] = -s_sn[i] * s_hc[i] + s_cs[i] * s_hc[i + 1];
+        s_hc[i] = t;
+      }
+      const double den = hypot(s_hc[j], s_hc[j + 1]);
+      const double cc = den > 0 ? s_hc[j] / den : 1.0, sv = den > 0 ? s_hc[j + 1] / den : 0.0;
+      s_cs[j] = cc;
+      s_sn[j] = sv;
+      s_hc[j] = den;
+      const double gj = s_g[j];
+      s_g[j + 1] = -sv * gj;
+      s_g[j] = cc * gj;
+      if (b == 0)
+        for (int i = 0; i <= j; ++i) c.H[static_cast<long long>(i) * m + j] = s_hc[i];
+      const double rr = fabs(sv * gj);
+      s_done = (rr <= c.target || hn == 0.0 || j + 1 == m) ? 1 : 0;
+      s_inv = hn > 0 ? 1.0 / hn : 0.0;
+      s_resid = rr;
+    }
+    __syncthreads();
+    kdone = j + 1;
+    resid = s_resid;
+    if (s_done) break;  // the same decision in every CTA
+    {
+      const double inv = s_inv;
+      TV* Vn = Vs + (j + 1) * Smax;
+      TV* Vg = c.V + (j + 1) * ldv + i0;
+      for (int e = tid; e < S; e += kFzThreads) {
+        const TV v = static_cast<TV>(ws[e] * inv);
+        Vn[e] = v;
+        Vg[e] = v;
+      }
+    }
+    if (!(ok = grid_sync(bar))) break;
+  }
+  // y = H(1:k,1:k) \ g(1:k) (CTA 0), then x += V y (every CTA, its own elements)
+  if (ok && b == 0 && tid == 0) {
+    for (int i = kdone - 1; i >= 0; --i) {
+      double acc = s_g[i];
+      for (int q = i + 1; q < kdone; ++q) acc -= c.H[static_cast<long long>(i) * m + q] * c.yv[q];
+      c.yv[i] = acc / c.H[static_cast<long long>(i) * m + i];
+    }
+  }
+  if (ok) ok = grid_sync(bar);
+  if (ok) {
+    for (int e = tid; e < S; e += kFzThreads) {
+      double acc = c.x64[i0 + e];
+      for (int k = 0; k < kdone; ++k) acc = fma(__ldcg(c.yv + k), static_cast<double>(Vs[k * Smax + e]), acc);
+      c.x64[i0 + e] = acc;
+    }
+  }
+  if (b == 0 && tid == 0) {
+    c.state->kdone = kdone;
+    c.state->resid = resid;
+    c.state->done = 1;
+  }
+}
+
 inline int grid_for(long long n) {
   const long long g = (n + 255) / 256;
   return static_cast<int>(g < 152LL * 16 ? (g > 0 ? g : 1) : 152LL * 16);
@@ -306,7 +603,7 @@ GmresLayout gmres_layout(long long n, int m, bool mixed) {
   L.axmv = take(n * (mixed ? sizeof(float) : sizeof(double)));
   L.h = take((m + 1) * sizeof(double));
   L.y = take((m + 1) * sizeof(double));
-  L.partial = take(static_cast<size_t>(m + 1) * asg::kRedBlocks * sizeof(double));
+  L.partial = take(static_cast<size_t>(2 * m + 2) * asg::kRedBlocks * sizeof(double));
   L.hcol = take((m + 1) * sizeof(double));
   L.hh = take(static_cast<size_t>(m + 1) * m * sizeof(double));
   L.cs = take(m * sizeof(double));
@@ -328,6 +625,174 @@ double host_norm(const double* d_partial, int nb, cudaStream_t s, asg_status* st
   double acc = 0.0;
   for (double v : p) acc += v;
   return std::sqrt(acc);
+}
+
+// Schedule of the fused cycle for a small-block plan, built once per plan: G CTAs (at most
+// one per SM and one per row, about one per 64 work entries), contiguous row ranges balanced
+// by work entries plus a per-row share for the vector work; each CTA's rows are cut into
+// chunks of at most max(8, E_b / (4 W)) entries (E_b: the CTA's entries, W: warps per CTA),
+// and the chunks go to the warps longest first, each to the least-loaded warp.
+asg_status fused_schedule(asg_plan* p) {
+  if (p->fz_G > 0) return ASG_OK;
+  int dev = 0, nsm = 0;
+  ASG_CUDA(cudaGetDevice(&dev));
+  ASG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  const int N = p->N, B = p->B, W = asg::kFzWarps;
+  const std::vector<long long>& rp = p->row_ptr;
+  const long long E = rp[N];
+  const int G = static_cast<int>(std::max<long long>(
+      1, std::min<long long>({static_cast<long long>(nsm), static_cast<long long>(N), (E + 63) / 64})));
+  const double rowc = 1.0 + B / 4.0;
+  std::vector<double> pre(N + 1, 0.0);
+  for (int r = 0; r < N; ++r) pre[r + 1] = pre[r] + static_cast<double>(rp[r + 1] - rp[r]) + rowc;
+  std::vector<int> blk_row(G + 1, 0), blk_slot(G + 1, 0), row_slot(N + 1, 0), warp_item(static_cast<size_t>(G) * W + 1, 0);
+  blk_row[G] = N;
+  for (int b = 1; b < G; ++b) {
+    const double target = pre[N] * b / G;
+    int r = static_cast<int>(std::lower_bound(pre.begin(), pre.end(), target) - pre.begin());
+    if (r > 0 && target - pre[r - 1] < pre[r] - target) --r;
+    r = std::max(r, blk_row[b - 1] + 1);
+    r = std::min(r, N - (G - b));
+    blk_row[b] = r;
+  }
+  std::vector<asg::FzItem> items;
+  int slot = 0, max_rows = 0, max_slots = 0;
+  for (int b = 0; b < G; ++b) {
+    const int r0 = blk_row[b], r1 = blk_row[b + 1];
+    const long long Eb = rp[r1] - rp[r0];
+    const long long ch = std::max<long long>(8, (Eb + 4 * W - 1) / (4 * W));
+    blk_slot[b] = slot;
+    std::vector<asg::FzItem> bi;
+    for (int r = r0; r < r1; ++r) {
+      row_slot[r] = slot;
+      const long long er = rp[r + 1] - rp[r];
+      const long long nch = (er + ch - 1) / ch;
+      long long q = rp[r];
+      for (long long k = 0; k < nch; ++k) {
+        const long long len = er / nch + (k < er % nch ? 1 : 0);
+        bi.push_back(asg::FzItem{q, static_cast<int>(len), slot++});
+        q += len;
+      }
+    }
+    max_rows = std::max(max_rows, r1 - r0);
+    max_slots = std::max(max_slots, slot - blk_slot[b]);
+    // longest first onto the least-loaded warp (ties: lowest warp)
+    std::vector<int> order(bi.size());
+    for (size_t k = 0; k < order.size(); ++k) order[k] = static_cast<int>(k);
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return bi[x].len > bi[y].len; });
+    std::vector<long long> load(W, 0);
+    std::vector<std::vector<asg::FzItem>> per(W);
+    for (int k : order) {
+      const int w = static_cast<int>(std::min_element(load.begin(), load.end()) - load.begin());
+      load[w] += bi[k].len + 2;
+      per[w].push_back(bi[k]);
+    }
+    for (int w = 0; w < W; ++w) {
+      warp_item[static_cast<size_t>(b) * W + w] = static_cast<int>(items.size());
+      items.insert(items.end(), per[w].begin(), per[w].end());
+    }
+  }
+  blk_slot[G] = slot;
+  row_slot[N] = slot;
+  warp_item[static_cast<size_t>(G) * W] = static_cast<int>(items.size());
+  std::vector<int> ints;
+  ints.insert(ints.end(), blk_row.begin(), blk_row.end());
+  ints.insert(ints.end(), blk_slot.begin(), blk_slot.end());
+  ints.insert(ints.end(), row_slot.begin(), row_slot.end());
+  ints.insert(ints.end(), warp_item.begin(), warp_item.end());
+  ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_fz_int), ints.size() * sizeof(int)));
+  ASG_CUDA(cudaMemcpy(p->d_fz_int, ints.data(), ints.size() * sizeof(int), cudaMemcpyHostToDevice));
+  if (!items.empty()) {
+    ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_fz_items), items.size() * sizeof(asg::FzItem)));
+    ASG_CUDA(cudaMemcpy(p->d_fz_items, items.data(), items.size() * sizeof(asg::FzItem), cudaMemcpyHostToDevice));
+  }
+  p->fz_max_rows = max_rows;
+  p->fz_max_slots = max_slots;
+  p->fz_G = G;
+  return ASG_OK;
+}
+
+// The fused cycle (one cooperative launch) for plans on the small-block single-mode kernel
+// with deg 2..4 whose per-CTA slices fit in shared memory; *used = false when the plan does
+// not qualify (the caller then runs the kernel-per-phase cycle).
+template <typename TV, int P, int MAXO>
+cudaError_t launch_fused(const asg::FusedArgs<TV>& c, int G, size_t smem, cudaStream_t s) {
+  auto kern = asg::k_gmres_fused<TV, P, MAXO>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  if (e != cudaSuccess) return e;
+  int dev = 0, nsm = 0, coop = 0, per_sm = 0;
+  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+  if ((e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev)) != cudaSuccess) return e;
+  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, asg::kFzThreads, smem)) != cudaSuccess) return e;
+  if (!coop || static_cast<long long>(per_sm) * nsm < G) return cudaErrorNotSupported;
+  void* args[] = {const_cast<asg::FusedArgs<TV>*>(&c)};
+  return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(kern), dim3(G), dim3(asg::kFzThreads), args, smem, s);
+}
+
+template <typename TV, int P>
+cudaError_t launch_fused_p(const asg::FusedArgs<TV>& c, int G, size_t smem, cudaStream_t s) {
+  const int B = c.a.B;
+  if (B <= 32) return launch_fused<TV, P, 1>(c, G, smem, s);
+  if (B <= 64) return launch_fused<TV, P, 2>(c, G, smem, s);
+  if (B <= 128) return launch_fused<TV, P, 4>(c, G, smem, s);
+  return launch_fused<TV, P, 8>(c, G, smem, s);
+}
+
+constexpr size_t kFusedSmemLimit = 200 * 1024;
+
+template <typename TV>
+asg_status gmres_cycle_fused(asg_plan* plan, long long n, double dt, double beta, const double* r0, double* x64,
+                             int m, double rtol_abs, unsigned char* base, const GmresLayout& L, cudaStream_t s,
+                             int* iters, double* resid, bool* used) {
+  *used = false;
+  asg::FusedArgs<TV> c{};
+  if (!asg::small_plan_args<TV>(plan, &c.a) || c.a.B > 256) return ASG_OK;
+  const int P = c.a.D >= 2 ? c.a.stride[c.a.D - 2] : c.a.B;
+  if (P < 2 || P > 4) return ASG_OK;
+  asg_status st = fused_schedule(plan);
+  if (st) return st;
+  const int G = plan->fz_G;
+  const size_t smem = asg::fused_smem<TV>(m, plan->fz_max_rows, plan->fz_max_slots, c.a.B);
+  if (smem > kFusedSmemLimit) return ASG_OK;
+  c.n = n;
+  c.ldv = basis_ld(n);
+  c.dt = dt;
+  c.target = rtol_abs;
+  c.beta = beta;
+  c.m = m;
+  c.V = reinterpret_cast<TV*>(base + L.v);
+  c.partial = reinterpret_cast<double*>(base + L.partial);
+  c.H = reinterpret_cast<double*>(base + L.hh);
+  c.yv = reinterpret_cast<double*>(base + L.y);
+  c.r0 = r0;
+  c.x64 = x64;
+  c.state = reinterpret_cast<asg::GmresState*>(base + L.state);
+  const int* fz = plan->d_fz_int;
+  c.blk_row = fz;
+  c.blk_slot = fz + (G + 1);
+  c.row_slot = fz + 2 * (G + 1);
+  c.warp_item = fz + 2 * (G + 1) + (plan->N + 1);
+  c.items = plan->d_fz_items;
+  c.max_rows = plan->fz_max_rows;
+  c.max_slots = plan->fz_max_slots;
+  ASG_CUDA(cudaMemsetAsync(c.state, 0, sizeof(asg::GmresState), s));
+  cudaError_t e = P == 2 ? launch_fused_p<TV, 2>(c, G, smem, s)
+                  : P == 3 ? launch_fused_p<TV, 3>(c, G, smem, s)
+                           : launch_fused_p<TV, 4>(c, G, smem, s);
+  if (e == cudaErrorNotSupported) {
+    cudaGetLastError();
+    return ASG_OK;  // the CTAs cannot all be resident: the caller runs the per-phase cycle
+  }
+  if (e != cudaSuccess) return asg::cuda_fail(e, "fused gmres cycle");
+  *used = true;
+  asg::GmresState hs{};
+  ASG_CUDA(cudaMemcpyAsync(&hs, c.state, sizeof(hs), cudaMemcpyDeviceToHost, s));
+  ASG_CUDA(cudaStreamSynchronize(s));
+  if (hs.bar[2]) return fail(ASG_ERR_TIMEOUT, "fused gmres cycle: grid barrier wait gave up (%d CTAs)", G);
+  *iters = hs.kdone;
+  *resid = hs.resid;
+  return ASG_OK;
 }
 
 // One GMRES(m) cycle on (I - dt A) delta = r0 (r0 FP64), adding delta to x64 in FP64.  TV is
@@ -352,6 +817,9 @@ asg_status gmres_cycle(asg_plan* plan, long long n, double dt, const double* r0,
   if (st) return st;
   *resid = beta;
   if (beta <= rtol_abs || beta == 0.0) return ASG_OK;
+  bool fused = false;
+  st = gmres_cycle_fused<TV>(plan, n, dt, beta, r0, x64, m, rtol_abs, base, L, s, iters, resid, &fused);
+  if (st || fused) return st;
   asg::k_store_basis<TV><<<gr, 256, 0, s>>>(n, 1.0 / beta, r0, V);
   double* hcol = reinterpret_cast<double*>(base + L.hcol);
   double* H = reinterpret_cast<double*>(base + L.hh);

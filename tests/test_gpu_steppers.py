@@ -233,3 +233,31 @@ def test_be_cfg3_ten_steps_mixed_vs_fp64(dev):
         assert im["converged"] and im["rel_residual"] <= 1e-10, (step, im)
         assert idd["converged"] and idd["rel_residual"] <= 1e-10, (step, idd)
     assert rel2(fm.cpu().numpy(), fd.cpu().numpy()) <= 1e-9
+
+
+@pytest.mark.parametrize("lev,deg,mixed", [(4, 2, True), (4, 3, False), (6, 4, True), (6, 4, False)])
+def test_be_fused_cycle_vs_per_phase_cycle(dev, lev, deg, mixed):
+    """Plans on the small-block kernel run each GMRES cycle as one cooperative launch; the same
+    plan switched to the warp-chain kernel runs the kernel-per-phase cycle.  Both solve
+    (I - dt A) x = b to the same tolerance and agree with each other."""
+    import asgkron
+    from asgkron import pdes
+    from asgkron._lib import KERNEL_CHAIN_WARP, KERNEL_NAMES
+    from asgkron.steppers import be_step
+
+    pde = pdes.diffusion2(lev)
+    idx = asgkron.hash_table_sparse_nD(pde.levels, 8).idx1d()
+    plan = asgkron.Plan.create(pde.term_mats(deg), idx, deg)
+    assert KERNEL_NAMES[plan.stats()["kernel_kind"]] == "single_mode_small"
+    f0 = pde.initial_condition(deg, idx) + 1e-3 * np.random.default_rng(5).standard_normal(plan.dof)
+    dt = pde.dt(1.0)
+    f = torch.from_numpy(f0).to(dev)
+    xf, inf_f = be_step(plan, f, dt, mixed=mixed, tol=1e-11, restart=20)
+    xf2, _ = be_step(plan, f, dt, mixed=mixed, tol=1e-11, restart=20)
+    plan.set_kernel(KERNEL_CHAIN_WARP)
+    xp, inf_p = be_step(plan, f, dt, mixed=mixed, tol=1e-11, restart=20)
+    torch.cuda.synchronize()
+    assert inf_f["converged"] and inf_p["converged"], (inf_f, inf_p)
+    assert inf_f["rel_residual"] <= 1e-11 and inf_p["rel_residual"] <= 1e-11
+    assert torch.equal(xf, xf2)  # fixed-order reductions: the fused cycle is reproducible
+    assert rel2(xf.cpu().numpy(), xp.cpu().numpy()) <= 1e-9
