@@ -111,7 +111,9 @@ struct GmresState {
   int kdone;     // Arnoldi steps taken
   double resid;  // |g[kdone]|, the residual estimate
   double inv;    // 1 / ||w|| of the last step (scales the next basis vector)
-  unsigned bar[3];  // fused cycle's grid barrier: arrivals, generation, timeout flag
+  unsigned bar[3];  // fused solve's grid barrier: arrivals, (unused), timeout flag
+  int outer, inner, converged;  // fused solve's result
+  double rel;
 };
 // w = V_j - dt * (A V_j), skipped once the cycle is done
 template <typename TV>
@@ -269,37 +271,41 @@ __global__ void k_sol_update_g(long long n, const double* __restrict__ y, const 
 }
 
 // ---------------------------------------------------------------------------------------
-// Fused GMRES cycle for plans on the small-block single-mode kernel: one cooperative launch
-// runs a whole GMRES(m) cycle.  CTA b owns a contiguous range of element rows (balanced by
-// work entries) and keeps its slice of the Krylov basis and of w in shared memory, so
-// everything but the operator application and the grid-wide sums stays on chip:
-//   1. A v_j for the CTA's own rows (the rows' entries split into chunks over the warps,
-//      chunk sums added per row in a fixed order; v_j read from the global basis copy),
+// Fused backward-Euler solve for plans on the small-block single-mode kernel: one cooperative
+// launch solves (I - dt A) x = b -- the FP64 outer residuals, their norms and the stopping
+// test, and every restarted GMRES(m) cycle on the correction (basis and operator in TV).  CTA
+// b owns a contiguous range of element rows (balanced by work entries) and keeps its slice
+// of the Krylov basis and of w in shared memory, so everything but the operator applications
+// and the grid-wide sums stays on chip.  A restart: r = b - (x - dt A x) in FP64 for the
+// CTA's rows and ||r|| (one grid barrier), the stopping test, v_0 = r / ||r|| (one barrier),
+// then per Arnoldi step:
+//   1. A v_j for the CTA's rows (the rows' entries cut into chunks over the warps, chunk sums
+//      added per row in a fixed order; v_j read from the global basis copy),
 //      w = v_j - dt A v_j, first Gram-Schmidt pass's partial dots          -> grid barrier
 //   2. h = grid sums, w -= V h, second pass's partial dots and ||w||^2    -> grid barrier
 //   3. h2 = grid sums, w -= V h2, ||w||^2 = ||w_before||^2 - ||h2||^2 (an explicit sum, with
 //      one more barrier, when ||h2||^2 > 1e-2 ||w_before||^2), the Givens step, v_{j+1} =
 //      w / ||w|| into shared memory and the global copy                    -> grid barrier
-// Every CTA reduces the same partials in the same order and runs the same Givens
-// recurrence, so all take the same stopping decision; CTA 0 keeps the Hessenberg matrix for
-// the back substitution.  Fixed-order reductions: bitwise reproducible.  The grid barrier's
-// wait is bounded (~2^31 cycles): on expiry the kernel records the timeout and returns.
+// and after the last step R y = g (every CTA holds the same R and g) and x += V y over the
+// CTA's slice (one barrier before the next residual).  Every CTA reduces the same partials
+// in the same order and runs the same recurrences, so all take the same decisions.
+// Fixed-order reductions: bitwise reproducible.  Grid barrier waits are bounded (~2^31
+// cycles): on expiry the kernel records the timeout and returns.
 // ---------------------------------------------------------------------------------------
 constexpr int kFzThreads = 512;
 constexpr int kFzWarps = kFzThreads / 32;
 
 template <typename TV>
 struct FusedArgs {
-  ApplyArgs<TV> a;             // the plan's apply arguments (a.f, a.y unused)
+  ApplyArgs<TV> a;             // the plan's apply arguments in the basis precision (f, y unused)
+  ApplyArgs<double> a64;       // and in FP64, for the outer residual
   long long n, ldv;
-  double dt, target, beta;
-  int m;
+  double dt, tol, inner_reduction;
+  int m, max_outer;
   TV* V;                       // global basis copy, read by the operator application
   double* partial;             // (2m + 2) rows of gridDim.x CTA partials
-  double* H;                   // [(m+1) x m] Hessenberg (CTA 0)
-  double* yv;
-  const double* r0;
-  double* x64;
+  const double* rhs;           // b
+  double* x;                   // initial guess in, solution out
   GmresState* state;           // zeroed before the launch; bar[] is the grid barrier
   const int* blk_row;          // [G+1] row range of CTA b
   const int* blk_slot;         // [G+1] its partial-sum slots
@@ -311,42 +317,49 @@ struct FusedArgs {
 
 __host__ __device__ constexpr size_t align16(size_t x) { return (x + 15) / 16 * 16; }
 
-// Dynamic shared memory of the fused cycle: basis slice [m+1][S], w [S] (FP64), partial-sum
-// slots [slots][B].
+// Dynamic shared memory of the fused solve: the triangular factor R [m][m] and the product of
+// the Givens rotations Q^T [m+1][m+1] (FP64), basis slice [m+1][S] (TV), w [S] (TV), r [S]
+// (FP64), partial-sum slots [slots][B] (FP64-sized: the residual's operator application uses
+// them in FP64, the Arnoldi steps' in TV).
 template <typename TV>
 __host__ __device__ constexpr size_t fused_smem(int m, int max_rows, int max_slots, int B) {
-  return align16(static_cast<size_t>(m + 1) * max_rows * B * sizeof(TV)) +
+  return align16(static_cast<size_t>(m) * m * sizeof(double)) +
+         align16(static_cast<size_t>(m + 1) * (m + 1) * sizeof(double)) +
+         align16(static_cast<size_t>(m + 1) * max_rows * B * sizeof(TV)) +
+         align16(static_cast<size_t>(max_rows) * B * sizeof(TV)) +
          align16(static_cast<size_t>(max_rows) * B * sizeof(double)) +
-         static_cast<size_t>(max_slots) * B * sizeof(TV);
+         static_cast<size_t>(max_slots) * B * sizeof(double);
 }
 
-// Grid-wide barrier for a cooperative launch (all CTAs resident): arrival counter plus a
-// generation word; bounded wait.  Returns false once any CTA has timed out.
-__device__ bool grid_sync(unsigned* bar) {
+// Grid-wide barrier for a cooperative launch (all CTAs resident).  bar[0] counts arrivals
+// over the whole launch (zeroed before it): thread 0 adds one with release semantics and
+// polls, with acquire semantics, until the count reaches (barriers passed) x gridDim.x --
+// one atomic per CTA, no reset.  The wait is bounded (~2^31 cycles); a CTA that gives up
+// sets bar[2], and every CTA then leaves this and every later barrier with false.
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void red_release_gpu(unsigned* p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ bool grid_sync(unsigned* bar, unsigned& target) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
-    volatile unsigned* gen = bar + 1;
-    volatile unsigned* flag = bar + 2;
-    int ok = *flag == 0u;
+    int ok = ld_acquire_gpu(bar + 2) == 0u;
     if (ok) {
-      const unsigned g0 = *gen;
-      __threadfence();
-      if (atomicAdd(bar, 1u) == gridDim.x - 1) {
-        atomicExch(bar, 0u);
-        __threadfence();
-        atomicAdd(bar + 1, 1u);
-      } else {
-        const long long t0 = clock64();
-        while (*gen == g0) {
-          if (*flag != 0u || clock64() - t0 > (1LL << 31)) {
-            atomicExch(bar + 2, 1u);
-            ok = 0;
-            break;
-          }
+      target += gridDim.x;
+      red_release_gpu(bar, 1u);
+      const long long t0 = clock64();
+      while (ld_acquire_gpu(bar) < target) {
+        if (ld_acquire_gpu(bar + 2) != 0u || clock64() - t0 > (1LL << 31)) {
+          atomicExch(bar + 2, 1u);
+          ok = 0;
+          break;
         }
       }
-      __threadfence();
     }
     s_ok = ok;
   }
@@ -355,35 +368,38 @@ __device__ bool grid_sync(unsigned* bar) {
 }
 
 // Sum over the CTA of one value per thread, fixed order; the result goes to every thread.
-__device__ double fz_block_sum(double v) {
-  __shared__ double red[kFzWarps];
-  __shared__ double total;
+template <typename T>
+__device__ T fz_block_sum(T v) {
+  __shared__ T red[kFzWarps];
+  __shared__ T total;
   for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double s = 0.0;
+    T s = T(0);
     for (int q = 0; q < kFzWarps; ++q) s += red[q];
     total = s;
   }
   __syncthreads();
-  const double r = total;
+  const T r = total;
   __syncthreads();
   return r;
 }
 
 // Warp sum, fixed order (every lane gets the total).
-__device__ __forceinline__ double fz_warp_sum(double v) {
+template <typename T>
+__device__ __forceinline__ T fz_warp_sum(T v) {
   for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
   return v;
 }
 
 // s_out[k] = sum over the grid's CTAs of partial[k * G + q], k < nk: one warp per row k, its
 // lanes adding q = lane, lane + 32, ...; every CTA computes the same values in the same order.
-__device__ void sum_partials(const double* partial, int nk, double* s_out) {
+template <typename T>
+__device__ void sum_partials(const T* partial, int nk, T* s_out) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, G = gridDim.x;
   for (int k = warp; k < nk; k += kFzWarps) {
-    double acc = 0.0;
+    T acc = T(0);
     for (int q = lane; q < G; q += 32) acc += __ldcg(partial + static_cast<long long>(k) * G + q);
     acc = fz_warp_sum(acc);
     if (lane == 0) s_out[k] = acc;
@@ -391,174 +407,281 @@ __device__ void sum_partials(const double* partial, int nk, double* s_out) {
   __syncthreads();
 }
 
+// A f over the CTA's rows into the partial-sum slots: warp items [it0, it1).
+template <typename T, int P, int MAXO>
+__device__ __forceinline__ void apply_items(const ApplyArgs<T>& a, const T* f, const FzItem* items, int it0, int it1,
+                                            int slot0, T* slots, int lane) {
+  for (int it = it0; it < it1; ++it) {
+    const FzItem t = items[it];
+    small_chunk<T, P, MAXO, sizeof(T) == 4>(a, f, t.q0, t.q0 + t.len, lane, slots + (t.slot - slot0) * a.B);
+  }
+}
+// Output o of row `row`: its slots added in slot order.
+template <typename T>
+__device__ __forceinline__ T slot_sum(const T* slots, const int* row_slot, int row, int slot0, int o, int B) {
+  const int s0 = row_slot[row] - slot0, s1 = row_slot[row + 1] - slot0;
+  T ax = T(0);
+  for (int q = s0; q < s1; ++q) ax += slots[q * B + o];
+  return ax;
+}
+
+// The Krylov vectors' arithmetic (w, the dot products and their sums, the orthogonalisation
+// updates, V y) runs in TV, the basis precision: FP32 for the mixed solver, on the FP32 pipes,
+// FP64 for the FP64 solver.  The outer residual, x, and the Givens/triangular recurrences
+// are FP64 in both.
 template <typename TV, int P, int MAXO>
-__global__ void __launch_bounds__(kFzThreads, 1) k_gmres_fused(const __grid_constant__ FusedArgs<TV> c) {
-  constexpr bool KAHAN = sizeof(TV) == 4;
+__global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constant__ FusedArgs<TV> c) {
   extern __shared__ __align__(16) unsigned char fz_smem[];
-  __shared__ double s_h[kMaxRestart], s_h2[kMaxRestart + 1], s_cs[kMaxRestart], s_sn[kMaxRestart],
-      s_g[kMaxRestart + 1], s_hc[kMaxRestart + 1];
-  __shared__ double s_hn2, s_inv, s_resid;
+  __shared__ TV s_h[kMaxRestart], s_h2[kMaxRestart + 1], s_yt[kMaxRestart];
+  __shared__ double s_g[kMaxRestart + 1], s_hc[kMaxRestart + 1], s_rc[kMaxRestart + 1], s_y[kMaxRestart];
+  __shared__ TV s_hn2;
+  __shared__ double s_inv, s_hn, s_sum, s_c, s_s;
   __shared__ int s_done, s_need;
   const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int B = c.a.B, m = c.m;
   const long long ldv = c.ldv;
   const int r0 = c.blk_row[b], r1 = c.blk_row[b + 1];
-  const int S = (r1 - r0) * B;                      // this CTA's elements
+  const int S = (r1 - r0) * B;  // this CTA's elements
   const long long i0 = static_cast<long long>(r0) * B;
   const int Smax = c.max_rows * B;
-  TV* Vs = reinterpret_cast<TV*>(fz_smem);          // [m+1][Smax]
-  double* ws = reinterpret_cast<double*>(fz_smem + align16(static_cast<size_t>(m + 1) * Smax * sizeof(TV)));
-  TV* slots = reinterpret_cast<TV*>(reinterpret_cast<unsigned char*>(ws) + align16(static_cast<size_t>(Smax) * sizeof(double)));
+  unsigned char* sp = fz_smem;
+  double* s_R = reinterpret_cast<double*>(sp);  // [m][m]: R(i, j) at i * m + j, i <= j
+  sp += align16(static_cast<size_t>(m) * m * sizeof(double));
+  double* s_Q = reinterpret_cast<double*>(sp);  // [m+1][m+1]: Q^T = G_{j-1} ... G_0
+  sp += align16(static_cast<size_t>(m + 1) * (m + 1) * sizeof(double));
+  TV* Vs = reinterpret_cast<TV*>(sp);  // [m+1][Smax]
+  sp += align16(static_cast<size_t>(m + 1) * Smax * sizeof(TV));
+  TV* ws = reinterpret_cast<TV*>(sp);
+  sp += align16(static_cast<size_t>(Smax) * sizeof(TV));
+  double* rs = reinterpret_cast<double*>(sp);
+  sp += align16(static_cast<size_t>(Smax) * sizeof(double));
+  TV* slots = reinterpret_cast<TV*>(sp);
+  double* slots64 = reinterpret_cast<double*>(sp);
   const int slot0 = c.blk_slot[b];
-  double* part1 = c.partial;
-  double* part2 = c.partial + static_cast<long long>(m) * G;
-  double* partn = c.partial + (2LL * m + 1) * G;
+  TV* pv = reinterpret_cast<TV*>(c.partial);  // rows of TV partials
+  TV* part1 = pv;
+  TV* part2 = pv + static_cast<long long>(m) * G;
+  TV* partg = pv + (2LL * m + 1) * G;
+  double* partn = c.partial + (2LL * m + 1) * G;  // FP64 norms of b and r
   unsigned* bar = c.state->bar;
-  {  // v_0 = r0 / beta
-    const double ib = 1.0 / c.beta;
-    for (int e = tid; e < S; e += kFzThreads) {
-      const TV v = static_cast<TV>(c.r0[i0 + e] * ib);
-      Vs[e] = v;
-      c.V[i0 + e] = v;
-    }
-  }
-  if (tid == 0) {
-    for (int k = 0; k <= m; ++k) s_g[k] = 0.0;
-    s_g[0] = c.beta;
-  }
+  unsigned bar_target = 0;  // arrivals expected at the next barrier (thread 0)
   const int it0 = c.warp_item[b * kFzWarps + warp], it1 = c.warp_item[b * kFzWarps + warp + 1];
-  int kdone = 0;
-  double resid = c.beta;
-  bool ok = grid_sync(bar);
-  for (int j = 0; j < m && ok; ++j) {
-    const TV* Vj = Vs + j * Smax;
-    // 1. A v_j for the CTA's rows, w = v_j - dt A v_j, pass-1 partial dots
+  const TV dtv = static_cast<TV>(c.dt);
+  {  // ||b||
+    double acc = 0.0;
+    for (int e = tid; e < S; e += kFzThreads) acc = fma(c.rhs[i0 + e], c.rhs[i0 + e], acc);
+    acc = fz_block_sum(acc);
+    if (tid == 0) partn[b] = acc;
+  }
+  bool ok = grid_sync(bar, bar_target);
+  double bnorm = 0.0;
+  if (ok) {
+    sum_partials(partn, 1, &s_sum);
+    bnorm = sqrt(s_sum);
+  }
+  int outer = 0, inner = 0, converged = 0;
+  double rel = 1.0;
+  for (; ok; ++outer) {
+    // ---- r = b - (x - dt A x) in FP64 and ||r|| ----
+    apply_items<double, P, MAXO>(c.a64, c.x, c.items, it0, it1, slot0, slots64, lane);
+    __syncthreads();
     {
-      const TV* f = c.V + j * ldv;
-      for (int it = it0; it < it1; ++it) {
-        const FzItem t = c.items[it];
-        small_chunk<TV, P, MAXO, KAHAN>(c.a, f, t.q0, t.q0 + t.len, lane, slots + (t.slot - slot0) * B);
+      double acc = 0.0;
+      for (int e = tid; e < S; e += kFzThreads) {
+        const int r = e / B;
+        const double ax = slot_sum(slots64, c.row_slot, r0 + r, slot0, e - r * B, B);
+        const double rv = c.rhs[i0 + e] - (c.x[i0 + e] - c.dt * ax);
+        rs[e] = rv;
+        acc = fma(rv, rv, acc);
       }
-    }
-    __syncthreads();
-    for (int e = tid; e < S; e += kFzThreads) {
-      const int r = e / B, o = e - r * B;
-      const int s0 = c.row_slot[r0 + r] - slot0, s1 = c.row_slot[r0 + r + 1] - slot0;
-      TV ax = TV(0);
-      for (int q = s0; q < s1; ++q) ax += slots[q * B + o];
-      ws[e] = static_cast<double>(Vj[e]) - c.dt * static_cast<double>(ax);
-    }
-    __syncthreads();
-    for (int k = warp; k <= j; k += kFzWarps) {
-      const TV* vk = Vs + k * Smax;
-      double acc = 0.0;
-      for (int e = lane; e < S; e += 32) acc = fma(ws[e], static_cast<double>(vk[e]), acc);
-      acc = fz_warp_sum(acc);
-      if (lane == 0) part1[static_cast<long long>(k) * G + b] = acc;
-    }
-    if (!(ok = grid_sync(bar))) break;
-    // 2. h; w -= V h; pass-2 partial dots and ||w||^2
-    sum_partials(part1, j + 1, s_h);
-    for (int e = tid; e < S; e += kFzThreads) {
-      double acc = ws[e];
-      for (int k = 0; k <= j; ++k) acc = fma(-s_h[k], static_cast<double>(Vs[k * Smax + e]), acc);
-      ws[e] = acc;
-    }
-    __syncthreads();
-    for (int k = warp; k <= j + 1; k += kFzWarps) {
-      double acc = 0.0;
-      if (k <= j) {
-        const TV* vk = Vs + k * Smax;
-        for (int e = lane; e < S; e += 32) acc = fma(ws[e], static_cast<double>(vk[e]), acc);
-      } else {
-        for (int e = lane; e < S; e += 32) acc = fma(ws[e], ws[e], acc);
-      }
-      acc = fz_warp_sum(acc);
-      if (lane == 0) part2[static_cast<long long>(k) * G + b] = acc;
-    }
-    if (!(ok = grid_sync(bar))) break;
-    // 3. h2; w -= V h2; ||w||; Givens; v_{j+1}
-    sum_partials(part2, j + 2, s_h2);
-    for (int e = tid; e < S; e += kFzThreads) {
-      double acc = ws[e];
-      for (int k = 0; k <= j; ++k) acc = fma(-s_h2[k], static_cast<double>(Vs[k * Smax + e]), acc);
-      ws[e] = acc;
-    }
-    if (tid == 0) {
-      double h2sq = 0.0;
-      for (int k = 0; k <= j; ++k) h2sq = fma(s_h2[k], s_h2[k], h2sq);
-      const double nw2 = s_h2[j + 1];
-      s_hn2 = nw2 - h2sq;
-      s_need = h2sq <= 1e-2 * nw2 ? 0 : 1;
-    }
-    __syncthreads();
-    if (s_need) {  // the same decision in every CTA: explicit ||w||^2
-      double acc = 0.0;
-      for (int e = tid; e < S; e += kFzThreads) acc = fma(ws[e], ws[e], acc);
       acc = fz_block_sum(acc);
       if (tid == 0) partn[b] = acc;
-      if (!(ok = grid_sync(bar))) break;
-      sum_partials(partn, 1, &s_hn2);
     }
-    if (tid == 0) {
-      const double hn = sqrt(fmax(s_hn2, 0.0));
-      for (int k = 0; k <= j; ++k) s_hc[k] = s_h[k] + s_h2[k];
-      s_hc[j + 1] = hn;
-      for (int i = 0; i < j; ++i) {
-        const double t = s_cs[i] * s_hc[i] + s_sn[i] * s_hc[i + 1];
-        s_hc[i + 1] = -s_sn[i] * s_hc[i] + s_cs[i] * s_hc[i + 1];
-        s_hc[i] = t;
+    if (!(ok = grid_sync(bar, bar_target))) break;
+    sum_partials(partn, 1, &s_sum);
+    const double rn = sqrt(s_sum);
+    rel = bnorm > 0 ? rn / bnorm : rn;
+    if (rn <= c.tol * bnorm || rn == 0.0) {
+      converged = 1;
+      break;
+    }
+    if (outer == c.max_outer) break;
+    // inner target: a fixed relative reduction (the TV operator limits what is attainable)
+    const double target = fmax(c.tol * bnorm, rn * c.inner_reduction);
+    // ---- one GMRES(m) cycle on (I - dt A) delta = r, x += delta ----
+    {
+      const double ib = 1.0 / rn;
+      for (int e = tid; e < S; e += kFzThreads) {
+        const TV v = static_cast<TV>(rs[e] * ib);
+        Vs[e] = v;
+        c.V[i0 + e] = v;
       }
-      const double den = hypot(s_hc[j], s_hc[j + 1]);
-      const double cc = den > 0 ? s_hc[j] / den : 1.0, sv = den > 0 ? s_hc[j + 1] / den : 0.0;
-      s_cs[j] = cc;
-      s_sn[j] = sv;
-      s_hc[j] = den;
-      const double gj = s_g[j];
-      s_g[j + 1] = -sv * gj;
-      s_g[j] = cc * gj;
-      if (b == 0)
-        for (int i = 0; i <= j; ++i) c.H[static_cast<long long>(i) * m + j] = s_hc[i];
-      const double rr = fabs(sv * gj);
-      s_done = (rr <= c.target || hn == 0.0 || j + 1 == m) ? 1 : 0;
-      s_inv = hn > 0 ? 1.0 / hn : 0.0;
-      s_resid = rr;
+    }
+    for (int q = tid; q < (m + 1) * (m + 1); q += kFzThreads) s_Q[q] = q == 0 ? 1.0 : 0.0;
+    if (tid == 0) {
+      for (int k = 0; k <= m; ++k) s_g[k] = 0.0;
+      s_g[0] = rn;
+    }
+    if (!(ok = grid_sync(bar, bar_target))) break;
+    int kdone = 0;
+    for (int j = 0; j < m; ++j) {
+      const TV* Vj = Vs + j * Smax;
+      // 1. A v_j for the CTA's rows, w = v_j - dt A v_j, pass-1 partial dots
+      apply_items<TV, P, MAXO>(c.a, c.V + j * ldv, c.items, it0, it1, slot0, slots, lane);
+      __syncthreads();
+      for (int e = tid; e < S; e += kFzThreads) {
+        const int r = e / B;
+        const TV ax = slot_sum(slots, c.row_slot, r0 + r, slot0, e - r * B, B);
+        ws[e] = fma(-dtv, ax, Vj[e]);
+      }
+      __syncthreads();
+      for (int k = warp; k <= j; k += kFzWarps) {
+        const TV* vk = Vs + k * Smax;
+        TV acc = TV(0);
+        for (int e = lane; e < S; e += 32) acc = fma(ws[e], vk[e], acc);
+        acc = fz_warp_sum(acc);
+        if (lane == 0) part1[static_cast<long long>(k) * G + b] = acc;
+      }
+      if (!(ok = grid_sync(bar, bar_target))) break;
+      // 2. h; w -= V h; pass-2 partial dots and ||w||^2
+      sum_partials(part1, j + 1, s_h);
+      for (int e = tid; e < S; e += kFzThreads) {
+        TV acc = ws[e];
+        for (int k = 0; k <= j; ++k) acc = fma(-s_h[k], Vs[k * Smax + e], acc);
+        ws[e] = acc;
+      }
+      __syncthreads();
+      for (int k = warp; k <= j + 1; k += kFzWarps) {
+        TV acc = TV(0);
+        if (k <= j) {
+          const TV* vk = Vs + k * Smax;
+          for (int e = lane; e < S; e += 32) acc = fma(ws[e], vk[e], acc);
+        } else {
+          for (int e = lane; e < S; e += 32) acc = fma(ws[e], ws[e], acc);
+        }
+        acc = fz_warp_sum(acc);
+        if (lane == 0) part2[static_cast<long long>(k) * G + b] = acc;
+      }
+      if (!(ok = grid_sync(bar, bar_target))) break;
+      // 3. h2; w -= V h2; ||w||; Givens; v_{j+1}
+      sum_partials(part2, j + 2, s_h2);
+      for (int e = tid; e < S; e += kFzThreads) {
+        TV acc = ws[e];
+        for (int k = 0; k <= j; ++k) acc = fma(-s_h2[k], Vs[k * Smax + e], acc);
+        ws[e] = acc;
+      }
+      for (int k = tid; k <= j; k += kFzThreads) s_hc[k] = static_cast<double>(s_h[k]) + static_cast<double>(s_h2[k]);
+      if (warp == 0) {  // ||w||^2 = ||w_before||^2 - ||h2||^2 unless that cancels badly
+        TV h2sq = TV(0);
+        for (int k = lane; k <= j; k += 32) h2sq = fma(s_h2[k], s_h2[k], h2sq);
+        h2sq = fz_warp_sum(h2sq);
+        const TV nw2 = s_h2[j + 1];
+        if (lane == 0) {
+          s_hn2 = nw2 - h2sq;
+          s_need = h2sq <= TV(1e-2) * nw2 ? 0 : 1;
+        }
+      }
+      __syncthreads();
+      if (s_need) {  // the same decision in every CTA: explicit ||w||^2
+        TV acc = TV(0);
+        for (int e = tid; e < S; e += kFzThreads) acc = fma(ws[e], ws[e], acc);
+        acc = fz_block_sum(acc);
+        if (tid == 0) partg[b] = acc;
+        if (!(ok = grid_sync(bar, bar_target))) break;
+        sum_partials(partg, 1, &s_hn2);
+      }
+      // earlier rotations on the new column as one product with Q^T (groups of 8 lanes per
+      // row, fixed order): FP64 latency is long here, so no serial chain over the rotations
+      {
+        const int sub = lane >> 3, l8 = lane & 7;
+        for (int i0w = warp * 4; i0w <= j; i0w += kFzWarps * 4) {  // warp-uniform trip count
+          const int i = i0w + sub;
+          double acc = 0.0;
+          if (i <= j) {
+            const double* qrow = s_Q + i * (m + 1);
+            for (int k = l8; k <= j; k += 8) acc = fma(qrow[k], s_hc[k], acc);
+          }
+          for (int off = 4; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+          if (l8 == 0 && i <= j) s_rc[i] = acc;
+        }
+        if (tid == kFzThreads - 1) {  // ||w|| and 1 / ||w||, alongside
+          const double hn2 = fmax(static_cast<double>(s_hn2), 0.0);
+          const double inv = hn2 > 0 ? rsqrt(hn2) : 0.0;
+          s_inv = inv;
+          s_hn = hn2 * inv;
+        }
+      }
+      __syncthreads();
+      if (tid == 0) {  // the new rotation from (r_j, ||w||)
+        const double rj = s_rc[j], hn = s_hn;
+        const double den2 = fma(rj, rj, hn * hn);
+        const double rd = den2 > 0 ? rsqrt(den2) : 0.0;
+        const double cc = den2 > 0 ? rj * rd : 1.0, sv = den2 > 0 ? hn * rd : 0.0;
+        s_c = cc;
+        s_s = sv;
+        s_rc[j] = den2 * rd;
+        const double gj = s_g[j];
+        s_g[j + 1] = -sv * gj;
+        s_g[j] = cc * gj;
+        s_done = (fabs(sv * gj) <= target || hn == 0.0 || j + 1 == m) ? 1 : 0;
+      }
+      __syncthreads();
+      {  // R(:, j), and rows j, j+1 of Q^T rotated
+        const double cc = s_c, sv = s_s;
+        for (int i = tid; i <= j; i += kFzThreads) s_R[i * m + j] = s_rc[i];
+        for (int k = tid; k <= j + 1; k += kFzThreads) {
+          const double old = k <= j ? s_Q[j * (m + 1) + k] : 0.0;
+          const double e = k == j + 1 ? 1.0 : 0.0;
+          s_Q[j * (m + 1) + k] = fma(cc, old, sv * e);
+          s_Q[(j + 1) * (m + 1) + k] = fma(-sv, old, cc * e);
+        }
+      }
+      kdone = j + 1;
+      if (s_done) break;  // the same decision in every CTA
+      {
+        const TV inv = static_cast<TV>(s_inv);
+        TV* Vn = Vs + (j + 1) * Smax;
+        TV* Vg = c.V + (j + 1) * ldv + i0;
+        for (int e = tid; e < S; e += kFzThreads) {
+          const TV v = ws[e] * inv;
+          Vn[e] = v;
+          Vg[e] = v;
+        }
+      }
+      if (!(ok = grid_sync(bar, bar_target))) break;
+    }
+    if (!ok) break;
+    // ---- y = R \ g by warp 0 (column sweep), x += V y over the CTA's slice ----
+    __syncthreads();
+    if (warp == 0) {
+      for (int q = lane; q < kdone; q += 32) {
+        s_y[q] = s_g[q];
+        s_hc[q] = 1.0 / s_R[q * m + q];
+      }
+      __syncwarp();
+      for (int i = kdone - 1; i >= 0; --i) {
+        const double yi = s_y[i] * s_hc[i];
+        __syncwarp();
+        for (int q = lane; q < i; q += 32) s_y[q] = fma(-s_R[q * m + i], yi, s_y[q]);
+        if (lane == 0) s_y[i] = yi;
+        __syncwarp();
+      }
+      for (int q = lane; q < kdone; q += 32) s_yt[q] = static_cast<TV>(s_y[q]);
     }
     __syncthreads();
-    kdone = j + 1;
-    resid = s_resid;
-    if (s_done) break;  // the same decision in every CTA
-    {
-      const double inv = s_inv;
-      TV* Vn = Vs + (j + 1) * Smax;
-      TV* Vg = c.V + (j + 1) * ldv + i0;
-      for (int e = tid; e < S; e += kFzThreads) {
-        const TV v = static_cast<TV>(ws[e] * inv);
-        Vn[e] = v;
-        Vg[e] = v;
-      }
-    }
-    if (!(ok = grid_sync(bar))) break;
-  }
-  // y = H(1:k,1:k) \ g(1:k) (CTA 0), then x += V y (every CTA, its own elements)
-  if (ok && b == 0 && tid == 0) {
-    for (int i = kdone - 1; i >= 0; --i) {
-      double acc = s_g[i];
-      for (int q = i + 1; q < kdone; ++q) acc -= c.H[static_cast<long long>(i) * m + q] * c.yv[q];
-      c.yv[i] = acc / c.H[static_cast<long long>(i) * m + i];
-    }
-  }
-  if (ok) ok = grid_sync(bar);
-  if (ok) {
     for (int e = tid; e < S; e += kFzThreads) {
-      double acc = c.x64[i0 + e];
-      for (int k = 0; k < kdone; ++k) acc = fma(__ldcg(c.yv + k), static_cast<double>(Vs[k * Smax + e]), acc);
-      c.x64[i0 + e] = acc;
+      TV d = TV(0);
+      for (int k = 0; k < kdone; ++k) d = fma(s_yt[k], Vs[k * Smax + e], d);
+      c.x[i0 + e] += static_cast<double>(d);
     }
+    inner += kdone;
+    if (!(ok = grid_sync(bar, bar_target))) break;  // x complete before the next residual
   }
   if (b == 0 && tid == 0) {
-    c.state->kdone = kdone;
-    c.state->resid = resid;
+    c.state->outer = outer;
+    c.state->inner = inner;
+    c.state->converged = converged;
+    c.state->rel = rel;
     c.state->done = 1;
   }
 }
@@ -627,9 +750,10 @@ double host_norm(const double* d_partial, int nb, cudaStream_t s, asg_status* st
   return std::sqrt(acc);
 }
 
-// Schedule of the fused cycle for a small-block plan, built once per plan: G CTAs (at most
-// one per SM and one per row, about one per 64 work entries), contiguous row ranges balanced
-// by work entries plus a per-row share for the vector work; each CTA's rows are cut into
+// Schedule of the fused solve for a small-block plan, built once per plan: at most G0 CTAs (G0:
+// the SM count, the row count and one per 64 work entries, whichever is least), contiguous
+// row ranges minimising the largest cost (work entries plus a per-row share for the vector
+// work); each CTA's rows are cut into
 // chunks of at most max(8, E_b / (4 W)) entries (E_b: the CTA's entries, W: warps per CTA),
 // and the chunks go to the warps longest first, each to the least-loaded warp.
 asg_status fused_schedule(asg_plan* p) {
@@ -640,21 +764,45 @@ asg_status fused_schedule(asg_plan* p) {
   const int N = p->N, B = p->B, W = asg::kFzWarps;
   const std::vector<long long>& rp = p->row_ptr;
   const long long E = rp[N];
-  const int G = static_cast<int>(std::max<long long>(
+  const int G0 = static_cast<int>(std::max<long long>(
       1, std::min<long long>({static_cast<long long>(nsm), static_cast<long long>(N), (E + 63) / 64})));
+  // contiguous row ranges with the smallest largest cost (a row costs its entries plus a share
+  // for the vector work): bisection on the cap, ranges filled greedily
   const double rowc = 1.0 + B / 4.0;
-  std::vector<double> pre(N + 1, 0.0);
-  for (int r = 0; r < N; ++r) pre[r + 1] = pre[r] + static_cast<double>(rp[r + 1] - rp[r]) + rowc;
-  std::vector<int> blk_row(G + 1, 0), blk_slot(G + 1, 0), row_slot(N + 1, 0), warp_item(static_cast<size_t>(G) * W + 1, 0);
-  blk_row[G] = N;
-  for (int b = 1; b < G; ++b) {
-    const double target = pre[N] * b / G;
-    int r = static_cast<int>(std::lower_bound(pre.begin(), pre.end(), target) - pre.begin());
-    if (r > 0 && target - pre[r - 1] < pre[r] - target) --r;
-    r = std::max(r, blk_row[b - 1] + 1);
-    r = std::min(r, N - (G - b));
-    blk_row[b] = r;
+  std::vector<double> cost(N);
+  double lo = 0.0, hi = 0.0;
+  for (int r = 0; r < N; ++r) {
+    cost[r] = static_cast<double>(rp[r + 1] - rp[r]) + rowc;
+    lo = std::max(lo, cost[r]);
+    hi += cost[r];
   }
+  lo = std::max(lo, hi / G0);
+  auto fill = [&](double cap, std::vector<int>* starts) {
+    int parts = 1;
+    double acc = 0.0;
+    if (starts) starts->assign(1, 0);
+    for (int r = 0; r < N; ++r) {
+      if (acc > 0.0 && acc + cost[r] > cap) {
+        ++parts;
+        acc = 0.0;
+        if (starts) starts->push_back(r);
+      }
+      acc += cost[r];
+    }
+    return parts;
+  };
+  for (int it = 0; it < 60 && hi - lo > 0.5; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (fill(mid, nullptr) <= G0)
+      hi = mid;
+    else
+      lo = mid;
+  }
+  std::vector<int> blk_row;
+  fill(hi, &blk_row);
+  const int G = static_cast<int>(blk_row.size());
+  blk_row.push_back(N);
+  std::vector<int> blk_slot(G + 1, 0), row_slot(N + 1, 0), warp_item(static_cast<size_t>(G) * W + 1, 0);
   std::vector<asg::FzItem> items;
   int slot = 0, max_rows = 0, max_slots = 0;
   for (int b = 0; b < G; ++b) {
@@ -712,20 +860,28 @@ asg_status fused_schedule(asg_plan* p) {
   return ASG_OK;
 }
 
-// The fused cycle (one cooperative launch) for plans on the small-block single-mode kernel
-// with deg 2..4 whose per-CTA slices fit in shared memory; *used = false when the plan does
-// not qualify (the caller then runs the kernel-per-phase cycle).
+// The fused solve (one cooperative launch) for plans on the small-block single-mode kernel
+// with deg 2..4 whose per-CTA slices fit in shared memory.
 template <typename TV, int P, int MAXO>
 cudaError_t launch_fused(const asg::FusedArgs<TV>& c, int G, size_t smem, cudaStream_t s) {
-  auto kern = asg::k_gmres_fused<TV, P, MAXO>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
-  if (e != cudaSuccess) return e;
-  int dev = 0, nsm = 0, coop = 0, per_sm = 0;
-  if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-  if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-  if ((e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev)) != cudaSuccess) return e;
-  if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, asg::kFzThreads, smem)) != cudaSuccess) return e;
-  if (!coop || static_cast<long long>(per_sm) * nsm < G) return cudaErrorNotSupported;
+  auto kern = asg::k_be_fused<TV, P, MAXO>;
+  // the shared-memory limit, co-residency and cooperative-launch support, queried once per
+  // instantiation and shared-memory size
+  static size_t checked_smem = 0;
+  static long long resident = 0;
+  cudaError_t e = cudaSuccess;
+  if (smem != checked_smem) {
+    if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem))) != cudaSuccess)
+      return e;
+    int dev = 0, nsm = 0, coop = 0, per_sm = 0;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev)) != cudaSuccess) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, asg::kFzThreads, smem)) != cudaSuccess) return e;
+    resident = coop ? static_cast<long long>(per_sm) * nsm : 0;
+    checked_smem = smem;
+  }
+  if (resident < G) return cudaErrorNotSupported;
   void* args[] = {const_cast<asg::FusedArgs<TV>*>(&c)};
   return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(kern), dim3(G), dim3(asg::kFzThreads), args, smem, s);
 }
@@ -741,15 +897,17 @@ cudaError_t launch_fused_p(const asg::FusedArgs<TV>& c, int G, size_t smem, cuda
 
 constexpr size_t kFusedSmemLimit = 200 * 1024;
 
+// The whole solve as one launch when the plan qualifies (*used = true; one synchronisation
+// to read the result); *used = false otherwise (the caller runs the host-driven solve).
 template <typename TV>
-asg_status gmres_cycle_fused(asg_plan* plan, long long n, double dt, double beta, const double* r0, double* x64,
-                             int m, double rtol_abs, unsigned char* base, const GmresLayout& L, cudaStream_t s,
-                             int* iters, double* resid, bool* used) {
+asg_status be_solve_fused(asg_plan* plan, long long n, double dt, const double* b, double* x, const asg_gmres_opts* o,
+                          asg_gmres_info* info, unsigned char* base, const GmresLayout& L, cudaStream_t s, bool* used) {
   *used = false;
   asg::FusedArgs<TV> c{};
-  if (!asg::small_plan_args<TV>(plan, &c.a) || c.a.B > 256) return ASG_OK;
+  if (!asg::small_plan_args<TV>(plan, &c.a) || !asg::small_plan_args<double>(plan, &c.a64) || c.a.B > 256) return ASG_OK;
   const int P = c.a.D >= 2 ? c.a.stride[c.a.D - 2] : c.a.B;
   if (P < 2 || P > 4) return ASG_OK;
+  const int m = o->restart;
   asg_status st = fused_schedule(plan);
   if (st) return st;
   const int G = plan->fz_G;
@@ -758,15 +916,14 @@ asg_status gmres_cycle_fused(asg_plan* plan, long long n, double dt, double beta
   c.n = n;
   c.ldv = basis_ld(n);
   c.dt = dt;
-  c.target = rtol_abs;
-  c.beta = beta;
+  c.tol = o->tol;
+  c.inner_reduction = o->inner_reduction;
   c.m = m;
+  c.max_outer = o->max_outer;
   c.V = reinterpret_cast<TV*>(base + L.v);
   c.partial = reinterpret_cast<double*>(base + L.partial);
-  c.H = reinterpret_cast<double*>(base + L.hh);
-  c.yv = reinterpret_cast<double*>(base + L.y);
-  c.r0 = r0;
-  c.x64 = x64;
+  c.rhs = b;
+  c.x = x;
   c.state = reinterpret_cast<asg::GmresState*>(base + L.state);
   const int* fz = plan->d_fz_int;
   c.blk_row = fz;
@@ -782,25 +939,33 @@ asg_status gmres_cycle_fused(asg_plan* plan, long long n, double dt, double beta
                            : launch_fused_p<TV, 4>(c, G, smem, s);
   if (e == cudaErrorNotSupported) {
     cudaGetLastError();
-    return ASG_OK;  // the CTAs cannot all be resident: the caller runs the per-phase cycle
+    return ASG_OK;  // the CTAs cannot all be resident: the caller runs the host-driven solve
   }
-  if (e != cudaSuccess) return asg::cuda_fail(e, "fused gmres cycle");
+  if (e != cudaSuccess) return asg::cuda_fail(e, "fused backward-Euler solve");
   *used = true;
   asg::GmresState hs{};
   ASG_CUDA(cudaMemcpyAsync(&hs, c.state, sizeof(hs), cudaMemcpyDeviceToHost, s));
   ASG_CUDA(cudaStreamSynchronize(s));
-  if (hs.bar[2]) return fail(ASG_ERR_TIMEOUT, "fused gmres cycle: grid barrier wait gave up (%d CTAs)", G);
-  *iters = hs.kdone;
-  *resid = hs.resid;
+  if (hs.bar[2]) return fail(ASG_ERR_TIMEOUT, "fused backward-Euler solve: grid barrier wait gave up (%d CTAs)", G);
+  if (info) {
+    asg_gmres_info inf{};
+    inf.outer_iters = hs.outer;
+    inf.inner_iters = hs.inner;
+    inf.converged = hs.converged;
+    inf.rel_residual = hs.rel;
+    *info = inf;
+  }
   return ASG_OK;
 }
 
-// One GMRES(m) cycle on (I - dt A) delta = r0 (r0 FP64), adding delta to x64 in FP64.  TV is
-// the basis and operator-application precision.  Stops early when the residual estimate
-// drops to rtol_abs.  *iters = Arnoldi steps taken, *resid = final residual estimate.
+// One GMRES(m) cycle on (I - dt A) delta = r0 (r0 FP64, beta = ||r0||), adding delta to x64
+// in FP64.  TV is the basis and operator-application precision.  Stops early when the
+// residual estimate drops to rtol_abs.  *iters = Arnoldi steps taken, *resid = final residual
+// estimate.
 template <typename TV>
-asg_status gmres_cycle(asg_plan* plan, long long n, double dt, const double* r0, double* x64, int m, double rtol_abs,
-                       unsigned char* base, const GmresLayout& L, cudaStream_t s, int* iters, double* resid) {
+asg_status gmres_cycle(asg_plan* plan, long long n, double dt, const double* r0, double beta, double* x64, int m,
+                       double rtol_abs, unsigned char* base, const GmresLayout& L, cudaStream_t s, int* iters,
+                       double* resid) {
   TV* V = reinterpret_cast<TV*>(base + L.v);
   const long long ldv = basis_ld(n);
   double* w = reinterpret_cast<double*>(base + L.w);
@@ -809,17 +974,10 @@ asg_status gmres_cycle(asg_plan* plan, long long n, double dt, const double* r0,
   double* y_dev = reinterpret_cast<double*>(base + L.y);
   double* partial = reinterpret_cast<double*>(base + L.partial);
   const int gr = asg::grid_for(n);
-  asg_status st = ASG_OK;
   *iters = 0;
   const int nb = asg::red_blocks(n);
-  asg::k_norm2<<<nb, asg::kRedThreads, 0, s>>>(n, r0, partial);
-  const double beta = host_norm(partial, nb, s, &st);
-  if (st) return st;
   *resid = beta;
   if (beta <= rtol_abs || beta == 0.0) return ASG_OK;
-  bool fused = false;
-  st = gmres_cycle_fused<TV>(plan, n, dt, beta, r0, x64, m, rtol_abs, base, L, s, iters, resid, &fused);
-  if (st || fused) return st;
   asg::k_store_basis<TV><<<gr, 256, 0, s>>>(n, 1.0 / beta, r0, V);
   double* hcol = reinterpret_cast<double*>(base + L.hcol);
   double* H = reinterpret_cast<double*>(base + L.hh);
@@ -884,6 +1042,8 @@ asg_status be_solve(asg_plan* p, double dt, const double* b, double* x, const as
   double* partial = reinterpret_cast<double*>(base + L.partial);
   const int gr = asg::grid_for(n);
   asg_status st = ASG_OK;
+  bool used = false;
+  if ((st = be_solve_fused<TV>(p, n, dt, b, x, o, info, base, L, s, &used)) || used) return st;
   const int nb = asg::red_blocks(n);
   asg::k_norm2<<<nb, asg::kRedThreads, 0, s>>>(n, b, partial);
   const double bnorm = host_norm(partial, nb, s, &st);
@@ -908,7 +1068,7 @@ asg_status be_solve(asg_plan* p, double dt, const double* b, double* x, const as
     const double target = std::max(o->tol * bnorm, rn * o->inner_reduction);
     int it = 0;
     double est = 0.0;
-    if ((st = gmres_cycle<TV>(p, n, dt, r, x, m, target, base, L, s, &it, &est))) return st;
+    if ((st = gmres_cycle<TV>(p, n, dt, r, rn, x, m, target, base, L, s, &it, &est))) return st;
     inf.inner_iters += it;
   }
   if (info) *info = inf;
