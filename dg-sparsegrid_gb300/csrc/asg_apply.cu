@@ -171,7 +171,8 @@ __global__ void __launch_bounds__(128) k_single_small(ApplyArgs<T> a) {
   const int lane = threadIdx.x & 31;
   const int warp = threadIdx.x >> 5;
   const int wpb = blockDim.x >> 5;
-  for (int row = blockIdx.x * wpb + warp; row < a.N; row += gridDim.x * wpb) small_row<T, P, MAXO, KAHAN>(a, row, lane);
+  const SmallLane<MAXO> sl = small_lane<T, P, MAXO>(a, lane);
+  for (int row = blockIdx.x * wpb + warp; row < a.N; row += gridDim.x * wpb) small_row<T, P, MAXO, KAHAN>(a, row, sl);
 }
 
 // ---------------------------------------------------------------------------------------

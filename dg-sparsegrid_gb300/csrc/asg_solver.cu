@@ -274,26 +274,28 @@ __global__ void k_sol_update_g(long long n, const double* __restrict__ y, const 
 // Fused backward-Euler solve for plans on the small-block single-mode kernel: one cooperative
 // launch solves (I - dt A) x = b -- the FP64 outer residuals, their norms and the stopping
 // test, and every restarted GMRES(m) cycle on the correction (basis and operator in TV).  CTA
-// b owns a contiguous range of element rows (balanced by work entries) and keeps its slice
-// of the Krylov basis and of w in shared memory, so everything but the operator applications
-// and the grid-wide sums stays on chip.  A restart: r = b - (x - dt A x) in FP64 for the
-// CTA's rows and ||r|| (one grid barrier), the stopping test, v_0 = r / ||r|| (one barrier),
-// then per Arnoldi step:
-//   1. A v_j for the CTA's rows (the rows' entries cut into chunks over the warps, chunk sums
-//      added per row in a fixed order; v_j read from the global basis copy),
-//      w = v_j - dt A v_j, first Gram-Schmidt pass's partial dots          -> grid barrier
-//   2. h = grid sums, w -= V h, second pass's partial dots and ||w||^2    -> grid barrier
-//   3. h2 = grid sums, w -= V h2, ||w||^2 = ||w_before||^2 - ||h2||^2 (an explicit sum, with
-//      one more barrier, when ||h2||^2 > 1e-2 ||w_before||^2), the Givens step, v_{j+1} =
-//      w / ||w|| into shared memory and the global copy                    -> grid barrier
-// and after the last step R y = g (every CTA holds the same R and g) and x += V y over the
-// CTA's slice (one barrier before the next residual).  Every CTA reduces the same partials
-// in the same order and runs the same recurrences, so all take the same decisions.
-// Fixed-order reductions: bitwise reproducible.  Grid barrier waits are bounded (~2^31
-// cycles): on expiry the kernel records the timeout and returns.
+// b owns a contiguous range of element rows (balanced by work entries) and keeps its slices
+// of the Krylov basis V and of Z = (I - dt A) V in shared memory, so everything but the
+// operator applications and the grid-wide sums stays on chip.  A restart: r = b - (x - dt A x)
+// in FP64 for the CTA's rows and ||r|| (one grid barrier), the stopping test, v_0 = r / ||r||
+// published (one barrier) and Z_0; then per Arnoldi step, with w = Z_j:
+//   1. first Gram-Schmidt pass's partial dots <w, v_k>                     -> grid barrier
+//   2. h = grid sums, w' = w - V h (published), second pass's partial dots and ||w'||^2
+//                                                                          -> grid barrier
+//   3. h2 = grid sums, ||w||^2 = ||w'||^2 - ||h2||^2 (an explicit sum, with one more barrier,
+//      when ||h2||^2 > 1e-2 ||w'||^2), the Givens step, v_{j+1} = (w' - V h2) / ||w||, and
+//      (I - dt A) w' for the CTA's rows (the rows' entries cut into chunks over the warps,
+//      chunk sums added per row in a fixed order; w' read from its global copy), giving
+//      Z_{j+1} = ((I - dt A) w' - Z h2) / ||w|| without a barrier to publish v_{j+1};
+// after the last step R y = g (every CTA holds the same R and g) and x += V y over the CTA's
+// slice (one barrier before the next residual).  Every CTA reduces the same partials in the
+// same order and runs the same recurrences, so all take the same decisions.  Fixed-order
+// reductions: bitwise reproducible.  Grid barrier waits are bounded (~2^31 cycles): on
+// expiry the kernel records the timeout and returns.
 // ---------------------------------------------------------------------------------------
 constexpr int kFzThreads = 512;
 constexpr int kFzWarps = kFzThreads / 32;
+constexpr int kFzGivensWarps = 2;  // warps that run the Givens step while the others apply the operator
 
 template <typename TV>
 struct FusedArgs {
@@ -302,7 +304,7 @@ struct FusedArgs {
   long long n, ldv;
   double dt, tol, inner_reduction;
   int m, max_outer;
-  TV* V;                       // global basis copy, read by the operator application
+  TV* V;                       // global copy of the vector the operator is applied to (n values)
   double* partial;             // (2m + 2) rows of gridDim.x CTA partials
   const double* rhs;           // b
   double* x;                   // initial guess in, solution out
@@ -318,14 +320,15 @@ struct FusedArgs {
 __host__ __device__ constexpr size_t align16(size_t x) { return (x + 15) / 16 * 16; }
 
 // Dynamic shared memory of the fused solve: the triangular factor R [m][m] and the product of
-// the Givens rotations Q^T [m+1][m+1] (FP64), basis slice [m+1][S] (TV), w [S] (TV), r [S]
+// the Givens rotations Q^T [m+1][m+1] (FP64), slices of the basis V and of Z = (I - dt A) V
+// [m+1][S] each (TV), w [S] (TV), r [S]
 // (FP64), partial-sum slots [slots][B] (FP64-sized: the residual's operator application uses
 // them in FP64, the Arnoldi steps' in TV).
 template <typename TV>
 __host__ __device__ constexpr size_t fused_smem(int m, int max_rows, int max_slots, int B) {
   return align16(static_cast<size_t>(m) * m * sizeof(double)) +
          align16(static_cast<size_t>(m + 1) * (m + 1) * sizeof(double)) +
-         align16(static_cast<size_t>(m + 1) * max_rows * B * sizeof(TV)) +
+         2 * align16(static_cast<size_t>(m + 1) * max_rows * B * sizeof(TV)) +
          align16(static_cast<size_t>(max_rows) * B * sizeof(TV)) +
          align16(static_cast<size_t>(max_rows) * B * sizeof(double)) +
          static_cast<size_t>(max_slots) * B * sizeof(double);
@@ -407,22 +410,40 @@ __device__ void sum_partials(const T* partial, int nk, T* s_out) {
   __syncthreads();
 }
 
+// Barrier of the Givens warps only (named barrier 1).
+__device__ __forceinline__ void givens_sync() {
+  asm volatile("bar.sync 1, %0;" ::"r"(32 * kFzGivensWarps) : "memory");
+}
+
 // A f over the CTA's rows into the partial-sum slots: warp items [it0, it1).
 template <typename T, int P, int MAXO>
 __device__ __forceinline__ void apply_items(const ApplyArgs<T>& a, const T* f, const FzItem* items, int it0, int it1,
-                                            int slot0, T* slots, int lane) {
+                                            int slot0, T* slots, const SmallLane<MAXO>& sl) {
   for (int it = it0; it < it1; ++it) {
     const FzItem t = items[it];
-    small_chunk<T, P, MAXO, sizeof(T) == 4>(a, f, t.q0, t.q0 + t.len, lane, slots + (t.slot - slot0) * a.B);
+    small_chunk<T, P, MAXO, sizeof(T) == 4>(a, f, t.q0, t.q0 + t.len, sl, slots + (t.slot - slot0) * a.B);
   }
 }
-// Output o of row `row`: its slots added in slot order.
+// ax[e] = the slots of e's row added at output e % B, for the CTA's S elements: a team of
+// `team` lanes per element (a power of two up to 32, larger when the CTA has few elements --
+// long rows have many slots), lane k adding slots k, k + team, ..., then a shuffle tree
+// inside the team.  Fixed order; ends with a CTA barrier.
 template <typename T>
-__device__ __forceinline__ T slot_sum(const T* slots, const int* row_slot, int row, int slot0, int o, int B) {
-  const int s0 = row_slot[row] - slot0, s1 = row_slot[row + 1] - slot0;
-  T ax = T(0);
-  for (int q = s0; q < s1; ++q) ax += slots[q * B + o];
-  return ax;
+__device__ __forceinline__ void slot_reduce(const T* slots, const int* row_slot, int r0, int slot0, int S, int B,
+                                            int team, T* ax) {
+  const int lg = __ffs(team) - 1;
+  for (int base = 0; base < S * team; base += kFzThreads) {  // the same trip count in every thread
+    const int t = base + threadIdx.x, e = t >> lg, k = t & (team - 1);
+    T acc = T(0);
+    if (e < S) {
+      const int r = e / B, o = e - r * B;
+      const int s0 = row_slot[r0 + r] - slot0, s1 = row_slot[r0 + r + 1] - slot0;
+      for (int q = s0 + k; q < s1; q += team) acc += slots[q * B + o];
+    }
+    for (int off = team >> 1; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+    if (e < S && k == 0) ax[e] = acc;
+  }
+  __syncthreads();
 }
 
 // The Krylov vectors' arithmetic (w, the dot products and their sums, the orthogonalisation
@@ -451,6 +472,8 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
   sp += align16(static_cast<size_t>(m + 1) * (m + 1) * sizeof(double));
   TV* Vs = reinterpret_cast<TV*>(sp);  // [m+1][Smax]
   sp += align16(static_cast<size_t>(m + 1) * Smax * sizeof(TV));
+  TV* Zs = reinterpret_cast<TV*>(sp);  // [m+1][Smax]
+  sp += align16(static_cast<size_t>(m + 1) * Smax * sizeof(TV));
   TV* ws = reinterpret_cast<TV*>(sp);
   sp += align16(static_cast<size_t>(Smax) * sizeof(TV));
   double* rs = reinterpret_cast<double*>(sp);
@@ -467,6 +490,10 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
   unsigned bar_target = 0;  // arrivals expected at the next barrier (thread 0)
   const int it0 = c.warp_item[b * kFzWarps + warp], it1 = c.warp_item[b * kFzWarps + warp + 1];
   const TV dtv = static_cast<TV>(c.dt);
+  const SmallLane<MAXO> sl = small_lane<TV, P, MAXO>(c.a, lane);  // same digits for the FP64 residual
+  int team = 1;  // lanes per element in the slot sums
+  while (team < 32 && 2 * team * S <= kFzThreads) team <<= 1;
+  TV* axs = reinterpret_cast<TV*>(rs);  // A w' for the CTA's rows (rs is free during a cycle)
   {  // ||b||
     double acc = 0.0;
     for (int e = tid; e < S; e += kFzThreads) acc = fma(c.rhs[i0 + e], c.rhs[i0 + e], acc);
@@ -483,14 +510,13 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
   double rel = 1.0;
   for (; ok; ++outer) {
     // ---- r = b - (x - dt A x) in FP64 and ||r|| ----
-    apply_items<double, P, MAXO>(c.a64, c.x, c.items, it0, it1, slot0, slots64, lane);
+    apply_items<double, P, MAXO>(c.a64, c.x, c.items, it0, it1, slot0, slots64, sl);
     __syncthreads();
+    slot_reduce(slots64, c.row_slot, r0, slot0, S, B, team, rs);
     {
       double acc = 0.0;
       for (int e = tid; e < S; e += kFzThreads) {
-        const int r = e / B;
-        const double ax = slot_sum(slots64, c.row_slot, r0 + r, slot0, e - r * B, B);
-        const double rv = c.rhs[i0 + e] - (c.x[i0 + e] - c.dt * ax);
+        const double rv = c.rhs[i0 + e] - (c.x[i0 + e] - c.dt * rs[e]);
         rs[e] = rv;
         acc = fma(rv, rv, acc);
       }
@@ -509,12 +535,16 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
     // inner target: a fixed relative reduction (the TV operator limits what is attainable)
     const double target = fmax(c.tol * bnorm, rn * c.inner_reduction);
     // ---- one GMRES(m) cycle on (I - dt A) delta = r, x += delta ----
+    // Zs[k] = (I - dt A) v_k.  The operator is applied to w' (w after the first Gram-Schmidt
+    // pass, published before the second barrier), and (I - dt A) v_{j+1} =
+    // ((I - dt A) w' - sum_k h2_k Z_k) / ||w|| -- so no barrier only to publish v_{j+1}.
+    TV* W = c.V;  // global copy of the vector the operator is applied to next
     {
       const double ib = 1.0 / rn;
       for (int e = tid; e < S; e += kFzThreads) {
         const TV v = static_cast<TV>(rs[e] * ib);
         Vs[e] = v;
-        c.V[i0 + e] = v;
+        W[i0 + e] = v;
       }
     }
     for (int q = tid; q < (m + 1) * (m + 1); q += kFzThreads) s_Q[q] = q == 0 ? 1.0 : 0.0;
@@ -523,18 +553,18 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
       s_g[0] = rn;
     }
     if (!(ok = grid_sync(bar, bar_target))) break;
+    apply_items<TV, P, MAXO>(c.a, W, c.items, it0, it1, slot0, slots, sl);
+    __syncthreads();
+    slot_reduce(slots, c.row_slot, r0, slot0, S, B, team, axs);
+    for (int e = tid; e < S; e += kFzThreads) {
+      const TV z = fma(-dtv, axs[e], Vs[e]);
+      Zs[e] = z;
+      ws[e] = z;
+    }
+    __syncthreads();
     int kdone = 0;
     for (int j = 0; j < m; ++j) {
-      const TV* Vj = Vs + j * Smax;
-      // 1. A v_j for the CTA's rows, w = v_j - dt A v_j, pass-1 partial dots
-      apply_items<TV, P, MAXO>(c.a, c.V + j * ldv, c.items, it0, it1, slot0, slots, lane);
-      __syncthreads();
-      for (int e = tid; e < S; e += kFzThreads) {
-        const int r = e / B;
-        const TV ax = slot_sum(slots, c.row_slot, r0 + r, slot0, e - r * B, B);
-        ws[e] = fma(-dtv, ax, Vj[e]);
-      }
-      __syncthreads();
+      // 1. w = Z_j (in ws): pass-1 partial dots
       for (int k = warp; k <= j; k += kFzWarps) {
         const TV* vk = Vs + k * Smax;
         TV acc = TV(0);
@@ -543,12 +573,13 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
         if (lane == 0) part1[static_cast<long long>(k) * G + b] = acc;
       }
       if (!(ok = grid_sync(bar, bar_target))) break;
-      // 2. h; w -= V h; pass-2 partial dots and ||w||^2
+      // 2. h; w' = w - V h (published); pass-2 partial dots and ||w'||^2
       sum_partials(part1, j + 1, s_h);
       for (int e = tid; e < S; e += kFzThreads) {
         TV acc = ws[e];
         for (int k = 0; k <= j; ++k) acc = fma(-s_h[k], Vs[k * Smax + e], acc);
         ws[e] = acc;
+        W[i0 + e] = acc;
       }
       __syncthreads();
       for (int k = warp; k <= j + 1; k += kFzWarps) {
@@ -563,15 +594,56 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
         if (lane == 0) part2[static_cast<long long>(k) * G + b] = acc;
       }
       if (!(ok = grid_sync(bar, bar_target))) break;
-      // 3. h2; w -= V h2; ||w||; Givens; v_{j+1}
+      // 3. the Givens warps: h2, ||w|| and the Givens step; the other warps meanwhile apply
+      //    (I - dt A) to w' (read from its global copy) -- the two do not depend on each other
+      auto givens = [&]() {  // run by the Givens warps
+        const int gt = tid;  // 0 .. 32 * kFzGivensWarps - 1
+        // earlier rotations on the new column as one product with Q^T (groups of 8 lanes per
+        // row, fixed order): FP64 latency is long here, so no serial chain over the rotations
+        const int sub = lane >> 3, l8 = lane & 7;
+        for (int i0w = warp * 4; i0w <= j; i0w += kFzGivensWarps * 4) {  // warp-uniform trip count
+          const int i = i0w + sub;
+          double acc = 0.0;
+          if (i <= j) {
+            const double* qrow = s_Q + i * (m + 1);
+            for (int k = l8; k <= j; k += 8) acc = fma(qrow[k], s_hc[k], acc);
+          }
+          for (int off = 4; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
+          if (l8 == 0 && i <= j) s_rc[i] = acc;
+        }
+        if (gt == 32 * kFzGivensWarps - 1) {  // ||w|| and 1 / ||w||, alongside
+          const double hn2 = fmax(static_cast<double>(s_hn2), 0.0);
+          const double inv = hn2 > 0 ? rsqrt(hn2) : 0.0;
+          s_inv = inv;
+          s_hn = hn2 * inv;
+        }
+        givens_sync();
+        if (gt == 0) {  // the new rotation from (r_j, ||w||)
+          const double rj = s_rc[j], hn = s_hn;
+          const double den2 = fma(rj, rj, hn * hn);
+          const double rd = den2 > 0 ? rsqrt(den2) : 0.0;
+          const double cc = den2 > 0 ? rj * rd : 1.0, sv = den2 > 0 ? hn * rd : 0.0;
+          s_c = cc;
+          s_s = sv;
+          s_rc[j] = den2 * rd;
+          const double gj = s_g[j];
+          s_g[j + 1] = -sv * gj;
+          s_g[j] = cc * gj;
+          s_done = (fabs(sv * gj) <= target || hn == 0.0 || j + 1 == m) ? 1 : 0;
+        }
+        givens_sync();
+        const double cc = s_c, sv = s_s;  // R(:, j), and rows j, j+1 of Q^T rotated
+        for (int i = gt; i <= j; i += 32 * kFzGivensWarps) s_R[i * m + j] = s_rc[i];
+        for (int k = gt; k <= j + 1; k += 32 * kFzGivensWarps) {
+          const double old = k <= j ? s_Q[j * (m + 1) + k] : 0.0;
+          const double e = k == j + 1 ? 1.0 : 0.0;
+          s_Q[j * (m + 1) + k] = fma(cc, old, sv * e);
+          s_Q[(j + 1) * (m + 1) + k] = fma(-sv, old, cc * e);
+        }
+      };
       sum_partials(part2, j + 2, s_h2);
-      for (int e = tid; e < S; e += kFzThreads) {
-        TV acc = ws[e];
-        for (int k = 0; k <= j; ++k) acc = fma(-s_h2[k], Vs[k * Smax + e], acc);
-        ws[e] = acc;
-      }
       for (int k = tid; k <= j; k += kFzThreads) s_hc[k] = static_cast<double>(s_h[k]) + static_cast<double>(s_h2[k]);
-      if (warp == 0) {  // ||w||^2 = ||w_before||^2 - ||h2||^2 unless that cancels badly
+      if (warp == 0) {  // ||w||^2 = ||w'||^2 - ||h2||^2 unless that cancels badly
         TV h2sq = TV(0);
         for (int k = lane; k <= j; k += 32) h2sq = fma(s_h2[k], s_h2[k], h2sq);
         h2sq = fz_warp_sum(h2sq);
@@ -582,73 +654,47 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
         }
       }
       __syncthreads();
-      if (s_need) {  // the same decision in every CTA: explicit ||w||^2
+      if (warp < kFzGivensWarps) {
+        if (!s_need) givens();
+      } else {
+        apply_items<TV, P, MAXO>(c.a, W, c.items, it0, it1, slot0, slots, sl);
+      }
+      __syncthreads();
+      if (s_need) {  // the same decision in every CTA: explicit ||w' - V h2||^2, then the Givens step
         TV acc = TV(0);
-        for (int e = tid; e < S; e += kFzThreads) acc = fma(ws[e], ws[e], acc);
+        for (int e = tid; e < S; e += kFzThreads) {
+          TV v = ws[e];
+          for (int k = 0; k <= j; ++k) v = fma(-s_h2[k], Vs[k * Smax + e], v);
+          acc = fma(v, v, acc);
+        }
         acc = fz_block_sum(acc);
         if (tid == 0) partg[b] = acc;
         if (!(ok = grid_sync(bar, bar_target))) break;
         sum_partials(partg, 1, &s_hn2);
-      }
-      // earlier rotations on the new column as one product with Q^T (groups of 8 lanes per
-      // row, fixed order): FP64 latency is long here, so no serial chain over the rotations
-      {
-        const int sub = lane >> 3, l8 = lane & 7;
-        for (int i0w = warp * 4; i0w <= j; i0w += kFzWarps * 4) {  // warp-uniform trip count
-          const int i = i0w + sub;
-          double acc = 0.0;
-          if (i <= j) {
-            const double* qrow = s_Q + i * (m + 1);
-            for (int k = l8; k <= j; k += 8) acc = fma(qrow[k], s_hc[k], acc);
-          }
-          for (int off = 4; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
-          if (l8 == 0 && i <= j) s_rc[i] = acc;
-        }
-        if (tid == kFzThreads - 1) {  // ||w|| and 1 / ||w||, alongside
-          const double hn2 = fmax(static_cast<double>(s_hn2), 0.0);
-          const double inv = hn2 > 0 ? rsqrt(hn2) : 0.0;
-          s_inv = inv;
-          s_hn = hn2 * inv;
-        }
-      }
-      __syncthreads();
-      if (tid == 0) {  // the new rotation from (r_j, ||w||)
-        const double rj = s_rc[j], hn = s_hn;
-        const double den2 = fma(rj, rj, hn * hn);
-        const double rd = den2 > 0 ? rsqrt(den2) : 0.0;
-        const double cc = den2 > 0 ? rj * rd : 1.0, sv = den2 > 0 ? hn * rd : 0.0;
-        s_c = cc;
-        s_s = sv;
-        s_rc[j] = den2 * rd;
-        const double gj = s_g[j];
-        s_g[j + 1] = -sv * gj;
-        s_g[j] = cc * gj;
-        s_done = (fabs(sv * gj) <= target || hn == 0.0 || j + 1 == m) ? 1 : 0;
-      }
-      __syncthreads();
-      {  // R(:, j), and rows j, j+1 of Q^T rotated
-        const double cc = s_c, sv = s_s;
-        for (int i = tid; i <= j; i += kFzThreads) s_R[i * m + j] = s_rc[i];
-        for (int k = tid; k <= j + 1; k += kFzThreads) {
-          const double old = k <= j ? s_Q[j * (m + 1) + k] : 0.0;
-          const double e = k == j + 1 ? 1.0 : 0.0;
-          s_Q[j * (m + 1) + k] = fma(cc, old, sv * e);
-          s_Q[(j + 1) * (m + 1) + k] = fma(-sv, old, cc * e);
-        }
+        if (warp < kFzGivensWarps) givens();
+        __syncthreads();
       }
       kdone = j + 1;
       if (s_done) break;  // the same decision in every CTA
+      slot_reduce(slots, c.row_slot, r0, slot0, S, B, team, axs);
       {
         const TV inv = static_cast<TV>(s_inv);
         TV* Vn = Vs + (j + 1) * Smax;
-        TV* Vg = c.V + (j + 1) * ldv + i0;
+        TV* Zn = Zs + (j + 1) * Smax;
         for (int e = tid; e < S; e += kFzThreads) {
-          const TV v = ws[e] * inv;
-          Vn[e] = v;
-          Vg[e] = v;
+          const TV wp = ws[e];
+          TV v = wp, z = fma(-dtv, axs[e], wp);
+          for (int k = 0; k <= j; ++k) {
+            v = fma(-s_h2[k], Vs[k * Smax + e], v);
+            z = fma(-s_h2[k], Zs[k * Smax + e], z);
+          }
+          Vn[e] = v * inv;
+          z *= inv;
+          Zn[e] = z;
+          ws[e] = z;
         }
       }
-      if (!(ok = grid_sync(bar, bar_target))) break;
+      __syncthreads();
     }
     if (!ok) break;
     // ---- y = R \ g by warp 0 (column sweep), x += V y over the CTA's slice ----
@@ -752,10 +798,10 @@ double host_norm(const double* d_partial, int nb, cudaStream_t s, asg_status* st
 
 // Schedule of the fused solve for a small-block plan, built once per plan: at most G0 CTAs (G0:
 // the SM count, the row count and one per 64 work entries, whichever is least), contiguous
-// row ranges minimising the largest cost (work entries plus a per-row share for the vector
-// work); each CTA's rows are cut into
-// chunks of at most max(8, E_b / (4 W)) entries (E_b: the CTA's entries, W: warps per CTA),
-// and the chunks go to the warps longest first, each to the least-loaded warp.
+// row ranges minimising the largest cost in warp rounds; each CTA's rows are cut into chunks
+// of whole rounds, at most max(2, U_b / (2 Wa)) rounds each (U_b: the CTA's rounds, Wa: its
+// warps that apply the operator -- all but the Givens warps), and the chunks go to those
+// warps longest first, each to the least-loaded one.
 asg_status fused_schedule(asg_plan* p) {
   if (p->fz_G > 0) return ASG_OK;
   int dev = 0, nsm = 0;
@@ -766,13 +812,17 @@ asg_status fused_schedule(asg_plan* p) {
   const long long E = rp[N];
   const int G0 = static_cast<int>(std::max<long long>(
       1, std::min<long long>({static_cast<long long>(nsm), static_cast<long long>(N), (E + 63) / 64})));
-  // contiguous row ranges with the smallest largest cost (a row costs its entries plus a share
-  // for the vector work): bisection on the cap, ranges filled greedily
-  const double rowc = 1.0 + B / 4.0;
+  // A warp retires `unit` entries per round (its lane groups times two entries in flight),
+  // so work is counted in rounds.  Contiguous row ranges with the smallest largest cost (a row
+  // costs its rounds plus one for the vector work): bisection on the cap, greedy fill.
+  int lanes = 1;
+  while (lanes < B && lanes < 32) lanes <<= 1;
+  const long long unit = 2 * (32 / lanes);
+  auto rounds = [&](long long len) { return (len + unit - 1) / unit; };
   std::vector<double> cost(N);
   double lo = 0.0, hi = 0.0;
   for (int r = 0; r < N; ++r) {
-    cost[r] = static_cast<double>(rp[r + 1] - rp[r]) + rowc;
+    cost[r] = static_cast<double>(rounds(rp[r + 1] - rp[r])) + 1.0;
     lo = std::max(lo, cost[r]);
     hi += cost[r];
   }
@@ -807,19 +857,23 @@ asg_status fused_schedule(asg_plan* p) {
   int slot = 0, max_rows = 0, max_slots = 0;
   for (int b = 0; b < G; ++b) {
     const int r0 = blk_row[b], r1 = blk_row[b + 1];
-    const long long Eb = rp[r1] - rp[r0];
-    const long long ch = std::max<long long>(8, (Eb + 4 * W - 1) / (4 * W));
+    long long Ub = 0;  // the CTA's rounds
+    for (int r = r0; r < r1; ++r) Ub += rounds(rp[r + 1] - rp[r]);
+    const long long Wa = W - asg::kFzGivensWarps;  // warps that apply the operator
+    const long long ch = std::max<long long>(2, (Ub + 2 * Wa - 1) / (2 * Wa));  // rounds per chunk
     blk_slot[b] = slot;
     std::vector<asg::FzItem> bi;
     for (int r = r0; r < r1; ++r) {
       row_slot[r] = slot;
-      const long long er = rp[r + 1] - rp[r];
-      const long long nch = (er + ch - 1) / ch;
-      long long q = rp[r];
-      for (long long k = 0; k < nch; ++k) {
-        const long long len = er / nch + (k < er % nch ? 1 : 0);
+      const long long er = rp[r + 1] - rp[r], ur = rounds(er);
+      const long long nch = (ur + ch - 1) / ch;
+      long long q = rp[r], left = er;
+      for (long long k = 0; k < nch; ++k) {  // whole rounds per chunk, the last one takes the rest
+        const long long uk = ur / nch + (k < ur % nch ? 1 : 0);
+        const long long len = std::min(left, uk * unit);
         bi.push_back(asg::FzItem{q, static_cast<int>(len), slot++});
         q += len;
+        left -= len;
       }
     }
     max_rows = std::max(max_rows, r1 - r0);
@@ -830,9 +884,10 @@ asg_status fused_schedule(asg_plan* p) {
     std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return bi[x].len > bi[y].len; });
     std::vector<long long> load(W, 0);
     std::vector<std::vector<asg::FzItem>> per(W);
+    const int w0 = asg::kFzGivensWarps;  // warps 0 .. w0-1 run the Givens step instead
     for (int k : order) {
-      const int w = static_cast<int>(std::min_element(load.begin(), load.end()) - load.begin());
-      load[w] += bi[k].len + 2;
+      const int w = static_cast<int>(std::min_element(load.begin() + w0, load.end()) - load.begin());
+      load[w] += rounds(bi[k].len) + 1;
       per[w].push_back(bi[k]);
     }
     for (int w = 0; w < W; ++w) {
