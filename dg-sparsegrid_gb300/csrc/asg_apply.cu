@@ -175,6 +175,16 @@ __global__ void __launch_bounds__(128) k_single_small(ApplyArgs<T> a) {
   for (int row = blockIdx.x * wpb + warp; row < a.N; row += gridDim.x * wpb) small_row<T, P, MAXO, KAHAN>(a, row, sl);
 }
 
+// Fiber-per-lane variant for P <= 4 (see fiber_entry): one warp per output element.
+template <typename T, int P, int MAXF, bool KAHAN>
+__global__ void __launch_bounds__(128) k_single_fiber(ApplyArgs<T> a) {
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int wpb = blockDim.x >> 5;
+  const FiberLane<MAXF> fl = fiber_lane<T, P, MAXF>(a, lane);
+  for (int row = blockIdx.x * wpb + warp; row < a.N; row += gridDim.x * wpb) fiber_row<T, P, MAXF, KAHAN>(a, row, fl);
+}
+
 // ---------------------------------------------------------------------------------------
 // Chain kernel, one CTA per output element (element blocks up to 4096 values).
 // ---------------------------------------------------------------------------------------
@@ -1325,6 +1335,16 @@ cudaError_t launch_p(const ApplyArgs<T>& a, int kind, cudaStream_t s) {
     if (a.B > 256 || !a.ed) return cudaErrorInvalidValue;
     const int wpb = 4;
     const int grid = (a.N + wpb - 1) / wpb;
+    if constexpr (P <= 4) {
+      const int Lf = a.B / P;
+      if (Lf <= 32)
+        k_single_fiber<T, P, 1, K><<<grid, wpb * 32, 0, s>>>(a);
+      else if (Lf <= 64)
+        k_single_fiber<T, P, 2, K><<<grid, wpb * 32, 0, s>>>(a);
+      else
+        k_single_fiber<T, P, 4, K><<<grid, wpb * 32, 0, s>>>(a);
+      return cudaGetLastError();
+    }
     if (a.B <= 32)
       k_single_small<T, P, 1, K><<<grid, wpb * 32, 0, s>>>(a);
     else if (a.B <= 64)

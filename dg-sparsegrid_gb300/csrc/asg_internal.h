@@ -177,11 +177,11 @@ struct asg_plan {
   int* d_cta_ptr[2] = {nullptr, nullptr};
   int* d_cta_rows[2] = {nullptr, nullptr};
   float* d_ops_pair = nullptr;
-  // fused GMRES cycle (small-block plans, built on first use): contiguous row ranges per CTA
-  // and chunks of their rows' entries per warp
-  int fz_G = 0, fz_max_rows = 0, fz_max_slots = 0;
-  int* d_fz_int = nullptr;           // blk_row[G+1], blk_slot[G+1], row_slot[N+1], warp_item[G*W+1]
-  asg::FzItem* d_fz_items = nullptr;
+  // fused backward-Euler solve (small-block plans, built on first use), per basis precision
+  // (0 FP64, 1 FP32): contiguous row ranges per CTA and chunks of their rows' entries per warp
+  int fz_G[2] = {0, 0}, fz_max_rows[2] = {0, 0}, fz_max_slots[2] = {0, 0};
+  int* d_fz_int[2] = {nullptr, nullptr};  // blk_row[G+1], blk_slot[G+1], row_slot[N+1], warp_item[G*W+1]
+  asg::FzItem* d_fz_items[2] = {nullptr, nullptr};
   int* d_err = nullptr;
   double* d_ops64 = nullptr;
   float* d_ops32 = nullptr;

@@ -74,8 +74,10 @@ void free_device(asg_plan* p) {
     cudaFree(p->d_cta_rows[k]);
   }
   cudaFree(p->d_ops_pair);
-  cudaFree(p->d_fz_int);
-  cudaFree(p->d_fz_items);
+  for (int k = 0; k < 2; ++k) {
+    cudaFree(p->d_fz_int[k]);
+    cudaFree(p->d_fz_items[k]);
+  }
   cudaFree(p->d_err);
   cudaFree(p->d_io);
   if (p->stream) cudaStreamDestroy(p->stream);

@@ -19,8 +19,9 @@ __device__ __forceinline__ void acc_add(T& s, T& c, T v, bool kahan) {
 }
 
 // ---------------------------------------------------------------------------------------
-// Small-block single-mode rows: every term has one applied factor and deg^d <= 256 (the
-// 2-D/3-D configurations).  One warp per output element; the warp's lanes form G groups of
+// Small-block single-mode rows, per-output form (used for P > 4; the fiber form below serves
+// P <= 4): every term has one applied factor and deg^d <= 256.  One warp per output
+// element; the warp's lanes form G groups of
 // L lanes (L = min(32, next power of two >= deg^d)), group g taking the row's entries
 // g, g+G, ...; lane r of a group owns outputs r, r+L, ...  An entry adds, for each owned
 // output o (digit a along the entry's dimension m, stride s), sum_b A[a][b] f_j[o + (b-a) s]:
@@ -159,6 +160,132 @@ __device__ __forceinline__ void small_chunk(const ApplyArgs<T>& a, const T* __re
 template <typename T, int P, int MAXO, bool KAHAN>
 __device__ __forceinline__ void small_row(const ApplyArgs<T>& a, int row, const SmallLane<MAXO>& sl) {
   small_chunk<T, P, MAXO, KAHAN>(a, a.f, a.row_ptr[row], a.row_ptr[row + 1], sl, a.y + static_cast<size_t>(row) * a.B);
+}
+
+// ---------------------------------------------------------------------------------------
+// Fiber-per-lane small-block rows (P <= 4): lane r of a group owns the fibers phi = r,
+// r + 32, ... of the output block along its last dimension (P consecutive values each);
+// Lf = deg^(d-1) fibers per block, Gf = 32 / Lf groups per warp (one when Lf > 32), group g
+// taking the entries g, g + Gf, ...  An entry along dimension m adds to fiber phi
+//   m = d-1:  y[phi P + t] += sum_b A[t][b] f_j[phi P + b]
+//   m < d-1:  y[phi P + t] += sum_b A[a][b] f_j[phi P + t + (b - a) s]   (a: phi's digit m)
+// -- both as acc[t] += sum_b X[t][b] Y[b][t] over a P x P register tile, X the rows
+// (t or a) of the P x P block and Y the input fibers (the one fiber at phi P, or the fibers at
+// phi P + (b - a) s), loaded as P-wide vectors, so entries of any dimension run the same
+// instructions (no divergence).  Group sums (Kahan-compensated in FP32 where asked) are added
+// across groups by a fixed shuffle tree: deterministic.
+// ---------------------------------------------------------------------------------------
+template <int MAXF>
+struct FiberLane {
+  int Lf, Gf, g, r;  // fibers per block, groups per warp, this lane's group and rank
+  unsigned dig[MAXF];  // base-P digits of each owned fiber's first output, 4 bits per dim
+};
+
+template <typename T, int P, int MAXF>
+__device__ __forceinline__ FiberLane<MAXF> fiber_lane(const ApplyArgs<T>& a, int lane) {
+  FiberLane<MAXF> fl;
+  const int Lf = a.B / P;
+  fl.Lf = Lf;
+  fl.Gf = Lf <= 32 ? 32 / Lf : 1;
+  fl.g = Lf <= 32 ? lane / Lf : 0;
+  fl.r = Lf <= 32 ? lane - fl.g * Lf : lane;
+#pragma unroll
+  for (int q = 0; q < MAXF; ++q) {
+    const int phi = fl.r + 32 * q;
+    unsigned d = 0u;
+    if (phi < Lf)
+      for (int m = 0; m < a.D; ++m) d |= static_cast<unsigned>((phi * P / a.stride[m]) % P) << (4 * m);
+    fl.dig[q] = d;
+  }
+  return fl;
+}
+
+template <typename T, int P>
+__device__ __forceinline__ void store_prow(T* __restrict__ p, const T (&v)[P]) {
+  if constexpr (sizeof(T) == 4 && P == 4) {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  } else if constexpr (sizeof(T) == 8 && P == 4) {
+    reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
+    reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
+  } else if constexpr (sizeof(T) == 4 && P == 2) {
+    *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
+  } else if constexpr (sizeof(T) == 8 && P == 2) {
+    *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+  } else {
+#pragma unroll
+    for (int t = 0; t < P; ++t) p[t] = v[t];
+  }
+}
+
+// Adds one entry to the lane's fibers (acc[q][t]); lanes of groups past Gf and fibers past
+// Lf add nothing.
+template <typename T, int P, int MAXF, bool KAHAN>
+__device__ __forceinline__ void fiber_entry(const ApplyArgs<T>& a, const T* __restrict__ f, const EntryDesc& e,
+                                            const FiberLane<MAXF>& fl, T (&acc)[MAXF][P], T (&cmp)[MAXF][P]) {
+  const int B = a.B;
+  const bool last = e.m == a.D - 1;
+  const int s = a.stride[e.m];
+  const int sh = 4 * e.m;
+  const T* fj = f + static_cast<size_t>(e.j) * B;
+  const T* Ab = a.ops + e.aoff;
+#pragma unroll
+  for (int q = 0; q < MAXF; ++q) {
+    const int phi = fl.r + 32 * q;
+    if (phi < fl.Lf) {
+      const int ad = static_cast<int>((fl.dig[q] >> sh) & 15u);
+      T X[P][P], Y[P][P];
+#pragma unroll
+      for (int t = 0; t < P; ++t) load_prow<T, P>(Ab + (last ? t : ad) * P, X[t]);
+#pragma unroll
+      for (int b = 0; b < P; ++b) load_prow<T, P>(fj + phi * P + (last ? 0 : (b - ad) * s), Y[b]);
+#pragma unroll
+      for (int t = 0; t < P; ++t) {
+        T v = T(0);
+#pragma unroll
+        for (int b = 0; b < P; ++b) v = fma(X[t][b], last ? Y[0][b] : Y[b][t], v);
+        acc_add(acc[q][t], cmp[q][t], v, KAHAN);
+      }
+    }
+  }
+}
+
+// Entries [q0, q1) of one row by one warp, reading the input vector f; the block's B sums go
+// to out[0..B) (16-byte aligned for P = 4).
+template <typename T, int P, int MAXF, bool KAHAN>
+__device__ __forceinline__ void fiber_chunk(const ApplyArgs<T>& a, const T* __restrict__ f, long long q0, long long q1,
+                                            const FiberLane<MAXF>& fl, T* out) {
+  T acc[MAXF][P], cmp[MAXF][P];
+#pragma unroll
+  for (int q = 0; q < MAXF; ++q)
+#pragma unroll
+    for (int t = 0; t < P; ++t) acc[q][t] = cmp[q][t] = T(0);
+  if (fl.g < fl.Gf)
+    for (long long q = q0 + fl.g; q < q1; q += fl.Gf) fiber_entry<T, P, MAXF, KAHAN>(a, f, a.ed[q], fl, acc, cmp);
+  // fixed-order tree across the groups: group g takes group g + off's sums (g % 2off == 0)
+  const int lane = fl.g * fl.Lf + fl.r;
+  for (int off = 1; off < fl.Gf; off <<= 1) {
+    const bool take = (fl.g % (2 * off)) == 0 && fl.g + off < fl.Gf;
+    const int src = take ? lane + off * fl.Lf : lane;
+#pragma unroll
+    for (int q = 0; q < MAXF; ++q)
+#pragma unroll
+      for (int t = 0; t < P; ++t) {
+        const T o = __shfl_sync(0xffffffffu, acc[q][t], src);
+        if (take) acc[q][t] += o;
+      }
+  }
+  if (fl.g == 0) {
+#pragma unroll
+    for (int q = 0; q < MAXF; ++q) {
+      const int phi = fl.r + 32 * q;
+      if (phi < fl.Lf) store_prow<T, P>(out + phi * P, acc[q]);
+    }
+  }
+}
+
+template <typename T, int P, int MAXF, bool KAHAN>
+__device__ __forceinline__ void fiber_row(const ApplyArgs<T>& a, int row, const FiberLane<MAXF>& fl) {
+  fiber_chunk<T, P, MAXF, KAHAN>(a, a.f, a.row_ptr[row], a.row_ptr[row + 1], fl, a.y + static_cast<size_t>(row) * a.B);
 }
 
 }  // namespace

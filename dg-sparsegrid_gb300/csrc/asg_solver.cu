@@ -7,6 +7,7 @@
 //                    solution update and every Arnoldi dot product and norm.
 // All reductions are two-pass and fixed-order, so results are bitwise reproducible.
 #include <algorithm>
+#include <type_traits>
 #include <cmath>
 #include <vector>
 
@@ -320,14 +321,14 @@ struct FusedArgs {
 __host__ __device__ constexpr size_t align16(size_t x) { return (x + 15) / 16 * 16; }
 
 // Dynamic shared memory of the fused solve: the triangular factor R [m][m] and the product of
-// the Givens rotations Q^T [m+1][m+1] (FP64), slices of the basis V and of Z = (I - dt A) V
+// the Givens rotations Q^T [m+1][m+1] (TV), slices of the basis V and of Z = (I - dt A) V
 // [m+1][S] each (TV), w [S] (TV), r [S]
 // (FP64), partial-sum slots [slots][B] (FP64-sized: the residual's operator application uses
 // them in FP64, the Arnoldi steps' in TV).
 template <typename TV>
 __host__ __device__ constexpr size_t fused_smem(int m, int max_rows, int max_slots, int B) {
-  return align16(static_cast<size_t>(m) * m * sizeof(double)) +
-         align16(static_cast<size_t>(m + 1) * (m + 1) * sizeof(double)) +
+  return align16(static_cast<size_t>(m) * m * sizeof(TV)) +
+         align16(static_cast<size_t>(m + 1) * (m + 1) * sizeof(TV)) +
          2 * align16(static_cast<size_t>(m + 1) * max_rows * B * sizeof(TV)) +
          align16(static_cast<size_t>(max_rows) * B * sizeof(TV)) +
          align16(static_cast<size_t>(max_rows) * B * sizeof(double)) +
@@ -410,18 +411,30 @@ __device__ void sum_partials(const T* partial, int nk, T* s_out) {
   __syncthreads();
 }
 
+__device__ __forceinline__ float fz_rsqrt(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double fz_rsqrt(double x) { return rsqrt(x); }
+
 // Barrier of the Givens warps only (named barrier 1).
 __device__ __forceinline__ void givens_sync() {
   asm volatile("bar.sync 1, %0;" ::"r"(32 * kFzGivensWarps) : "memory");
 }
 
-// A f over the CTA's rows into the partial-sum slots: warp items [it0, it1).
+// A f over the CTA's rows into the partial-sum slots: warp items [it0, it1).  Plain sums (no
+// compensation): inside the solver the FP64 outer residual corrects the rounding.
+template <typename T, int P, int MAXF>
+__device__ __forceinline__ void apply_items(const ApplyArgs<T>& a, const T* f, const FzItem* items, int it0, int it1,
+                                            int slot0, T* slots, const FiberLane<MAXF>& fl) {
+  for (int it = it0; it < it1; ++it) {
+    const FzItem t = items[it];
+    fiber_chunk<T, P, MAXF, false>(a, f, t.q0, t.q0 + t.len, fl, slots + (t.slot - slot0) * a.B);
+  }
+}
 template <typename T, int P, int MAXO>
 __device__ __forceinline__ void apply_items(const ApplyArgs<T>& a, const T* f, const FzItem* items, int it0, int it1,
                                             int slot0, T* slots, const SmallLane<MAXO>& sl) {
   for (int it = it0; it < it1; ++it) {
     const FzItem t = items[it];
-    small_chunk<T, P, MAXO, sizeof(T) == 4>(a, f, t.q0, t.q0 + t.len, sl, slots + (t.slot - slot0) * a.B);
+    small_chunk<T, P, MAXO, false>(a, f, t.q0, t.q0 + t.len, sl, slots + (t.slot - slot0) * a.B);
   }
 }
 // ax[e] = the slots of e's row added at output e % B, for the CTA's S elements: a team of
@@ -446,17 +459,19 @@ __device__ __forceinline__ void slot_reduce(const T* slots, const int* row_slot,
   __syncthreads();
 }
 
-// The Krylov vectors' arithmetic (w, the dot products and their sums, the orthogonalisation
-// updates, V y) runs in TV, the basis precision: FP32 for the mixed solver, on the FP32 pipes,
-// FP64 for the FP64 solver.  The outer residual, x, and the Givens/triangular recurrences
-// are FP64 in both.
+// The inner GMRES cycle (w, the dot products and their sums, the orthogonalisation updates,
+// the Givens rotations, R y = g and V y) runs in TV, the basis precision: FP32 for the mixed
+// solver, on the FP32 pipes (an FP32 basis holds the Arnoldi relation to FP32 accuracy
+// only, and the FP64 outer residual corrects), FP64 for the FP64 solver.  The outer
+// residual, its norm, b and x are FP64 in both.
 template <typename TV, int P, int MAXO>
 __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constant__ FusedArgs<TV> c) {
   extern __shared__ __align__(16) unsigned char fz_smem[];
-  __shared__ TV s_h[kMaxRestart], s_h2[kMaxRestart + 1], s_yt[kMaxRestart];
-  __shared__ double s_g[kMaxRestart + 1], s_hc[kMaxRestart + 1], s_rc[kMaxRestart + 1], s_y[kMaxRestart];
+  __shared__ TV s_h[kMaxRestart], s_h2[kMaxRestart + 1];
+  __shared__ TV s_g[kMaxRestart + 1], s_hc[kMaxRestart + 1], s_rc[kMaxRestart + 1], s_y[kMaxRestart];
   __shared__ TV s_hn2;
-  __shared__ double s_inv, s_hn, s_sum, s_c, s_s;
+  __shared__ TV s_inv, s_hn, s_c, s_s;
+  __shared__ double s_sum;
   __shared__ int s_done, s_need;
   const int G = gridDim.x, b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int B = c.a.B, m = c.m;
@@ -466,10 +481,10 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
   const long long i0 = static_cast<long long>(r0) * B;
   const int Smax = c.max_rows * B;
   unsigned char* sp = fz_smem;
-  double* s_R = reinterpret_cast<double*>(sp);  // [m][m]: R(i, j) at i * m + j, i <= j
-  sp += align16(static_cast<size_t>(m) * m * sizeof(double));
-  double* s_Q = reinterpret_cast<double*>(sp);  // [m+1][m+1]: Q^T = G_{j-1} ... G_0
-  sp += align16(static_cast<size_t>(m + 1) * (m + 1) * sizeof(double));
+  TV* s_R = reinterpret_cast<TV*>(sp);  // [m][m]: R(i, j) at i * m + j, i <= j
+  sp += align16(static_cast<size_t>(m) * m * sizeof(TV));
+  TV* s_Q = reinterpret_cast<TV*>(sp);  // [m+1][m+1]: Q^T = G_{j-1} ... G_0
+  sp += align16(static_cast<size_t>(m + 1) * (m + 1) * sizeof(TV));
   TV* Vs = reinterpret_cast<TV*>(sp);  // [m+1][Smax]
   sp += align16(static_cast<size_t>(m + 1) * Smax * sizeof(TV));
   TV* Zs = reinterpret_cast<TV*>(sp);  // [m+1][Smax]
@@ -490,7 +505,14 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
   unsigned bar_target = 0;  // arrivals expected at the next barrier (thread 0)
   const int it0 = c.warp_item[b * kFzWarps + warp], it1 = c.warp_item[b * kFzWarps + warp + 1];
   const TV dtv = static_cast<TV>(c.dt);
-  const SmallLane<MAXO> sl = small_lane<TV, P, MAXO>(c.a, lane);  // same digits for the FP64 residual
+  // row routine: fiber rows for FP32, per-output rows for FP64 (the faster of the two in each
+  // precision); the FP64 residual uses the same lane layout
+  using Lane = typename std::conditional<sizeof(TV) == 4, FiberLane<MAXO>, SmallLane<MAXO>>::type;
+  Lane sl;
+  if constexpr (sizeof(TV) == 4)
+    sl = fiber_lane<TV, P, MAXO>(c.a, lane);
+  else
+    sl = small_lane<TV, P, MAXO>(c.a, lane);
   int team = 1;  // lanes per element in the slot sums
   while (team < 32 && 2 * team * S <= kFzThreads) team <<= 1;
   TV* axs = reinterpret_cast<TV*>(rs);  // A w' for the CTA's rows (rs is free during a cycle)
@@ -533,7 +555,7 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
     }
     if (outer == c.max_outer) break;
     // inner target: a fixed relative reduction (the TV operator limits what is attainable)
-    const double target = fmax(c.tol * bnorm, rn * c.inner_reduction);
+    const TV target = static_cast<TV>(fmax(c.tol * bnorm, rn * c.inner_reduction));
     // ---- one GMRES(m) cycle on (I - dt A) delta = r, x += delta ----
     // Zs[k] = (I - dt A) v_k.  The operator is applied to w' (w after the first Gram-Schmidt
     // pass, published before the second barrier), and (I - dt A) v_{j+1} =
@@ -547,10 +569,10 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
         W[i0 + e] = v;
       }
     }
-    for (int q = tid; q < (m + 1) * (m + 1); q += kFzThreads) s_Q[q] = q == 0 ? 1.0 : 0.0;
+    for (int q = tid; q < (m + 1) * (m + 1); q += kFzThreads) s_Q[q] = q == 0 ? TV(1) : TV(0);
     if (tid == 0) {
-      for (int k = 0; k <= m; ++k) s_g[k] = 0.0;
-      s_g[0] = rn;
+      for (int k = 0; k <= m; ++k) s_g[k] = TV(0);
+      s_g[0] = static_cast<TV>(rn);
     }
     if (!(ok = grid_sync(bar, bar_target))) break;
     apply_items<TV, P, MAXO>(c.a, W, c.items, it0, it1, slot0, slots, sl);
@@ -603,46 +625,46 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
         const int sub = lane >> 3, l8 = lane & 7;
         for (int i0w = warp * 4; i0w <= j; i0w += kFzGivensWarps * 4) {  // warp-uniform trip count
           const int i = i0w + sub;
-          double acc = 0.0;
+          TV acc = TV(0);
           if (i <= j) {
-            const double* qrow = s_Q + i * (m + 1);
+            const TV* qrow = s_Q + i * (m + 1);
             for (int k = l8; k <= j; k += 8) acc = fma(qrow[k], s_hc[k], acc);
           }
           for (int off = 4; off > 0; off >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, off);
           if (l8 == 0 && i <= j) s_rc[i] = acc;
         }
         if (gt == 32 * kFzGivensWarps - 1) {  // ||w|| and 1 / ||w||, alongside
-          const double hn2 = fmax(static_cast<double>(s_hn2), 0.0);
-          const double inv = hn2 > 0 ? rsqrt(hn2) : 0.0;
+          const TV hn2 = s_hn2 > TV(0) ? s_hn2 : TV(0);
+          const TV inv = hn2 > TV(0) ? fz_rsqrt(hn2) : TV(0);
           s_inv = inv;
           s_hn = hn2 * inv;
         }
         givens_sync();
         if (gt == 0) {  // the new rotation from (r_j, ||w||)
-          const double rj = s_rc[j], hn = s_hn;
-          const double den2 = fma(rj, rj, hn * hn);
-          const double rd = den2 > 0 ? rsqrt(den2) : 0.0;
-          const double cc = den2 > 0 ? rj * rd : 1.0, sv = den2 > 0 ? hn * rd : 0.0;
+          const TV rj = s_rc[j], hn = s_hn;
+          const TV den2 = fma(rj, rj, hn * hn);
+          const TV rd = den2 > TV(0) ? fz_rsqrt(den2) : TV(0);
+          const TV cc = den2 > TV(0) ? rj * rd : TV(1), sv = den2 > TV(0) ? hn * rd : TV(0);
           s_c = cc;
           s_s = sv;
           s_rc[j] = den2 * rd;
-          const double gj = s_g[j];
+          const TV gj = s_g[j];
           s_g[j + 1] = -sv * gj;
           s_g[j] = cc * gj;
-          s_done = (fabs(sv * gj) <= target || hn == 0.0 || j + 1 == m) ? 1 : 0;
+          s_done = (fabs(sv * gj) <= target || hn == TV(0) || j + 1 == m) ? 1 : 0;
         }
         givens_sync();
-        const double cc = s_c, sv = s_s;  // R(:, j), and rows j, j+1 of Q^T rotated
+        const TV cc = s_c, sv = s_s;  // R(:, j), and rows j, j+1 of Q^T rotated
         for (int i = gt; i <= j; i += 32 * kFzGivensWarps) s_R[i * m + j] = s_rc[i];
         for (int k = gt; k <= j + 1; k += 32 * kFzGivensWarps) {
-          const double old = k <= j ? s_Q[j * (m + 1) + k] : 0.0;
-          const double e = k == j + 1 ? 1.0 : 0.0;
+          const TV old = k <= j ? s_Q[j * (m + 1) + k] : TV(0);
+          const TV e = k == j + 1 ? TV(1) : TV(0);
           s_Q[j * (m + 1) + k] = fma(cc, old, sv * e);
           s_Q[(j + 1) * (m + 1) + k] = fma(-sv, old, cc * e);
         }
       };
       sum_partials(part2, j + 2, s_h2);
-      for (int k = tid; k <= j; k += kFzThreads) s_hc[k] = static_cast<double>(s_h[k]) + static_cast<double>(s_h2[k]);
+      for (int k = tid; k <= j; k += kFzThreads) s_hc[k] = s_h[k] + s_h2[k];
       if (warp == 0) {  // ||w||^2 = ||w'||^2 - ||h2||^2 unless that cancels badly
         TV h2sq = TV(0);
         for (int k = lane; k <= j; k += 32) h2sq = fma(s_h2[k], s_h2[k], h2sq);
@@ -678,7 +700,7 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
       if (s_done) break;  // the same decision in every CTA
       slot_reduce(slots, c.row_slot, r0, slot0, S, B, team, axs);
       {
-        const TV inv = static_cast<TV>(s_inv);
+        const TV inv = s_inv;
         TV* Vn = Vs + (j + 1) * Smax;
         TV* Zn = Zs + (j + 1) * Smax;
         for (int e = tid; e < S; e += kFzThreads) {
@@ -702,22 +724,21 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
     if (warp == 0) {
       for (int q = lane; q < kdone; q += 32) {
         s_y[q] = s_g[q];
-        s_hc[q] = 1.0 / s_R[q * m + q];
+        s_hc[q] = TV(1) / s_R[q * m + q];
       }
       __syncwarp();
       for (int i = kdone - 1; i >= 0; --i) {
-        const double yi = s_y[i] * s_hc[i];
+        const TV yi = s_y[i] * s_hc[i];
         __syncwarp();
         for (int q = lane; q < i; q += 32) s_y[q] = fma(-s_R[q * m + i], yi, s_y[q]);
         if (lane == 0) s_y[i] = yi;
         __syncwarp();
       }
-      for (int q = lane; q < kdone; q += 32) s_yt[q] = static_cast<TV>(s_y[q]);
     }
     __syncthreads();
     for (int e = tid; e < S; e += kFzThreads) {
       TV d = TV(0);
-      for (int k = 0; k < kdone; ++k) d = fma(s_yt[k], Vs[k * Smax + e], d);
+      for (int k = 0; k < kdone; ++k) d = fma(s_y[k], Vs[k * Smax + e], d);
       c.x[i0 + e] += static_cast<double>(d);
     }
     inner += kdone;
@@ -802,8 +823,8 @@ double host_norm(const double* d_partial, int nb, cudaStream_t s, asg_status* st
 // of whole rounds, at most max(2, U_b / (2 Wa)) rounds each (U_b: the CTA's rounds, Wa: its
 // warps that apply the operator -- all but the Givens warps), and the chunks go to those
 // warps longest first, each to the least-loaded one.
-asg_status fused_schedule(asg_plan* p) {
-  if (p->fz_G > 0) return ASG_OK;
+asg_status fused_schedule(asg_plan* p, int k) {
+  if (p->fz_G[k] > 0) return ASG_OK;
   int dev = 0, nsm = 0;
   ASG_CUDA(cudaGetDevice(&dev));
   ASG_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -812,12 +833,19 @@ asg_status fused_schedule(asg_plan* p) {
   const long long E = rp[N];
   const int G0 = static_cast<int>(std::max<long long>(
       1, std::min<long long>({static_cast<long long>(nsm), static_cast<long long>(N), (E + 63) / 64})));
-  // A warp retires `unit` entries per round (its lane groups times two entries in flight),
-  // so work is counted in rounds.  Contiguous row ranges with the smallest largest cost (a row
-  // costs its rounds plus one for the vector work): bisection on the cap, greedy fill.
-  int lanes = 1;
-  while (lanes < B && lanes < 32) lanes <<= 1;
-  const long long unit = 2 * (32 / lanes);
+  // A warp retires `unit` entries per round -- FP32 (fiber rows): one per lane group of
+  // deg^(d-1) lanes; FP64 (per-output rows): two per lane group of L >= deg^d lanes -- so work
+  // is counted in rounds.  Contiguous row ranges with the smallest largest cost (a row costs
+  // its rounds plus one for the vector work): bisection on the cap, greedy fill.
+  long long unit = 1;
+  if (k == 1) {
+    const int fibers = B / p->P;
+    unit = fibers <= 32 ? 32 / fibers : 1;
+  } else {
+    int lanes = 1;
+    while (lanes < B && lanes < 32) lanes <<= 1;
+    unit = 2 * (32 / lanes);
+  }
   auto rounds = [&](long long len) { return (len + unit - 1) / unit; };
   std::vector<double> cost(N);
   double lo = 0.0, hi = 0.0;
@@ -903,15 +931,15 @@ asg_status fused_schedule(asg_plan* p) {
   ints.insert(ints.end(), blk_slot.begin(), blk_slot.end());
   ints.insert(ints.end(), row_slot.begin(), row_slot.end());
   ints.insert(ints.end(), warp_item.begin(), warp_item.end());
-  ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_fz_int), ints.size() * sizeof(int)));
-  ASG_CUDA(cudaMemcpy(p->d_fz_int, ints.data(), ints.size() * sizeof(int), cudaMemcpyHostToDevice));
+  ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_fz_int[k]), ints.size() * sizeof(int)));
+  ASG_CUDA(cudaMemcpy(p->d_fz_int[k], ints.data(), ints.size() * sizeof(int), cudaMemcpyHostToDevice));
   if (!items.empty()) {
-    ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_fz_items), items.size() * sizeof(asg::FzItem)));
-    ASG_CUDA(cudaMemcpy(p->d_fz_items, items.data(), items.size() * sizeof(asg::FzItem), cudaMemcpyHostToDevice));
+    ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_fz_items[k]), items.size() * sizeof(asg::FzItem)));
+    ASG_CUDA(cudaMemcpy(p->d_fz_items[k], items.data(), items.size() * sizeof(asg::FzItem), cudaMemcpyHostToDevice));
   }
-  p->fz_max_rows = max_rows;
-  p->fz_max_slots = max_slots;
-  p->fz_G = G;
+  p->fz_max_rows[k] = max_rows;
+  p->fz_max_slots[k] = max_slots;
+  p->fz_G[k] = G;
   return ASG_OK;
 }
 
@@ -943,11 +971,18 @@ cudaError_t launch_fused(const asg::FusedArgs<TV>& c, int G, size_t smem, cudaSt
 
 template <typename TV, int P>
 cudaError_t launch_fused_p(const asg::FusedArgs<TV>& c, int G, size_t smem, cudaStream_t s) {
-  const int B = c.a.B;
-  if (B <= 32) return launch_fused<TV, P, 1>(c, G, smem, s);
-  if (B <= 64) return launch_fused<TV, P, 2>(c, G, smem, s);
-  if (B <= 128) return launch_fused<TV, P, 4>(c, G, smem, s);
-  return launch_fused<TV, P, 8>(c, G, smem, s);
+  // outputs (FP64, per-output rows) or fibers (FP32) per lane
+  const int B = c.a.B, Lf = B / P;
+  if constexpr (sizeof(TV) == 4) {
+    if (Lf <= 32) return launch_fused<TV, P, 1>(c, G, smem, s);
+    if (Lf <= 64) return launch_fused<TV, P, 2>(c, G, smem, s);
+    return launch_fused<TV, P, 4>(c, G, smem, s);
+  } else {
+    if (B <= 32) return launch_fused<TV, P, 1>(c, G, smem, s);
+    if (B <= 64) return launch_fused<TV, P, 2>(c, G, smem, s);
+    if (B <= 128) return launch_fused<TV, P, 4>(c, G, smem, s);
+    return launch_fused<TV, P, 8>(c, G, smem, s);
+  }
 }
 
 constexpr size_t kFusedSmemLimit = 200 * 1024;
@@ -963,10 +998,11 @@ asg_status be_solve_fused(asg_plan* plan, long long n, double dt, const double* 
   const int P = c.a.D >= 2 ? c.a.stride[c.a.D - 2] : c.a.B;
   if (P < 2 || P > 4) return ASG_OK;
   const int m = o->restart;
-  asg_status st = fused_schedule(plan);
+  const int k = sizeof(TV) == 4 ? 1 : 0;
+  asg_status st = fused_schedule(plan, k);
   if (st) return st;
-  const int G = plan->fz_G;
-  const size_t smem = asg::fused_smem<TV>(m, plan->fz_max_rows, plan->fz_max_slots, c.a.B);
+  const int G = plan->fz_G[k];
+  const size_t smem = asg::fused_smem<TV>(m, plan->fz_max_rows[k], plan->fz_max_slots[k], c.a.B);
   if (smem > kFusedSmemLimit) return ASG_OK;
   c.n = n;
   c.ldv = basis_ld(n);
@@ -980,14 +1016,14 @@ asg_status be_solve_fused(asg_plan* plan, long long n, double dt, const double* 
   c.rhs = b;
   c.x = x;
   c.state = reinterpret_cast<asg::GmresState*>(base + L.state);
-  const int* fz = plan->d_fz_int;
+  const int* fz = plan->d_fz_int[k];
   c.blk_row = fz;
   c.blk_slot = fz + (G + 1);
   c.row_slot = fz + 2 * (G + 1);
   c.warp_item = fz + 2 * (G + 1) + (plan->N + 1);
-  c.items = plan->d_fz_items;
-  c.max_rows = plan->fz_max_rows;
-  c.max_slots = plan->fz_max_slots;
+  c.items = plan->d_fz_items[k];
+  c.max_rows = plan->fz_max_rows[k];
+  c.max_slots = plan->fz_max_slots[k];
   ASG_CUDA(cudaMemsetAsync(c.state, 0, sizeof(asg::GmresState), s));
   cudaError_t e = P == 2 ? launch_fused_p<TV, 2>(c, G, smem, s)
                   : P == 3 ? launch_fused_p<TV, 3>(c, G, smem, s)
