@@ -44,8 +44,9 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-rows", type=int, default=48, help="rows in the bounded CPU sample")
     ap.add_argument("--skip-variants", action="store_true")
-    ap.add_argument("--workload", default="continuity6", choices=["continuity6", "batched"],
-                    help="batched: the 256-problem persistent-launch configuration (own JSON line)")
+    ap.add_argument("--workload", default="continuity6", choices=["continuity6", "batched", "implicit"],
+                    help="batched: the 256-problem persistent-launch configuration; implicit: the "
+                         "backward-Euler diffusion2 configuration (each its own JSON line)")
     ap.add_argument("--batch-problems", type=int, default=256,
                     help="batched workload: number of problems drawn (the configuration has 256)")
     ap.add_argument("--batch-max-level", type=int, default=7,
@@ -462,6 +463,28 @@ def run_batched(args, rank, local):
         p.close()
 
 
+def run_implicit(args, rank, local):
+    """The implicit configuration alone (rank 0): diffusion2 SG 8, deg 4, ten backward-Euler
+    steps, mixed and FP64 (see implicit_steps); one JSON line, time per step (lower is
+    better)."""
+    import torch
+
+    if rank != 0:
+        return
+    torch.cuda.set_device(local)
+    out = implicit_steps(torch.device("cuda", local))
+    line = {
+        "metric": "backward-Euler step time, mixed-precision GMRES(30)-IR to 1e-10", "impl": "ours",
+        "value": out["mixed"]["ms_per_step"], "unit": "ms/step", "n_gpus": 1, "steps": 10, "warmup": 1,
+        "ms_per_step": out["mixed"]["ms_per_step"], "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 inner / f64 outer",
+        "data": "synthetic (projection of sin(pi x) sin(pi y) + 1e-3 N(0,1), seed 2)",
+        "config": {"workload": "diffusion2 LDG, SG lev 8, deg 4, dt = h^2, Dirichlet zero", "dof": out["dof"]},
+        "variants": out,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def graph_replay(plan, f, y, stream, n_apply=100, reps=10):
     """n_apply back-to-back applies captured in one CUDA graph (no flush between them: the
     operands stay in L2), replayed reps times; returns microseconds per apply."""
@@ -516,6 +539,9 @@ def main():
         return
     if args.workload == "batched":
         run_batched(args, rank, local)
+        return
+    if args.workload == "implicit":
+        run_implicit(args, rank, local)
         return
     import numpy as np
     import torch
