@@ -142,6 +142,7 @@ SIGNATURES = {
     "asg_be_workspace": (C.c_int, [C.c_void_p, C.POINTER(GmresOpts), C.POINTER(C.c_size_t)]),
     "asg_be_solve": (C.c_int, [C.c_void_p, C.c_double, _P, _P, C.POINTER(GmresOpts), C.POINTER(GmresInfo), _P,
                                C.c_size_t, _P]),
+    "asg_debug_withhold_arrival": (C.c_int, [C.c_int]),
 }
 
 _LIB = None

@@ -316,6 +316,7 @@ struct FusedArgs {
   const int* warp_item;        // [G*W+1] items of warp w of CTA b
   const FzItem* items;
   int max_rows, max_slots;
+  int withhold;                // test hook: barrier at which CTA 0 does not arrive (-1: none)
 };
 
 __host__ __device__ constexpr size_t align16(size_t x) { return (x + 15) / 16 * 16; }
@@ -348,14 +349,14 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
 __device__ __forceinline__ void red_release_gpu(unsigned* p, unsigned v) {
   asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
-__device__ bool grid_sync(unsigned* bar, unsigned& target) {
+__device__ bool grid_sync(unsigned* bar, unsigned& target, bool withhold = false) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = ld_acquire_gpu(bar + 2) == 0u;
     if (ok) {
       target += gridDim.x;
-      red_release_gpu(bar, 1u);
+      if (!withhold) red_release_gpu(bar, 1u);  // withhold: the test hook's missing arrival
       const long long t0 = clock64();
       while (ld_acquire_gpu(bar) < target) {
         if (ld_acquire_gpu(bar + 2) != 0u || clock64() - t0 > (1LL << 31)) {
@@ -503,6 +504,8 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
   double* partn = c.partial + (2LL * m + 1) * G;  // FP64 norms of b and r
   unsigned* bar = c.state->bar;
   unsigned bar_target = 0;  // arrivals expected at the next barrier (thread 0)
+  int bar_count = 0;        // barriers entered (the test hook's index)
+  auto gsync = [&]() { return grid_sync(bar, bar_target, b == 0 && bar_count++ == c.withhold); };
   const int it0 = c.warp_item[b * kFzWarps + warp], it1 = c.warp_item[b * kFzWarps + warp + 1];
   const TV dtv = static_cast<TV>(c.dt);
   // row routine: fiber rows for FP32, per-output rows for FP64 (the faster of the two in each
@@ -522,7 +525,7 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
     acc = fz_block_sum(acc);
     if (tid == 0) partn[b] = acc;
   }
-  bool ok = grid_sync(bar, bar_target);
+  bool ok = gsync();
   double bnorm = 0.0;
   if (ok) {
     sum_partials(partn, 1, &s_sum);
@@ -545,7 +548,7 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
       acc = fz_block_sum(acc);
       if (tid == 0) partn[b] = acc;
     }
-    if (!(ok = grid_sync(bar, bar_target))) break;
+    if (!(ok = gsync())) break;
     sum_partials(partn, 1, &s_sum);
     const double rn = sqrt(s_sum);
     rel = bnorm > 0 ? rn / bnorm : rn;
@@ -574,7 +577,7 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
       for (int k = 0; k <= m; ++k) s_g[k] = TV(0);
       s_g[0] = static_cast<TV>(rn);
     }
-    if (!(ok = grid_sync(bar, bar_target))) break;
+    if (!(ok = gsync())) break;
     apply_items<TV, P, MAXO>(c.a, W, c.items, it0, it1, slot0, slots, sl);
     __syncthreads();
     slot_reduce(slots, c.row_slot, r0, slot0, S, B, team, axs);
@@ -594,7 +597,7 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
         acc = fz_warp_sum(acc);
         if (lane == 0) part1[static_cast<long long>(k) * G + b] = acc;
       }
-      if (!(ok = grid_sync(bar, bar_target))) break;
+      if (!(ok = gsync())) break;
       // 2. h; w' = w - V h (published); pass-2 partial dots and ||w'||^2
       sum_partials(part1, j + 1, s_h);
       for (int e = tid; e < S; e += kFzThreads) {
@@ -615,7 +618,7 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
         acc = fz_warp_sum(acc);
         if (lane == 0) part2[static_cast<long long>(k) * G + b] = acc;
       }
-      if (!(ok = grid_sync(bar, bar_target))) break;
+      if (!(ok = gsync())) break;
       // 3. the Givens warps: h2, ||w|| and the Givens step; the other warps meanwhile apply
       //    (I - dt A) to w' (read from its global copy) -- the two do not depend on each other
       auto givens = [&]() {  // run by the Givens warps
@@ -691,7 +694,7 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
         }
         acc = fz_block_sum(acc);
         if (tid == 0) partg[b] = acc;
-        if (!(ok = grid_sync(bar, bar_target))) break;
+        if (!(ok = gsync())) break;
         sum_partials(partg, 1, &s_hn2);
         if (warp < kFzGivensWarps) givens();
         __syncthreads();
@@ -742,7 +745,7 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
       c.x[i0 + e] += static_cast<double>(d);
     }
     inner += kdone;
-    if (!(ok = grid_sync(bar, bar_target))) break;  // x complete before the next residual
+    if (!(ok = gsync())) break;  // x complete before the next residual
   }
   if (b == 0 && tid == 0) {
     c.state->outer = outer;
@@ -986,6 +989,7 @@ cudaError_t launch_fused_p(const asg::FusedArgs<TV>& c, int G, size_t smem, cuda
 }
 
 constexpr size_t kFusedSmemLimit = 200 * 1024;
+int g_withhold = -1;  // asg_debug_withhold_arrival
 
 // The whole solve as one launch when the plan qualifies (*used = true; one synchronisation
 // to read the result); *used = false otherwise (the caller runs the host-driven solve).
@@ -995,6 +999,7 @@ asg_status be_solve_fused(asg_plan* plan, long long n, double dt, const double* 
   *used = false;
   asg::FusedArgs<TV> c{};
   if (!asg::small_plan_args<TV>(plan, &c.a) || !asg::small_plan_args<double>(plan, &c.a64) || c.a.B > 256) return ASG_OK;
+  if ((reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(x)) & 15) return ASG_OK;  // vector loads of x
   const int P = c.a.D >= 2 ? c.a.stride[c.a.D - 2] : c.a.B;
   if (P < 2 || P > 4) return ASG_OK;
   const int m = o->restart;
@@ -1024,6 +1029,8 @@ asg_status be_solve_fused(asg_plan* plan, long long n, double dt, const double* 
   c.items = plan->d_fz_items[k];
   c.max_rows = plan->fz_max_rows[k];
   c.max_slots = plan->fz_max_slots[k];
+  c.withhold = g_withhold;
+  g_withhold = -1;
   ASG_CUDA(cudaMemsetAsync(c.state, 0, sizeof(asg::GmresState), s));
   cudaError_t e = P == 2 ? launch_fused_p<TV, 2>(c, G, smem, s)
                   : P == 3 ? launch_fused_p<TV, 3>(c, G, smem, s)
@@ -1240,6 +1247,12 @@ asg_status asg_be_solve(asg_plan* plan, double dt, const double* d_b, double* d_
     return fail(ASG_ERR_INVALID, "be_solve: bad options");
   return opts->mixed ? be_solve<float>(plan, dt, d_b, d_x, opts, info, d_work, work_bytes, stream)
                      : be_solve<double>(plan, dt, d_b, d_x, opts, info, d_work, work_bytes, stream);
+}
+
+asg_status asg_debug_withhold_arrival(int barrier) {
+  if (barrier < -1) return fail(ASG_ERR_INVALID, "debug_withhold_arrival: barrier=%d", barrier);
+  g_withhold = barrier;
+  return ASG_OK;
 }
 
 }  // extern "C"

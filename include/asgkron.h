@@ -214,12 +214,20 @@ typedef struct {
   double rel_residual;     /* final FP64 ||b - (I - dt A) x|| / ||b|| */
 } asg_gmres_info;
 /* Backward Euler solve (I - dt A) x = b (backward_euler, time_advance.m:267-349, which
- * assembles A and uses a direct solve): matrix-free GMRES(m) inside iterative refinement;
- * the residual, the update of x and all Arnoldi dot products and norms are FP64.  d_x holds the
- * initial guess on entry.  Synchronises the stream (one host read per Arnoldi step). */
+ * assembles A and uses a direct solve): matrix-free GMRES(m) inside iterative refinement.
+ * The outer residual b - (I - dt A) x, its norm and x are FP64; each GMRES cycle runs in the
+ * basis precision (FP32 with opts->mixed, else FP64).  Plans on the small-block kernel with
+ * deg 2..4 run the whole solve as one cooperative launch (one synchronisation); other plans
+ * run it kernel by kernel.  d_x holds the initial guess on entry; d_b and d_x 16-byte
+ * aligned.  ASG_ERR_TIMEOUT: a bounded grid-barrier wait of the one-launch solve gave up. */
 asg_status asg_be_workspace(const asg_plan* plan, const asg_gmres_opts* opts, size_t* bytes);
 asg_status asg_be_solve(asg_plan* plan, double dt, const double* d_b, double* d_x, const asg_gmres_opts* opts,
                         asg_gmres_info* info, void* d_work, size_t work_bytes, void* stream);
+/* Test hook (no reference counterpart): in the next one-launch backward-Euler solve of this
+ * process, CTA 0 withholds its arrival at grid barrier number `barrier` (0-based, counted
+ * from the launch), so every CTA's bounded wait (~2^31 cycles) runs out and the solve returns
+ * ASG_ERR_TIMEOUT with the context intact.  -1 clears it. */
+asg_status asg_debug_withhold_arrival(int barrier);
 
 /* ---------------------------------------------------------------------------------------
  * Kronecker products and batched small GEMMs (Kronmult/)

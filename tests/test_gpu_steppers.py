@@ -261,3 +261,32 @@ def test_be_fused_cycle_vs_per_phase_cycle(dev, lev, deg, mixed):
     assert inf_f["rel_residual"] <= 1e-11 and inf_p["rel_residual"] <= 1e-11
     assert torch.equal(xf, xf2)  # fixed-order reductions: the fused cycle is reproducible
     assert rel2(xf.cpu().numpy(), xp.cpu().numpy()) <= 1e-9
+
+
+def test_be_fused_barrier_timeout_reports_and_recovers(dev):
+    """The one-launch solve's grid barriers wait a bounded time.  With CTA 0 withholding one
+    arrival (the test hook), every CTA's wait runs out (~1 s), the solve returns
+    ASG_ERR_TIMEOUT, and the context stays usable: the same solve then succeeds and matches
+    a direct solve."""
+    import asgkron
+    from asgkron import pdes
+    from asgkron._lib import AsgError, check, lib
+    from asgkron.steppers import be_step
+
+    pde = pdes.diffusion2(4)
+    idx = asgkron.hash_table_sparse_nD(pde.levels, 8).idx1d()
+    mats = pde.term_mats(2)
+    plan = asgkron.Plan.create(mats, idx, 2)
+    f0 = pde.initial_condition(2, idx) + 1e-3 * np.random.default_rng(7).standard_normal(plan.dof)
+    dt = pde.dt(1.0)
+    f = torch.from_numpy(f0).to(dev)
+    for mixed in (True, False):
+        check(lib().asg_debug_withhold_arrival(5))
+        with pytest.raises(AsgError, match="grid barrier"):
+            be_step(plan, f, dt, mixed=mixed)
+    x, info = be_step(plan, f, dt, mixed=True, tol=1e-11)
+    torch.cuda.synchronize()
+    assert info["converged"]
+    _, A = O.apply_A_loop(mats, idx.astype(np.int64), 2, f0, build_A=True)
+    want = O.backward_euler_step(A, f0, dt, np.zeros_like(f0))
+    assert rel2(x.cpu().numpy(), want) <= 1e-9
