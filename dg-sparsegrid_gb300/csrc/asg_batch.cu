@@ -5,7 +5,7 @@
 // descending cost (chain flops); persistent warps take items from a device counter (reset
 // by a memset in the same stream, so the launch is graph-capturable) and run the warp chain
 // algorithm of the single-problem kernel for each row, dispatching on the problem's degree,
-// with the next entry's operands prefetched by asynchronous copies.
+// with the operands of the next entries prefetched by asynchronous copies.
 // Each row is still computed by one warp in a fixed order: results do not depend on which
 // warp took the item.  A tuner times (warps per CTA, rows per item) candidates.
 #include <algorithm>
@@ -30,6 +30,7 @@ struct BatchProblem {
   const unsigned* active;
   int N, D, B, P, T;
   int stride[kMaxDims];
+  int vec;  // f blocks start on 16-byte boundaries: 16-byte asynchronous copies
 };
 
 struct BatchItem {
@@ -47,28 +48,38 @@ __device__ __forceinline__ void cp_async_elem(T* dst, const T* src) {
   else
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
 }
+// 16-byte asynchronous global -> shared copy (both addresses 16-byte aligned), L2 only.
+template <typename T>
+__device__ __forceinline__ void cp_async16(T* dst, const T* src) {
+  const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cp_async_wait_prev() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait_pending() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
-// Per-warp shared memory of the row kernel: the row's block-base table (8-byte entries), then
-// in elements of T two stages of (column block), two chain buffers and two stages of factor
-// blocks.
+// Per-warp shared memory of the row kernel: the row's block-base table (8-byte entries), the
+// active-factor masks of the stages in flight, then in elements of T kBatchStages stages of
+// (column block), two chain buffers and kBatchStages stages of factor blocks.
+constexpr int kBatchStages = 2;           // entries in flight per warp (the one computed + 1)
 constexpr int kStageVals = 256;           // one element block (deg^d <= 256)
 constexpr int kAmatVals = kMaxDims * 16;  // every factor block of one entry (deg <= 4)
-constexpr int kWarpVals = 2 * kStageVals + 2 * kStageVals + 2 * kAmatVals;
+constexpr int kWarpVals = kBatchStages * kStageVals + 2 * kStageVals + kBatchStages * kAmatVals;
+constexpr int kWarpHdr = kMaxTerms * kMaxDims * sizeof(long long) + 16 * sizeof(unsigned);
 template <typename T>
 __host__ __device__ constexpr size_t warp_smem_bytes() {
-  return kMaxTerms * kMaxDims * sizeof(long long) + kWarpVals * sizeof(T);
+  return kWarpHdr + kWarpVals * sizeof(T);
 }
 
 // One row of a problem, computed by one warp: for each work entry (column j, term t) the
 // column's block goes through the term's mode-product chain (fastest dimension first,
 // kronmult method 1, identity factors skipped) and is added to the row's accumulators
 // (Kahan-compensated in FP32), entries in list order -- the single-plan warp chain kernel's
-// arithmetic, so results equal it bitwise.  Entries are software-pipelined: while entry q is
-// computed, the warp's asynchronous copies bring entry q+1's column block and all its factor
-// blocks into the other shared-memory stage, so the global-memory latency of an entry is
-// paid once instead of once per mode and overlaps the previous entry's arithmetic.  The row's
+// arithmetic, so results equal it bitwise.  Entries are software-pipelined through a ring of
+// kBatchStages shared-memory stages: while entry q is computed, the asynchronous copies of
+// entries q+1 .. q+S-1 (column block and every applied factor block) are in flight, so an
+// entry's global-memory latency overlaps the arithmetic of the ones before it (four stages
+// measured no faster than two on the 256-problem batch).  The row's
 // per-(term, dimension) block bases sit in a shared table; for deg 2 and 4 the fiber indexing
 // uses shifts instead of divisions.
 template <typename T, int P>
@@ -76,10 +87,12 @@ __device__ __forceinline__ void warp_row(const BatchProblem& pb, int row, unsign
   constexpr int MAXE = 8;
   constexpr bool KAHAN = sizeof(T) == 4;
   constexpr int LG = P == 2 ? 1 : (P == 4 ? 2 : 0);  // log2(P) when P is a power of two
+  constexpr int S = kBatchStages;
   long long* abase = reinterpret_cast<long long*>(wsm);
-  T* stage = reinterpret_cast<T*>(wsm + kMaxTerms * kMaxDims * sizeof(long long));  // [2][256]
-  T* work = stage + 2 * kStageVals;                                                  // [2][256]
-  T* amat = work + 2 * kStageVals;                                                   // [2][kAmatVals]
+  unsigned* acts = reinterpret_cast<unsigned*>(wsm + kMaxTerms * kMaxDims * sizeof(long long));  // [S]
+  T* stage = reinterpret_cast<T*>(wsm + kWarpHdr);  // [S][256]
+  T* work = stage + S * kStageVals;                 // [2][256]
+  T* amat = work + 2 * kStageVals;                  // [S][kAmatVals]
   const T* f = static_cast<const T*>(pb.f);
   T* y = static_cast<T*>(pb.y);
   const T* ops = sizeof(T) == 8 ? reinterpret_cast<const T*>(pb.ops64) : reinterpret_cast<const T*>(pb.ops32);
@@ -91,19 +104,35 @@ __device__ __forceinline__ void warp_row(const BatchProblem& pb, int row, unsign
   }
   __syncwarp();
   // issue the copies of entry q into stage st: the column block and every applied factor block
+  // (16-byte pieces where the alignment allows: f blocks when pb.vec, factor blocks for
+  // deg 2 and 4, whose P x P blocks are whole 16-byte multiples at aligned offsets)
   auto issue = [&](long long q, int st) {
     const int e = pb.ent[q];
     const int j = e >> 4, t = e & 15;
     const unsigned act = pb.active[t];
     const T* src = f + static_cast<size_t>(j) * B;
     T* dst = stage + st * kStageVals;
-    for (int k = lane; k < B; k += 32) cp_async_elem(dst + k, src + k);
+    constexpr int V = 16 / static_cast<int>(sizeof(T));
+    if (pb.vec) {
+      for (int k = lane * V; k < B; k += 32 * V) cp_async16(dst + k, src + k);
+    } else {
+      for (int k = lane; k < B; k += 32) cp_async_elem(dst + k, src + k);
+    }
     T* ad = amat + st * kAmatVals;
-    for (int k = lane; k < D * P * P; k += 32) {
-      const int m = k / (P * P), r = k - m * (P * P);
-      if ((act >> m) & 1u)
-        cp_async_elem(ad + m * 16 + r,
-                      ops + abase[t * D + m] + static_cast<long long>(pb.idx1d[j * D + m]) * (P * P) + r);
+    if constexpr ((P * P) % V == 0) {
+      constexpr int PV = P * P / V;  // 16-byte pieces per factor block
+      for (int k = lane; k < D * PV; k += 32) {
+        const int m = k / PV, r = (k - m * PV) * V;
+        if ((act >> m) & 1u)
+          cp_async16(ad + m * 16 + r, ops + abase[t * D + m] + static_cast<long long>(pb.idx1d[j * D + m]) * (P * P) + r);
+      }
+    } else {
+      for (int k = lane; k < D * P * P; k += 32) {
+        const int m = k / (P * P), r = k - m * (P * P);
+        if ((act >> m) & 1u)
+          cp_async_elem(ad + m * 16 + r,
+                        ops + abase[t * D + m] + static_cast<long long>(pb.idx1d[j * D + m]) * (P * P) + r);
+      }
     }
     return act;
   };
@@ -111,16 +140,25 @@ __device__ __forceinline__ void warp_row(const BatchProblem& pb, int row, unsign
 #pragma unroll
   for (int k = 0; k < MAXE; ++k) acc[k] = cmp[k] = T(0);
   const long long q0 = pb.row_ptr[row], q1 = pb.row_ptr[row + 1];
-  unsigned act_next = 0;
-  if (q0 < q1) act_next = issue(q0, 0);
-  cp_async_commit();
-  for (long long q = q0; q < q1; ++q) {
-    const int cur = static_cast<int>((q - q0) & 1);
-    const unsigned act = act_next;
-    if (q + 1 < q1) act_next = issue(q + 1, cur ^ 1);
+  // entries q0 .. q0+S-2 in flight first (one commit group each, empty past the row's end)
+  for (int k = 0; k < S - 1; ++k) {
+    if (q0 + k < q1) {
+      const unsigned a0 = issue(q0 + k, k);
+      if (lane == 0) acts[k] = a0;
+    }
     cp_async_commit();
-    cp_async_wait_prev();  // this lane's copies of entry q have landed
-    __syncwarp();          // ... and every lane's
+  }
+  for (long long q = q0; q < q1; ++q) {
+    const int cur = static_cast<int>((q - q0) % S);
+    if (q + S - 1 < q1) {  // refill the stage consumed by entry q-1
+      const int nx = (cur + S - 1) % S;
+      const unsigned a1 = issue(q + S - 1, nx);
+      if (lane == 0) acts[nx] = a1;
+    }
+    cp_async_commit();
+    cp_async_wait_pending<S - 1>();  // this lane's copies of entry q have landed
+    __syncwarp();                    // ... and every lane's (and acts[cur])
+    const unsigned act = acts[cur];
     const T* in = stage + cur * kStageVals;
     const T* Am = amat + cur * kAmatVals;
     int wsel = 0;
@@ -128,8 +166,19 @@ __device__ __forceinline__ void warp_row(const BatchProblem& pb, int row, unsign
     for (int m = D - 1; m >= 0; --m, s *= P, sh += LG) {
       if (!((act >> m) & 1u)) continue;
       T A[P * P];
+      if constexpr (sizeof(T) == 4 && P == 4) {  // four 16-byte shared loads
 #pragma unroll
-      for (int r = 0; r < P * P; ++r) A[r] = Am[m * 16 + r];
+        for (int r = 0; r < 4; ++r) {
+          const float4 v = reinterpret_cast<const float4*>(Am + m * 16)[r];
+          A[4 * r] = v.x;
+          A[4 * r + 1] = v.y;
+          A[4 * r + 2] = v.z;
+          A[4 * r + 3] = v.w;
+        }
+      } else {
+#pragma unroll
+        for (int r = 0; r < P * P; ++r) A[r] = Am[m * 16 + r];
+      }
       T* out = work + wsel * kStageVals;
       for (int fi = lane; fi < B / P; fi += 32) {
         int hi, lo;
@@ -228,9 +277,11 @@ namespace {
 constexpr int kRowsPerItem[3] = {1, 2, 4};
 
 asg_status upload_probs(asg_batch* b, bool f32) {
+  const size_t es = f32 ? sizeof(float) : sizeof(double);
   for (size_t k = 0; k < b->probs.size(); ++k) {
     b->probs[k].f = f32 ? b->f32[k] : b->f64[k];
     b->probs[k].y = f32 ? b->y32[k] : b->y64[k];
+    b->probs[k].vec = (reinterpret_cast<uintptr_t>(b->probs[k].f) % 16 == 0 && (b->probs[k].B * es) % 16 == 0) ? 1 : 0;
   }
   ASG_CUDA(cudaMemcpy(b->d_probs, b->probs.data(), b->probs.size() * sizeof(asg::BatchProblem),
                       cudaMemcpyHostToDevice));
