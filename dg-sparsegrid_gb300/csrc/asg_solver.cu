@@ -398,16 +398,32 @@ __device__ __forceinline__ T fz_warp_sum(T v) {
   return v;
 }
 
-// s_out[k] = sum over the grid's CTAs of partial[k * G + q], k < nk: one warp per row k, its
-// lanes adding q = lane, lane + 32, ...; every CTA computes the same values in the same order.
+// s_out[k] = sum over the grid's CTAs of partial[k * G + q], k < nk: warp w takes rows w,
+// w + 16, ... (up to four loaded together in FP32), its lanes adding q = lane, lane + 32, ... and a
+// shuffle tree adding the lanes; every CTA computes the same values in the same order.
 template <typename T>
 __device__ void sum_partials(const T* partial, int nk, T* s_out) {
+  // rows in flight per warp: four in FP32; one in FP64, where the kernel sits at its register
+  // limit and more rows in flight measured slower
+  constexpr int U = sizeof(T) == 4 ? 4 : 1;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, G = gridDim.x;
-  for (int k = warp; k < nk; k += kFzWarps) {
-    T acc = T(0);
-    for (int q = lane; q < G; q += 32) acc += __ldcg(partial + static_cast<long long>(k) * G + q);
-    acc = fz_warp_sum(acc);
-    if (lane == 0) s_out[k] = acc;
+  for (int k0 = warp; k0 < nk; k0 += U * kFzWarps) {  // rows k0, k0 + 16, ... together
+    T acc[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) acc[u] = T(0);
+    for (int q = lane; q < G; q += 32) {
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int k = k0 + u * kFzWarps;
+        if (k < nk) acc[u] += __ldcg(partial + static_cast<long long>(k) * G + q);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int k = k0 + u * kFzWarps;
+      const T v = fz_warp_sum(acc[u]);
+      if (lane == 0 && k < nk) s_out[k] = v;
+    }
   }
   __syncthreads();
 }
