@@ -8,6 +8,8 @@
 // FP32 accumulation across the column reduction is Kahan-compensated.
 #include <cstdio>
 
+#include <type_traits>
+
 #include "asg_internal.h"
 #include "asg_rows.cuh"
 
@@ -173,6 +175,33 @@ __global__ void __launch_bounds__(128) k_single_small(ApplyArgs<T> a) {
   const int wpb = blockDim.x >> 5;
   const SmallLane<MAXO> sl = small_lane<T, P, MAXO>(a, lane);
   for (int row = blockIdx.x * wpb + warp; row < a.N; row += gridDim.x * wpb) small_row<T, P, MAXO, KAHAN>(a, row, sl);
+}
+
+// Fiber-per-lane variant for P <= 4 (see fiber_entry), one CTA of WR warps per output
+// element: warp w takes the row's entries w Gf + g, (w + WR) Gf + g, ... (g its lane group),
+// writes its partial block to shared memory, and the CTA adds the WR partials in warp order
+// (deterministic) -- WR times the parallelism of a warp per row, for the small element
+// counts these plans have (hundreds to a few thousand rows).
+template <typename T, int P, int MAXF, bool KAHAN, int WR>
+__global__ void __launch_bounds__(32 * WR) k_single_fiber_split(ApplyArgs<T> a) {
+  __shared__ __align__(16) T part[WR][256];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const int B = a.B;
+  const FiberLane<MAXF> fl = fiber_lane<T, P, MAXF>(a, lane);
+  for (int row = blockIdx.x; row < a.N; row += gridDim.x) {
+    fiber_chunk<T, P, MAXF, KAHAN>(a, a.f, a.row_ptr[row], a.row_ptr[row + 1], fl, part[warp], warp * fl.Gf,
+                                   WR * fl.Gf);
+    __syncthreads();
+    T* yr = a.y + static_cast<size_t>(row) * B;
+    for (int e = threadIdx.x; e < B; e += 32 * WR) {
+      T v = part[0][e];
+#pragma unroll
+      for (int w = 1; w < WR; ++w) v += part[w][e];
+      yr[e] = v;
+    }
+    __syncthreads();
+  }
 }
 
 // Fiber-per-lane variant for P <= 4 (see fiber_entry): one warp per output element.
@@ -1336,14 +1365,25 @@ cudaError_t launch_p(const ApplyArgs<T>& a, int kind, cudaStream_t s) {
     const int wpb = 4;
     const int grid = (a.N + wpb - 1) / wpb;
     if constexpr (P <= 4) {
-      const int Lf = a.B / P;
-      if (Lf <= 32)
-        k_single_fiber<T, P, 1, K><<<grid, wpb * 32, 0, s>>>(a);
-      else if (Lf <= 64)
-        k_single_fiber<T, P, 2, K><<<grid, wpb * 32, 0, s>>>(a);
-      else
-        k_single_fiber<T, P, 4, K><<<grid, wpb * 32, 0, s>>>(a);
-      return cudaGetLastError();
+      const int Lf = a.B / P, Gf = Lf <= 32 ? 32 / Lf : 1;
+      // warps per row: enough that each warp gets a few rounds of the row's entries (one entry
+      // per lane group per round), at most 4 in FP32 and 2 in FP64 (FP64 issue-bound sooner)
+      const int rounds = a.row_entries / Gf;
+      const int wr = rounds >= 4 ? (sizeof(T) == 4 ? 4 : 2) : (rounds >= 2 ? 2 : 1);
+      const int g2 = a.N < 152 * 16 ? a.N : 152 * 16;  // split: one CTA per row, at most 16 per SM
+      auto launch = [&](auto maxf) -> cudaError_t {
+        constexpr int MF = decltype(maxf)::value;
+        if (wr == 4)
+          k_single_fiber_split<T, P, MF, K, 4><<<g2, 128, 0, s>>>(a);
+        else if (wr == 2)
+          k_single_fiber_split<T, P, MF, K, 2><<<g2, 64, 0, s>>>(a);
+        else
+          k_single_fiber<T, P, MF, K><<<grid, wpb * 32, 0, s>>>(a);
+        return cudaGetLastError();
+      };
+      if (Lf <= 32) return launch(std::integral_constant<int, 1>{});
+      if (Lf <= 64) return launch(std::integral_constant<int, 2>{});
+      return launch(std::integral_constant<int, 4>{});
     }
     if (a.B <= 32)
       k_single_small<T, P, 1, K><<<grid, wpb * 32, 0, s>>>(a);

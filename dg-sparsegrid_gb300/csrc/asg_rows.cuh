@@ -249,18 +249,20 @@ __device__ __forceinline__ void fiber_entry(const ApplyArgs<T>& a, const T* __re
   }
 }
 
-// Entries [q0, q1) of one row by one warp, reading the input vector f; the block's B sums go
-// to out[0..B) (16-byte aligned for P = 4).
+// Entries q0 + gofs + g, q0 + gofs + g + gstride, ... (< q1) of one row by one warp (g: the
+// lane's group; a whole row: gofs 0, gstride Gf), reading the input vector f; the warp's B
+// sums go to out[0..B) (16-byte aligned for P = 4).
 template <typename T, int P, int MAXF, bool KAHAN>
 __device__ __forceinline__ void fiber_chunk(const ApplyArgs<T>& a, const T* __restrict__ f, long long q0, long long q1,
-                                            const FiberLane<MAXF>& fl, T* out) {
+                                            const FiberLane<MAXF>& fl, T* out, int gofs = 0, int gstride = 0) {
   T acc[MAXF][P], cmp[MAXF][P];
 #pragma unroll
   for (int q = 0; q < MAXF; ++q)
 #pragma unroll
     for (int t = 0; t < P; ++t) acc[q][t] = cmp[q][t] = T(0);
+  const int step = gstride > 0 ? gstride : fl.Gf;
   if (fl.g < fl.Gf)
-    for (long long q = q0 + fl.g; q < q1; q += fl.Gf) fiber_entry<T, P, MAXF, KAHAN>(a, f, a.ed[q], fl, acc, cmp);
+    for (long long q = q0 + gofs + fl.g; q < q1; q += step) fiber_entry<T, P, MAXF, KAHAN>(a, f, a.ed[q], fl, acc, cmp);
   // fixed-order tree across the groups: group g takes group g + off's sums (g % 2off == 0)
   const int lane = fl.g * fl.Lf + fl.r;
   for (int off = 1; off < fl.Gf; off <<= 1) {
