@@ -204,15 +204,6 @@ __global__ void __launch_bounds__(32 * WR) k_single_fiber_split(ApplyArgs<T> a) 
   }
 }
 
-// Fiber-per-lane variant for P <= 4 (see fiber_entry): one warp per output element.
-template <typename T, int P, int MAXF, bool KAHAN>
-__global__ void __launch_bounds__(128) k_single_fiber(ApplyArgs<T> a) {
-  const int lane = threadIdx.x & 31;
-  const int warp = threadIdx.x >> 5;
-  const int wpb = blockDim.x >> 5;
-  const FiberLane<MAXF> fl = fiber_lane<T, P, MAXF>(a, lane);
-  for (int row = blockIdx.x * wpb + warp; row < a.N; row += gridDim.x * wpb) fiber_row<T, P, MAXF, KAHAN>(a, row, fl);
-}
 
 // ---------------------------------------------------------------------------------------
 // Chain kernel, one CTA per output element (element blocks up to 4096 values).
@@ -1365,20 +1356,15 @@ cudaError_t launch_p(const ApplyArgs<T>& a, int kind, cudaStream_t s) {
     const int wpb = 4;
     const int grid = (a.N + wpb - 1) / wpb;
     if constexpr (P <= 4) {
-      const int Lf = a.B / P, Gf = Lf <= 32 ? 32 / Lf : 1;
-      // warps per row: enough that each warp gets a few rounds of the row's entries (one entry
-      // per lane group per round), at most 4 in FP32 and 2 in FP64 (FP64 issue-bound sooner)
-      const int rounds = a.row_entries / Gf;
-      const int wr = rounds >= 4 ? (sizeof(T) == 4 ? 4 : 2) : (rounds >= 2 ? 2 : 1);
-      const int g2 = a.N < 152 * 16 ? a.N : 152 * 16;  // split: one CTA per row, at most 16 per SM
+      const int Lf = a.B / P;
+      // warps per row: 4 in FP32, 2 in FP64 (FP64 issue-bound sooner) -- the fastest or tied
+      // on every measured plan (continuity2/3, diffusion2); fixed by the precision alone, so a
+      // row is summed in the same order in every plan that holds it
+      constexpr int WR = sizeof(T) == 4 ? 4 : 2;
+      const int g2 = a.N < 152 * 16 ? a.N : 152 * 16;  // one CTA per row, at most 16 per SM
       auto launch = [&](auto maxf) -> cudaError_t {
         constexpr int MF = decltype(maxf)::value;
-        if (wr == 4)
-          k_single_fiber_split<T, P, MF, K, 4><<<g2, 128, 0, s>>>(a);
-        else if (wr == 2)
-          k_single_fiber_split<T, P, MF, K, 2><<<g2, 64, 0, s>>>(a);
-        else
-          k_single_fiber<T, P, MF, K><<<grid, wpb * 32, 0, s>>>(a);
+        k_single_fiber_split<T, P, MF, K, WR><<<g2, 32 * WR, 0, s>>>(a);
         return cudaGetLastError();
       };
       if (Lf <= 32) return launch(std::integral_constant<int, 1>{});

@@ -64,7 +64,6 @@ struct ApplyArgs {
   const int* cta_ptr;        // [nctas+1] persistent single-mode kernel: rows of CTA c are
   const int* cta_rows;       //   cta_rows[cta_ptr[c] .. cta_ptr[c+1]) (static LPT assignment)
   int nctas;
-  int row_entries;           // mean work entries per row (launch heuristics)
 };
 
 template <typename T>

@@ -472,7 +472,6 @@ ApplyArgs<T> make_args(const asg_plan* p, const T* f, T* y, const T* ops) {
   a.cta_ptr = p->d_cta_ptr[pk];
   a.cta_rows = p->d_cta_rows[pk];
   a.nctas = p->cta_ptr[pk].empty() ? 0 : static_cast<int>(p->cta_ptr[pk].size()) - 1;
-  a.row_entries = p->N > 0 ? static_cast<int>(p->ent.size() / p->N) : 0;
   int s = 1;
   for (int m = p->D - 1; m >= 0; --m) {
     a.stride[m] = s;

@@ -285,10 +285,6 @@ __device__ __forceinline__ void fiber_chunk(const ApplyArgs<T>& a, const T* __re
   }
 }
 
-template <typename T, int P, int MAXF, bool KAHAN>
-__device__ __forceinline__ void fiber_row(const ApplyArgs<T>& a, int row, const FiberLane<MAXF>& fl) {
-  fiber_chunk<T, P, MAXF, KAHAN>(a, a.f, a.row_ptr[row], a.row_ptr[row + 1], fl, a.y + static_cast<size_t>(row) * a.B);
-}
 
 }  // namespace
 }  // namespace asg
