@@ -41,15 +41,6 @@ struct Row<float, 4> {
   }
 };
 template <>
-struct Row<float, 2> {
-  float v[2];
-  __device__ __forceinline__ void load(const float* p) {
-    const float2 q = *reinterpret_cast<const float2*>(p);
-    v[0] = q.x; v[1] = q.y;
-  }
-  __device__ __forceinline__ void store(float* p) const { *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]); }
-};
-template <>
 struct Row<double, 4> {
   double v[4];
   __device__ __forceinline__ void load(const double* p) {
@@ -61,15 +52,6 @@ struct Row<double, 4> {
     reinterpret_cast<double2*>(p)[0] = make_double2(v[0], v[1]);
     reinterpret_cast<double2*>(p)[1] = make_double2(v[2], v[3]);
   }
-};
-template <>
-struct Row<double, 2> {
-  double v[2];
-  __device__ __forceinline__ void load(const double* p) {
-    const double2 a = *reinterpret_cast<const double2*>(p);
-    v[0] = a.x; v[1] = a.y;
-  }
-  __device__ __forceinline__ void store(double* p) const { *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]); }
 };
 
 // Cooperative copy of n values (16-byte vectors when both ends allow it).
@@ -468,31 +450,6 @@ __device__ __forceinline__ void tile_rows(T (&g)[4][4], const T* A, const T* xs,
       for (int c = 0; c < 4; ++c) g[aa][c] = fma(A[aa * 4 + b], x.v[c], g[aa][c]);
   }
 }
-template <>
-__device__ __forceinline__ void tile_rows<float>(float (&g)[4][4], const float* A, const float* xs, int s) {
-  float2 acc[4][2];
-#pragma unroll
-  for (int aa = 0; aa < 4; ++aa) {
-    acc[aa][0] = make_float2(g[aa][0], g[aa][1]);
-    acc[aa][1] = make_float2(g[aa][2], g[aa][3]);
-  }
-#pragma unroll
-  for (int b = 0; b < 4; ++b) {
-    const float4 x = *reinterpret_cast<const float4*>(xs + b * s);
-    const float2 x01 = make_float2(x.x, x.y), x23 = make_float2(x.z, x.w);
-#pragma unroll
-    for (int aa = 0; aa < 4; ++aa) {
-      const float2 ab = make_float2(A[aa * 4 + b], A[aa * 4 + b]);
-      acc[aa][0] = ffma2(ab, x01, acc[aa][0]);
-      acc[aa][1] = ffma2(ab, x23, acc[aa][1]);
-    }
-  }
-#pragma unroll
-  for (int aa = 0; aa < 4; ++aa) {
-    g[aa][0] = acc[aa][0].x; g[aa][1] = acc[aa][0].y;
-    g[aa][2] = acc[aa][1].x; g[aa][3] = acc[aa][1].y;
-  }
-}
 // g[r][a] += sum_b A[a][b] * x[r][b] with tile rows s apart
 template <typename T>
 __device__ __forceinline__ void tile_cols_s(T (&g)[4][4], const T* A, const T* xs, int s) {
@@ -504,22 +461,6 @@ __device__ __forceinline__ void tile_cols_s(T (&g)[4][4], const T* A, const T* x
     for (int aa = 0; aa < 4; ++aa)
 #pragma unroll
       for (int b = 0; b < 4; ++b) g[r][aa] = fma(A[aa * 4 + b], x.v[b], g[r][aa]);
-  }
-}
-template <>
-__device__ __forceinline__ void tile_cols_s<float>(float (&g)[4][4], const float* A, const float* xs, int s) {
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const float4 x = *reinterpret_cast<const float4*>(xs + r * s);
-    const float xv[4] = {x.x, x.y, x.z, x.w};
-    float2 acc0 = make_float2(g[r][0], g[r][1]), acc1 = make_float2(g[r][2], g[r][3]);
-#pragma unroll
-    for (int b = 0; b < 4; ++b) {
-      const float2 xb = make_float2(xv[b], xv[b]);
-      acc0 = ffma2(make_float2(A[0 * 4 + b], A[1 * 4 + b]), xb, acc0);
-      acc1 = ffma2(make_float2(A[2 * 4 + b], A[3 * 4 + b]), xb, acc1);
-    }
-    g[r][0] = acc0.x; g[r][1] = acc0.y; g[r][2] = acc1.x; g[r][3] = acc1.y;
   }
 }
 
