@@ -135,6 +135,7 @@ SIGNATURES = {
     "asg_batch_prepare": (C.c_int, [C.c_void_p, C.c_int]),
     "asg_batch_apply": (C.c_int, [C.c_void_p, C.c_int, _P]),
     "asg_batch_tune": (C.c_int, [C.c_void_p, C.c_int, _P, C.POINTER(C.c_float)]),
+    "asg_batch_configure": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "asg_batch_info": (C.c_int, [C.c_void_p, _I, _I, C.POINTER(C.c_double)]),
     "asg_rk3_step_f64": (C.c_int, [C.c_void_p, _P, C.c_double, C.POINTER(C.c_void_p), _P, C.c_size_t, _P]),
     "asg_rk3_step_f32": (C.c_int, [C.c_void_p, _P, C.c_double, C.POINTER(C.c_void_p), _P, C.c_size_t, _P]),

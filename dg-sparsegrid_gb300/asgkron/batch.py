@@ -39,6 +39,10 @@ class Batch:
                                    C.byref(ms)))
         return ms.value
 
+    def configure(self, warps_per_cta, rows_per_item):
+        """Fixed launch shape instead of tune(): 4 or 8 warps per CTA, 1, 2 or 4 rows per item."""
+        check(lib().asg_batch_configure(self._h, int(warps_per_cta), int(rows_per_item)))
+
     def info(self):
         w, r, fl = C.c_int(0), C.c_int(0), C.c_double(0)
         check(lib().asg_batch_info(self._h, C.byref(w), C.byref(r), C.byref(fl)))

@@ -6,8 +6,8 @@
 // by a memset in the same stream, so the launch is graph-capturable) and run the warp chain
 // algorithm of the single-problem kernel for each row, dispatching on the problem's degree,
 // with the operands of the next entries prefetched by asynchronous copies.
-// Each row is still computed by one warp in a fixed order: results do not depend on which
-// warp took the item.  A tuner times (warps per CTA, rows per item) candidates.
+// Each row is computed by a fixed set of lanes in a fixed order: results do not depend on
+// which warp took the item.  A tuner times (warps per CTA, rows per item) candidates.
 #include <algorithm>
 #include <new>
 #include <vector>
@@ -31,6 +31,7 @@ struct BatchProblem {
   int N, D, B, P, T;
   int stride[kMaxDims];
   int vec;  // f blocks start on 16-byte boundaries: 16-byte asynchronous copies
+  int R;    // rows a warp computes side by side (1, 2 or 4; capped by the rows per item)
 };
 
 struct BatchItem {
@@ -58,12 +59,15 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait_pending() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
+// ceil(2^16 / 3^k), k = 0..4: the fiber-index reciprocals of deg 3 (at most 81 fibers)
+__constant__ unsigned c_recip3[5] = {65536u, 21846u, 7282u, 2428u, 810u};
+
 // Per-warp shared memory of the row kernel: the row's block-base table (8-byte entries), the
 // active-factor masks of the stages in flight, then in elements of T kBatchStages stages of
 // (column block), two chain buffers and kBatchStages stages of factor blocks.
 constexpr int kBatchStages = 2;           // entries in flight per warp (the one computed + 1)
 constexpr int kStageVals = 256;           // one element block (deg^d <= 256)
-constexpr int kAmatVals = kMaxDims * 16;  // every factor block of one entry (deg <= 4)
+constexpr int kAmatVals = 128;  // every factor block of the entries of the rows side by side
 constexpr int kWarpVals = kBatchStages * kStageVals + 2 * kStageVals + kBatchStages * kAmatVals;
 constexpr int kWarpHdr = kMaxTerms * kMaxDims * sizeof(long long) + 16 * sizeof(unsigned);
 template <typename T>
@@ -71,67 +75,74 @@ __host__ __device__ constexpr size_t warp_smem_bytes() {
   return kWarpHdr + kWarpVals * sizeof(T);
 }
 
-// One row of a problem, computed by one warp: for each work entry (column j, term t) the
-// column's block goes through the term's mode-product chain (fastest dimension first,
-// kronmult method 1, identity factors skipped) and is added to the row's accumulators
-// (Kahan-compensated in FP32), entries in list order -- the single-plan warp chain kernel's
-// arithmetic, so results equal it bitwise.  Entries are software-pipelined through a ring of
-// kBatchStages shared-memory stages: while entry q is computed, the asynchronous copies of
-// entries q+1 .. q+S-1 (column block and every applied factor block) are in flight, so an
-// entry's global-memory latency overlaps the arithmetic of the ones before it (four stages
-// measured no faster than two on the 256-problem batch).  The row's
-// per-(term, dimension) block bases sit in a shared table; for deg 2 and 4 the fiber indexing
-// uses shifts instead of divisions.
-template <typename T, int P>
-__device__ __forceinline__ void warp_row(const BatchProblem& pb, int row, unsigned char* wsm, int lane) {
+// R rows of a problem side by side in one warp, each on 32/R lanes with its own slice of every
+// buffer (with one row a small deg^d leaves most lanes idle).  For each work entry (column j,
+// term t) of a row, the column's block goes through the term's mode-product chain (fastest
+// dimension first, kronmult method 1, identity factors skipped) and is added to the row's
+// accumulators (Kahan-compensated in FP32), entries in list order -- the single-plan warp
+// chain kernel's arithmetic, so results equal it bitwise.  Entries are software-pipelined
+// through a ring of kBatchStages shared-memory stages: while entry q is computed, the
+// asynchronous copies of entries q+1 .. q+S-1 (column block and every applied factor block)
+// are in flight, so an entry's global-memory latency overlaps the arithmetic of the ones
+// before it (four stages measured no faster than two on the 256-problem batch).  The rows'
+// per-(term, dimension) block bases sit in a shared table; the fiber indexing uses shifts
+// for deg 2 and 4 and a multiply by a reciprocal for deg 3 instead of divisions.
+template <typename T, int P, int R>
+__device__ __forceinline__ void warp_rows(const BatchProblem& pb, int row0, int nrows, unsigned char* wsm, int lane) {
   constexpr int MAXE = 8;
   constexpr bool KAHAN = sizeof(T) == 4;
   constexpr int LG = P == 2 ? 1 : (P == 4 ? 2 : 0);  // log2(P) when P is a power of two
   constexpr int S = kBatchStages;
+  constexpr int L = 32 / R;  // lanes per row
+  const int sub = lane / L, sl = lane - sub * L;
+  const bool on = sub < nrows;  // this lane's row exists
+  const int row = row0 + (on ? sub : 0);
   long long* abase = reinterpret_cast<long long*>(wsm);
-  unsigned* acts = reinterpret_cast<unsigned*>(wsm + kMaxTerms * kMaxDims * sizeof(long long));  // [S]
+  unsigned* acts = reinterpret_cast<unsigned*>(wsm + kMaxTerms * kMaxDims * sizeof(long long));  // [S][R]
   T* stage = reinterpret_cast<T*>(wsm + kWarpHdr);  // [S][256]
   T* work = stage + S * kStageVals;                 // [2][256]
   T* amat = work + 2 * kStageVals;                  // [S][kAmatVals]
   const T* f = static_cast<const T*>(pb.f);
   T* y = static_cast<T*>(pb.y);
   const T* ops = sizeof(T) == 8 ? reinterpret_cast<const T*>(pb.ops64) : reinterpret_cast<const T*>(pb.ops32);
-  const int B = pb.B, D = pb.D, nt = pb.T;
+  const int B = pb.B, D = pb.D, nt = pb.T, TD = nt * D;
+  constexpr int PP = P * P;
+  // each row's slices: stage and chain buffers B values apart, factor blocks D*P^2 apart
+  const int so = sub * B, ao = sub * D * PP;
   // block base of operator (t, m) at this row's 1-D index: op_off + I_m(row) * nb * P^2
-  for (int k = lane; k < nt * D; k += 32) {
+  for (int k = sl; k < TD; k += L) {
     const long long off = pb.op_off[k];
-    abase[k] = off < 0 ? 0 : off + static_cast<long long>(pb.idx1d[row * D + k % D]) * pb.op_nb[k] * (P * P);
+    abase[sub * TD + k] =
+        off < 0 ? 0 : off + static_cast<long long>(pb.idx1d[row * D + k % D]) * pb.op_nb[k] * PP;
   }
   __syncwarp();
-  // issue the copies of entry q into stage st: the column block and every applied factor block
-  // (16-byte pieces where the alignment allows: f blocks when pb.vec, factor blocks for
-  // deg 2 and 4, whose P x P blocks are whole 16-byte multiples at aligned offsets)
+  // issue the copies of this row's entry q into stage st: the column block and every applied
+  // factor block (16-byte pieces where the alignment allows: f blocks when pb.vec, factor
+  // blocks for deg 2 and 4, whose P x P blocks are whole 16-byte multiples at aligned offsets)
   auto issue = [&](long long q, int st) {
     const int e = pb.ent[q];
     const int j = e >> 4, t = e & 15;
     const unsigned act = pb.active[t];
     const T* src = f + static_cast<size_t>(j) * B;
-    T* dst = stage + st * kStageVals;
+    T* dst = stage + st * kStageVals + so;
     constexpr int V = 16 / static_cast<int>(sizeof(T));
     if (pb.vec) {
-      for (int k = lane * V; k < B; k += 32 * V) cp_async16(dst + k, src + k);
+      for (int k = sl * V; k < B; k += L * V) cp_async16(dst + k, src + k);
     } else {
-      for (int k = lane; k < B; k += 32) cp_async_elem(dst + k, src + k);
+      for (int k = sl; k < B; k += L) cp_async_elem(dst + k, src + k);
     }
-    T* ad = amat + st * kAmatVals;
-    if constexpr ((P * P) % V == 0) {
-      constexpr int PV = P * P / V;  // 16-byte pieces per factor block
-      for (int k = lane; k < D * PV; k += 32) {
+    T* ad = amat + st * kAmatVals + ao;
+    const long long* ab = abase + sub * TD + t * D;
+    if constexpr (PP % V == 0) {
+      constexpr int PV = PP / V;  // 16-byte pieces per factor block
+      for (int k = sl; k < D * PV; k += L) {
         const int m = k / PV, r = (k - m * PV) * V;
-        if ((act >> m) & 1u)
-          cp_async16(ad + m * 16 + r, ops + abase[t * D + m] + static_cast<long long>(pb.idx1d[j * D + m]) * (P * P) + r);
+        if ((act >> m) & 1u) cp_async16(ad + m * PP + r, ops + ab[m] + static_cast<long long>(pb.idx1d[j * D + m]) * PP + r);
       }
     } else {
-      for (int k = lane; k < D * P * P; k += 32) {
-        const int m = k / (P * P), r = k - m * (P * P);
-        if ((act >> m) & 1u)
-          cp_async_elem(ad + m * 16 + r,
-                        ops + abase[t * D + m] + static_cast<long long>(pb.idx1d[j * D + m]) * (P * P) + r);
+      for (int k = sl; k < D * PP; k += L) {
+        const int m = k / PP, r = k - m * PP;
+        if ((act >> m) & 1u) cp_async_elem(ad + m * PP + r, ops + ab[m] + static_cast<long long>(pb.idx1d[j * D + m]) * PP + r);
       }
     }
     return act;
@@ -139,37 +150,44 @@ __device__ __forceinline__ void warp_row(const BatchProblem& pb, int row, unsign
   T acc[MAXE], cmp[MAXE];
 #pragma unroll
   for (int k = 0; k < MAXE; ++k) acc[k] = cmp[k] = T(0);
-  const long long q0 = pb.row_ptr[row], q1 = pb.row_ptr[row + 1];
+  const long long q0 = on ? pb.row_ptr[row] : 0, q1 = on ? pb.row_ptr[row + 1] : 0;
+  // the rows' entry counts may differ: the warp runs to the longest, each row's lanes idle
+  // past their own end (the batch's all-pairs rows all have N * T entries)
+  long long n = q1 - q0;
+  for (int off = L; off < 32; off <<= 1) n = max(n, __shfl_xor_sync(0xffffffffu, n, off));
   // entries q0 .. q0+S-2 in flight first (one commit group each, empty past the row's end)
   for (int k = 0; k < S - 1; ++k) {
     if (q0 + k < q1) {
       const unsigned a0 = issue(q0 + k, k);
-      if (lane == 0) acts[k] = a0;
+      if (sl == 0) acts[k * R + sub] = a0;
     }
     cp_async_commit();
   }
-  for (long long q = q0; q < q1; ++q) {
-    const int cur = static_cast<int>((q - q0) % S);
+  for (long long kq = 0; kq < n; ++kq) {
+    const long long q = q0 + kq;
+    const int cur = static_cast<int>(kq % S);
     if (q + S - 1 < q1) {  // refill the stage consumed by entry q-1
       const int nx = (cur + S - 1) % S;
       const unsigned a1 = issue(q + S - 1, nx);
-      if (lane == 0) acts[nx] = a1;
+      if (sl == 0) acts[nx * R + sub] = a1;
     }
     cp_async_commit();
     cp_async_wait_pending<S - 1>();  // this lane's copies of entry q have landed
-    __syncwarp();                    // ... and every lane's (and acts[cur])
-    const unsigned act = acts[cur];
-    const T* in = stage + cur * kStageVals;
-    const T* Am = amat + cur * kAmatVals;
+    __syncwarp();                    // ... and every lane's (and acts)
+    const bool live = q < q1;        // this row still has entry q
+    const unsigned act = live ? acts[cur * R + sub] : 0u;
+    const T* in = stage + cur * kStageVals + so;
+    const T* Am = amat + cur * kAmatVals + ao;
     int wsel = 0;
     int s = 1, sh = 0;  // stride P^(D-1-m) of dimension m; for P = 2, 4: s = 1 << sh
     for (int m = D - 1; m >= 0; --m, s *= P, sh += LG) {
-      if (!((act >> m) & 1u)) continue;
-      T A[P * P];
+      const bool applied = (act >> m) & 1u;
+      if (!__any_sync(0xffffffffu, applied)) continue;
+      T A[PP];
       if constexpr (sizeof(T) == 4 && P == 4) {  // four 16-byte shared loads
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
-          const float4 v = reinterpret_cast<const float4*>(Am + m * 16)[r];
+          const float4 v = reinterpret_cast<const float4*>(Am + m * PP)[r];
           A[4 * r] = v.x;
           A[4 * r + 1] = v.y;
           A[4 * r + 2] = v.z;
@@ -177,56 +195,77 @@ __device__ __forceinline__ void warp_row(const BatchProblem& pb, int row, unsign
         }
       } else {
 #pragma unroll
-        for (int r = 0; r < P * P; ++r) A[r] = Am[m * 16 + r];
+        for (int r = 0; r < PP; ++r) A[r] = Am[m * PP + r];
       }
-      T* out = work + wsel * kStageVals;
-      for (int fi = lane; fi < B / P; fi += 32) {
-        int hi, lo;
-        if constexpr (LG > 0) {
-          hi = fi >> sh;
-          lo = fi & (s - 1);
-        } else {
-          hi = fi / s;
-          lo = fi - hi * s;
-        }
-        const int base = hi * s * P + lo;
-        T x[P];
+      T* out = work + wsel * kStageVals + so;
+      // fi / s without a division for deg 3 (s = 3^k): fi * ceil(2^16 / s) >> 16, exact for
+      // fi < 256 and s <= 81 (checked exhaustively); deg 1 has s = 1
+      const unsigned rs = P == 3 ? c_recip3[D - 1 - m] : 65536u;
+      if (applied) {
+        for (int fi = sl; fi < B / P; fi += L) {
+          int hi, lo;
+          if constexpr (LG > 0) {
+            hi = fi >> sh;
+            lo = fi & (s - 1);
+          } else {
+            hi = static_cast<int>((static_cast<unsigned>(fi) * rs) >> 16);
+            lo = fi - hi * s;
+          }
+          const int base = hi * s * P + lo;
+          T x[P];
 #pragma unroll
-        for (int b = 0; b < P; ++b) x[b] = in[base + b * s];
+          for (int b = 0; b < P; ++b) x[b] = in[base + b * s];
 #pragma unroll
-        for (int a = 0; a < P; ++a) {
-          T sum = A[a * P] * x[0];
+          for (int a = 0; a < P; ++a) {
+            T sum = A[a * P] * x[0];
 #pragma unroll
-          for (int b = 1; b < P; ++b) sum = fma(A[a * P + b], x[b], sum);
-          out[base + a * s] = sum;
+            for (int b = 1; b < P; ++b) sum = fma(A[a * P + b], x[b], sum);
+            out[base + a * s] = sum;
+          }
         }
       }
       __syncwarp();
-      in = out;
-      wsel ^= 1;
+      if (applied) {
+        in = out;
+        wsel ^= 1;
+      }
     }
+    if (live) {
 #pragma unroll
-    for (int k = 0; k < MAXE; ++k) {
-      const int idx = lane + 32 * k;
-      if (idx < B) {
-        if (KAHAN) {
-          const T yv = in[idx] - cmp[k];
-          const T tt = acc[k] + yv;
-          cmp[k] = (tt - acc[k]) - yv;
-          acc[k] = tt;
-        } else {
-          acc[k] += in[idx];
+      for (int k = 0; k < MAXE; ++k) {
+        const int idx = sl + L * k;
+        if (idx < B) {
+          if (KAHAN) {
+            const T yv = in[idx] - cmp[k];
+            const T tt = acc[k] + yv;
+            cmp[k] = (tt - acc[k]) - yv;
+            acc[k] = tt;
+          } else {
+            acc[k] += in[idx];
+          }
         }
       }
     }
     __syncwarp();  // stage cur is refilled by the next iteration's copies
   }
-  T* yr = y + static_cast<size_t>(row) * B;
+  if (on) {
+    T* yr = y + static_cast<size_t>(row) * B;
 #pragma unroll
-  for (int k = 0; k < MAXE; ++k) {
-    const int idx = lane + 32 * k;
-    if (idx < B) yr[idx] = acc[k];
+    for (int k = 0; k < MAXE; ++k) {
+      const int idx = sl + L * k;
+      if (idx < B) yr[idx] = acc[k];
+    }
   }
+}
+
+template <typename T, int P>
+__device__ __forceinline__ void rows_deg(const BatchProblem& pb, int row, int nr, int R, unsigned char* wsm, int lane) {
+  if (R == 4)
+    warp_rows<T, P, 4>(pb, row, nr, wsm, lane);
+  else if (R == 2)
+    warp_rows<T, P, 2>(pb, row, nr, wsm, lane);
+  else
+    warp_rows<T, P, 1>(pb, row, nr, wsm, lane);
 }
 
 template <typename T>
@@ -243,12 +282,14 @@ __global__ void k_batch(const BatchProblem* __restrict__ probs, const BatchItem*
     const BatchItem w = items[it];
     const BatchProblem pb = probs[w.prob];
     const int r1 = min(pb.N, w.row + rows_per_item);
-    for (int row = w.row; row < r1; ++row) {
+    const int R = min(pb.R, rows_per_item);
+    for (int row = w.row; row < r1; row += R) {
+      const int nr = min(R, r1 - row);
       switch (pb.P) {
-        case 1: warp_row<T, 1>(pb, row, wsm, lane); break;
-        case 2: warp_row<T, 2>(pb, row, wsm, lane); break;
-        case 3: warp_row<T, 3>(pb, row, wsm, lane); break;
-        case 4: warp_row<T, 4>(pb, row, wsm, lane); break;
+        case 1: rows_deg<T, 1>(pb, row, nr, R, wsm, lane); break;
+        case 2: rows_deg<T, 2>(pb, row, nr, R, wsm, lane); break;
+        case 3: rows_deg<T, 3>(pb, row, nr, R, wsm, lane); break;
+        case 4: rows_deg<T, 4>(pb, row, nr, R, wsm, lane); break;
         default: break;  // rejected at batch creation
       }
     }
@@ -328,6 +369,15 @@ asg_status asg_batch_create(asg_plan* const* plans, int count, asg_batch** out) 
     pb.B = p->B;
     pb.P = p->P;
     pb.T = p->T;
+    // rows side by side: each row's block-base table (T*D), stage (B) and factor blocks
+    // (D*deg^2) must fit the warp's buffers, the stages' masks (kBatchStages*R) its header
+    pb.R = 1;
+    for (int r = 4; r > 1; r /= 2)
+      if (r * p->T * p->D <= asg::kMaxTerms * asg::kMaxDims && r * p->B <= asg::kStageVals &&
+          r * p->D * p->P * p->P <= asg::kAmatVals && r * asg::kBatchStages <= 16) {
+        pb.R = r;
+        break;
+      }
     int sd = 1;
     for (int m = p->D - 1; m >= 0; --m) {
       pb.stride[m] = sd;
@@ -482,6 +532,19 @@ asg_status asg_batch_tune(asg_batch* b, int precision, void* stream, float* best
   b->wpb = bw;
   b->rpi_choice = bc;
   if (best_ms) *best_ms = best / 3;
+  return ASG_OK;
+}
+
+asg_status asg_batch_configure(asg_batch* b, int warps_per_cta, int rows_per_item) {
+  if (!b) return fail(ASG_ERR_INVALID, "batch_configure: NULL batch");
+  if (warps_per_cta != 4 && warps_per_cta != 8)
+    return fail(ASG_ERR_INVALID, "batch_configure: warps_per_cta=%d (4 or 8)", warps_per_cta);
+  int c = -1;
+  for (int k = 0; k < 3; ++k)
+    if (kRowsPerItem[k] == rows_per_item) c = k;
+  if (c < 0) return fail(ASG_ERR_INVALID, "batch_configure: rows_per_item=%d (1, 2 or 4)", rows_per_item);
+  b->wpb = warps_per_cta;
+  b->rpi_choice = c;
   return ASG_OK;
 }
 

@@ -180,6 +180,10 @@ asg_status asg_batch_prepare(asg_batch* batch, int precision);
 asg_status asg_batch_apply(asg_batch* batch, int precision, void* stream);
 /* Times (warps per CTA, rows per work item) candidates and keeps the fastest. */
 asg_status asg_batch_tune(asg_batch* batch, int precision, void* stream, float* best_ms);
+/* Sets the launch shape instead of tuning: warps per CTA (4 or 8) and rows per work item (1,
+ * 2 or 4; a warp computes up to that many rows of a problem side by side when the problem's
+ * blocks are small).  Results do not depend on the shape. */
+asg_status asg_batch_configure(asg_batch* batch, int warps_per_cta, int rows_per_item);
 asg_status asg_batch_info(const asg_batch* batch, int* warps_per_cta, int* rows_per_item, double* flops);
 
 /* ---------------------------------------------------------------------------------------

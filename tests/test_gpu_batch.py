@@ -82,6 +82,53 @@ def test_batch_matches_single_plans_and_oracle(dev):
     assert info["warps_per_cta"] in (4, 8) and info["rows_per_item"] in (1, 2, 4)
 
 
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_batch_launch_shapes_bitwise(dev, dtype):
+    """Every (warps per CTA, rows per item) shape equals the single-plan launches bitwise: a
+    warp computes up to four rows of a small-block problem side by side (deg 1..4, d 2..4,
+    row counts not multiples of the rows per item), each with the single-row arithmetic."""
+    import asgkron
+    from asgkron.batch import Batch
+
+    rng = np.random.default_rng(11)
+    plans, fs = [], []
+    for deg in (1, 2, 3, 4):
+        for d in (2, 3, 4):
+            lev = 3
+            table = asgkron.hash_table_sparse_nD([lev] * d, 8)
+            n = deg * 2 ** lev
+            mats = [[rng.normal(0.0, 1.0 / np.sqrt(deg), (n, n)) for _ in range(d)] for _ in range(d)]
+            plans.append(asgkron.Plan.create(mats, table.idx1d(), deg, structure="detect"))
+            fs.append(torch.from_numpy(rng.standard_normal(table.num_elems * deg ** d)).to(dev, getattr(torch, dtype)))
+    singles = [p.apply(f) for p, f in zip(plans, fs)]
+    ys = [torch.empty_like(f) for f in fs]
+    b = Batch(plans)
+    b.set_io(fs, ys)
+    for wpb, rpi in ((4, 1), (8, 2), (4, 4)):
+        b.configure(wpb, rpi)
+        for y in ys:
+            y.fill_(float("nan"))
+        b.apply()
+        torch.cuda.synchronize()
+        assert b.info()["rows_per_item"] == rpi
+        for k, (y, want) in enumerate(zip(ys, singles)):
+            assert torch.equal(y, want), (wpb, rpi, k)
+
+
+def test_batch_configure_rejects_bad_shapes(dev):
+    import asgkron
+    from asgkron._lib import AsgError
+    from asgkron.batch import Batch
+    from cases import problem
+
+    _, _, idx, mats = problem("continuity2", 3, 2)
+    b = Batch([asgkron.Plan.create(mats, idx, 2)])
+    with pytest.raises(AsgError, match="warps_per_cta=6"):
+        b.configure(6, 1)
+    with pytest.raises(AsgError, match="rows_per_item=3"):
+        b.configure(4, 3)
+
+
 def test_batch_rejects_large_blocks(dev):
     import asgkron
     from asgkron._lib import AsgError
