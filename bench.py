@@ -365,8 +365,9 @@ def run_batched(args, rank, local):
     degree ~ U{2..4} (seed 3), d terms of dense N(0, 1/deg) 1-D operators (no structure, so
     every (pair, term) of all N^2 pairs is executed: the reference work model), f ~ N(0,1).
     One step = one persistent launch over all problems (FP32, tuned, replayed from a CUDA
-    graph).  Baseline: the same problems as sequential FP64 single-problem launches.  The inputs (62 MB of f,
-    6.3 GB of work lists) exceed L2, so no flush is needed."""
+    graph).  Baseline: the same problems as sequential FP64 single-problem launches.  The inputs of
+    the 256-problem draw (62 MB of f, 5.8 GB of work lists at 4 bytes per work entry) exceed L2, so
+    no flush is needed; config["l2"] reports the size of the draw actually run."""
     import numpy as np
     import torch
 
@@ -379,7 +380,7 @@ def run_batched(args, rank, local):
     torch.cuda.set_device(dev)
     rng = np.random.default_rng(3)
     plans, f64s = [], []
-    flops = 0.0
+    flops, wl_bytes = 0.0, 0
     for _ in range(args.batch_problems):
         d = int(rng.choice([2, 3, 4]))
         lev = int(rng.integers(3, args.batch_max_level + 1))
@@ -389,7 +390,9 @@ def run_batched(args, rank, local):
         mats = [[rng.normal(0.0, 1.0 / np.sqrt(deg), (n, n)) for _ in range(d)] for _ in range(d)]
         p = asgkron.Plan.create(mats, idx, deg, structure="none")
         p.term_mats = None  # the plan holds its own packed copy; drop the host operators
-        flops += p.stats()["flops_executed"]
+        st = p.stats()
+        flops += st["flops_executed"]
+        wl_bytes += 4 * st["num_entries"]  # one 4-byte (column, term) word per work entry
         plans.append(p)
         f64s.append(torch.from_numpy(rng.standard_normal(p.dof)).to(dev))
     dof = sum(p.dof for p in plans)
@@ -446,7 +449,8 @@ def run_batched(args, rank, local):
         "data": "synthetic (dense N(0,1/deg) operators, f ~ N(0,1), seed 3)",
         "config": {"workload": "batched: %d problems, d in {2,3,4}, SG lev 3..%d, deg 2..4, all pairs"
                                % (args.batch_problems, args.batch_max_level),
-                   "dof": dof, "flops_per_step": flops, "l2": "inputs larger than L2 (6.3 GB work lists)",
+                   "dof": dof, "flops_per_step": flops, "l2": ("inputs larger than L2 (%.3g GB work lists)" if wl_bytes > 129e6 else
+                          "work lists within L2 (%.3g GB), no flush") % (wl_bytes / 1e9),
                    "launch": "one persistent launch replayed from a CUDA graph", "tuned": info},
         "compute": {"gflops_per_s": flops / (ms * 1e-3) / 1e9},
         "variants": {"fp64_sequential_launches": {"count": len(plans), "ms": ms64, "value": dof / (ms64 * 1e-3) / 1e9,
