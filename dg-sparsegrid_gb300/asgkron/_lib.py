@@ -49,6 +49,17 @@ class PlanDesc(C.Structure):
     ]
 
 
+class PartialTermDesc(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int),
+        ("LF", C.c_double),
+        ("bcl", C.c_char),
+        ("bcr", C.c_char),
+        ("g_quad", C.POINTER(C.c_double)),
+        ("g_face", C.POINTER(C.c_double)),
+    ]
+
+
 class PlanStats(C.Structure):
     _fields_ = [
         ("num_pairs", C.c_longlong),
@@ -84,6 +95,7 @@ class GmresInfo(C.Structure):
 
 _P = C.c_void_p
 _I = C.POINTER(C.c_int)
+_D = C.POINTER(C.c_double)
 
 # name -> (restype, argtypes); every symbol include/asgkron.h declares
 SIGNATURES = {
@@ -144,6 +156,11 @@ SIGNATURES = {
     "asg_be_solve": (C.c_int, [C.c_void_p, C.c_double, _P, _P, C.POINTER(GmresOpts), C.POINTER(GmresInfo), _P,
                                C.c_size_t, _P]),
     "asg_debug_withhold_arrival": (C.c_int, [C.c_int]),
+    "asg_gauss_legendre_f64": (C.c_int, [C.c_int, C.c_double, C.c_double, _D, _D]),
+    "asg_multiwavelet_filters_f64": (C.c_int, [C.c_int, _D, _D]),
+    "asg_fmwt_matrix_f64": (C.c_int, [C.c_int, C.c_int, _D]),
+    "asg_coeff_matrix_f64": (C.c_int, [C.c_int, C.c_int, C.c_double, C.c_double, C.c_int,
+                                       C.POINTER(PartialTermDesc), _D]),
 }
 
 _LIB = None

@@ -237,10 +237,8 @@ def realspace_matrix(deg, lo, hi, lev, pt):
                     nbr = [(c - 1) % N, c, c, (c + 1) % N]
                 else:
                     nbr = [c, c, c, c]
-            elif c == 0:
-                use = [1, 2, 3]
-            elif c == N - 1:
-                use = [0, 1, 2]
+            else:  # no neighbour outside the domain (a single cell has neither)
+                use = [b for b in use if 0 <= nbr[b] < N]
             for b in use:
                 M[c * deg:(c + 1) * deg, nbr[b] * deg:(nbr[b] + 1) * deg] += blocks[b]
         if pt.kind == "grad":

@@ -41,8 +41,15 @@ class PDE:
         ml = max_lev if max_lev is not None else max(8, max(self.levels))
         return _grid.hash_table_sparse_nD(self.levels, ml, grid_type)
 
-    def term_mats(self, deg, construction_level=None):
-        """pde.terms{t}.terms_1D{d}.mat for every term (get_coeff_mats.m:29-50)."""
+    def term_mats(self, deg, construction_level=None, builder="native"):
+        """pde.terms{t}.terms_1D{d}.mat for every term (get_coeff_mats.m:29-50).  builder
+        "native" runs the C++ builder (asg_coeff_matrix_f64: realspace chain, one rotation);
+        "numpy" rotates every partial term and solves the mass in wavelet space as the
+        reference does.  The two agree to the transform's orthogonality round-off."""
+        if builder not in ("numpy", "native"):
+            raise ValueError("builder must be 'numpy' or 'native', not %r" % (builder,))
+        if builder == "native":
+            from . import coeff as _coeff
         cache = {}
         out = []
         for t in self.terms:
@@ -52,7 +59,8 @@ class PDE:
                 lev = self.levels[d] if construction_level is None else construction_level
                 key = (d, lev, tuple((p.kind, p.LF, p.bcl, p.bcr, id(p.g)) for p in pts))
                 if key not in cache:
-                    cache[key] = term_matrix(deg, lo, hi, lev, pts)
+                    build = _coeff.term_matrix if builder == "native" else term_matrix
+                    cache[key] = build(deg, lo, hi, lev, pts)
                 row.append(cache[key])
             out.append(row)
         return out

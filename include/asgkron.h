@@ -162,6 +162,35 @@ asg_status asg_connect_nd(int num_dims, long long num_elems, const int* levels, 
                           long long capacity, long long* num_pairs);
 
 /* ---------------------------------------------------------------------------------------
+ * Producer of the path's inputs on the host: wavelet-space 1-D DG operators
+ * ------------------------------------------------------------------------------------- */
+/* n-point Gauss-Legendre rule on [a, b], nodes ascending (Quadrature/lgwt.m). */
+asg_status asg_gauss_legendre_f64(int n, double a, double b, double* x, double* w);
+/* Two-scale filters H0, G0 (deg x deg, row-major) of the Alpert multiwavelets
+ * (two_scale/MultiwaveletGen.m; entries below 1e-5 zeroed). */
+asg_status asg_multiwavelet_filters_f64(int deg, double* H0, double* G0);
+/* Forward multiwavelet transform F (n x n, n = deg 2^lev <= 16384, row-major): rows are the
+ * level-0 scaling functions, then the wavelets level by level, cells left to right
+ * (OperatorTwoScale_wavelet2.m:127-144). */
+asg_status asg_fmwt_matrix_f64(int deg, int lev, double* F);
+/* One partial term of a 1-D operator (PARTIAL_SD_TERM.m with MASS.m / DIV.m / GRAD.m). */
+typedef struct asg_partial_term {
+  int kind;              /* 0 mass, 1 div, 2 grad */
+  double LF;             /* flux parameter as given to DIV / GRAD (GRAD negates it) */
+  char bcl, bcr;         /* 'P', 'D' or 'N' as given (GRAD swaps D and N) */
+  const double* g_quad;  /* [2^lev][nq] coefficient g at each cell's Gauss nodes, cells
+                          * left to right, nq = max(deg + 1, 10) nodes of
+                          * asg_gauss_legendre_f64(nq, -1, 1) mapped to the cell; NULL = 1 */
+  const double* g_face;  /* [2^lev + 1] g at the cell faces lo + c h; NULL = 1 */
+} asg_partial_term;
+/* pde.terms{t}.terms_1D{d}.mat: the chain (M \ L_1)(M \ L_2)... of partial terms with the
+ * unit LHS mass, in wavelet space (n x n row-major; coeff_matrix.m:105-342,
+ * pterm_coeff_matrix.m:6-20, sd_term_coeff_matrix.m:9-22).  Chained in realspace and rotated
+ * once by F: equal to rotating each factor to the transform's orthogonality round-off. */
+asg_status asg_coeff_matrix_f64(int deg, int lev, double lo, double hi, int nterms, const asg_partial_term* terms,
+                                double* out);
+
+/* ---------------------------------------------------------------------------------------
  * Many independent problems in one persistent launch (no reference counterpart: the
  * prototype applies one operator at a time)
  * ------------------------------------------------------------------------------------- */

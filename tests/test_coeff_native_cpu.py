@@ -1,0 +1,120 @@
+"""The native (C++) 1-D operator builder (asg_coeff_matrix_f64 and its helpers, asgkron.coeff)
+against the reference's quadrature / two-scale / transform gold data, the oracle's
+restatement of coeff_matrix.m, and the numpy builder.  Host code only: no GPU needed."""
+import os
+
+import numpy as np
+import pytest
+
+from asgkron import coeff as N
+from asgkron import operators as P
+from asgkron import pdes
+from asgkron._lib import AsgError
+from oracle import asgard_oracle as O
+
+G = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def test_native_gauss_legendre_gold():
+    q = np.load(os.path.join(G, "quadrature.npz"))
+    x, w = N.gauss_legendre(32, -5, 2)
+    np.testing.assert_allclose(x, q["lgwt_roots_32_neg5_2"].ravel(), atol=5e-15)
+    np.testing.assert_allclose(w, q["lgwt_weights_32_neg5_2"].ravel(), atol=5e-16)
+    x, w = N.gauss_legendre(1, 0.0, 3.0)
+    assert x[0] == 1.5 and w[0] == 3.0
+
+
+@pytest.mark.parametrize("k", range(1, 9))
+def test_native_multiwavelet_filters_match_reference_mat(k):
+    z = np.load(os.path.join(G, "two_scale_rel.npz"))
+    H0, G0 = N.multiwavelet_filters(k)
+    tol = 1e-14 if k <= 5 else 5e-12  # Gram-Schmidt round-off grows with the degree
+    np.testing.assert_allclose(H0, z["H0_%d" % k], rtol=0, atol=tol)
+    np.testing.assert_allclose(G0, z["G0_%d" % k], rtol=0, atol=tol)
+
+
+@pytest.mark.parametrize("deg,lev", [(2, 2), (2, 3), (4, 3), (5, 5)])
+def test_native_fmwt_matches_gold(deg, lev):
+    t = np.load(os.path.join(G, "transformations.npz"))
+    np.testing.assert_allclose(N.fmwt_matrix(deg, lev), t["operator_two_scale_%d_%d" % (deg, lev)], atol=2e-14)
+
+
+@pytest.mark.parametrize("deg,lev", [(1, 0), (3, 0), (1, 4), (3, 4), (4, 6)])
+def test_native_fmwt_matches_numpy_and_is_orthogonal(deg, lev):
+    F = N.fmwt_matrix(deg, lev)
+    assert np.abs(F - P.fmwt_matrix(deg, lev)).max() <= 1e-14
+    assert np.abs(F @ F.T - np.eye(F.shape[0])).max() <= 1e-13
+
+
+@pytest.mark.parametrize("name,lev,deg", [("continuity2", 4, 2), ("continuity3", 3, 3), ("diffusion2", 3, 4),
+                                          ("continuity2", 3, 4)])
+def test_native_term_mats_match_oracle(name, lev, deg):
+    prod = getattr(pdes, name)(lev) if name == "diffusion2" else getattr(pdes, name)(lev, -1.0)
+    orac = getattr(O, name)(lev) if name == "diffusion2" else getattr(O, name)(lev, LF=-1.0)
+    A = prod.term_mats(deg, builder="native")
+    B = O.build_term_mats(orac, deg)
+    for ra, rb in zip(A, B):
+        for a, b in zip(ra, rb):
+            assert np.abs(a - b).max() <= 1e-13 * np.abs(b).max()
+
+
+def _g_var(x):
+    return 1.5 + np.sin(x)  # a non-constant coefficient, positive on the interval
+
+
+def _g_sign(x):
+    return x - 0.2  # changes sign inside [-1, 1]: exercises the |g| of the flux
+
+
+@pytest.mark.parametrize("deg", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("lev", [0, 1, 2, 5])
+def test_native_term_matrix_matches_numpy_builder(deg, lev):
+    """Every partial-term kind, flux and boundary pairing the builder distinguishes, constant
+    and variable coefficients, single terms and LDG-style chains, on 1 / 2 / 4 / 32 cells
+    (periodic wrap on one and two cells included)."""
+    cases = []
+    for bcl, bcr in (("P", "P"), ("D", "D"), ("N", "N"), ("D", "N"), ("N", "D")):
+        for LF in (0.0, -1.0, 1.0):
+            cases.append([P.div_term(None, LF, bcl, bcr)])
+            cases.append([P.grad_term(_g_var, LF, bcl, bcr)])
+            cases.append([P.div_term(_g_sign, LF, bcl, bcr), P.grad_term(None, LF, bcl, bcr)])
+    cases.append([P.mass_term(_g_var)])
+    cases.append([P.mass_term(), P.div_term(_g_var, -1.0, "P", "P"), P.mass_term(_g_var)])
+    for pts in cases:
+        a = P.term_matrix(deg, -1.0, 1.0, lev, pts)
+        b = N.term_matrix(deg, -1.0, 1.0, lev, pts)
+        # a periodic single-cell div of a constant cancels to round-off: the floor is the
+        # size of its parts (1/h on cells of width 2/2^lev)
+        scale = max(np.abs(a).max(), 2.0 ** lev / 2)
+        assert np.abs(a - b).max() <= 5e-13 * scale, ([p.kind for p in pts], pts[0].BCL, pts[0].BCR)
+
+
+def test_native_builder_on_a_shifted_interval():
+    pts = [P.div_term(_g_var, -1.0, "D", "N"), P.grad_term(None, -1.0, "D", "N")]
+    a = P.term_matrix(3, 0.5, 4.0, 4, pts)
+    b = N.term_matrix(3, 0.5, 4.0, 4, pts)
+    assert np.abs(a - b).max() <= 5e-13 * np.abs(a).max()
+
+
+def test_native_builder_rejects_bad_arguments():
+    with pytest.raises(AsgError, match="deg=0"):
+        N.multiwavelet_filters(0)
+    with pytest.raises(AsgError, match="lev=-1"):
+        N.fmwt_matrix(2, -1)
+    with pytest.raises(AsgError, match="deg\\*2\\^lev"):
+        N.fmwt_matrix(4, 13)
+    with pytest.raises(AsgError, match="n=0"):
+        N.gauss_legendre(0)
+    with pytest.raises(AsgError, match="empty interval"):
+        N.term_matrix(2, 1.0, 1.0, 2, [P.mass_term()])
+    bad = P.div_term(None, 0.0, "X", "P")
+    with pytest.raises(AsgError, match="boundary types"):
+        N.term_matrix(2, 0.0, 1.0, 2, [bad])
+    bad = P.mass_term()
+    bad.kind = "curl"
+    with pytest.raises(KeyError):
+        N.term_matrix(2, 0.0, 1.0, 2, [bad])
+    with pytest.raises(ValueError, match="at least one"):
+        N.term_matrix(2, 0.0, 1.0, 2, [])
+    with pytest.raises(ValueError, match="builder"):
+        pdes.continuity2(2, -1.0).term_mats(2, builder="fortran")
