@@ -462,20 +462,34 @@ static asg_status coeff_matrix(int deg, int lev, double lo, double hi, int nterm
   for (int c = 0; c < N; ++c)
     if (!invert(deg, Mr[c].v.data(), &Minv[static_cast<size_t>(c) * dd]))
       return fail(ASG_ERR_INVALID, "coeff_matrix: singular mass block at cell %d", c);
-  // factors M^-1 L_k, grouped by block row
-  std::vector<std::vector<std::vector<Block>>> fac(nterms);
+  // factors M^-1 L_k, grouped by block row.  A mass term with g = 1 at every node has the
+  // LHS mass's own matrix, so its factor is exactly the identity (the reference's
+  // M_w \ M_w) and is left out; a chain of such terms is exactly the identity.
+  std::vector<std::vector<std::vector<Block>>> fac;
   for (int k = 0; k < nterms; ++k) {
+    if (terms[k].kind == 0) {
+      bool unit_mass = true;
+      if (terms[k].g_quad)
+        for (long long x = 0; x < static_cast<long long>(N) * nq && unit_mass; ++x) unit_mass = terms[k].g_quad[x] == 1.0;
+      if (unit_mass) continue;
+    }
+    fac.emplace_back();
     const Term t{terms[k].kind, terms[k].LF, terms[k].bcl, terms[k].bcr, terms[k].g_quad, terms[k].g_face};
     std::vector<Block> L = realspace(deg, lev, lo, hi, t, xq.data(), wq.data(), nq);
-    fac[k].assign(N, {});
+    fac.back().assign(N, {});
     for (auto& bl : L) {
       const double* mi = &Minv[static_cast<size_t>(bl.r) * dd];
       std::vector<double> v(dd, 0.0);
       for (int a = 0; a < deg; ++a)
         for (int x = 0; x < deg; ++x)
           for (int b = 0; b < deg; ++b) v[a * deg + b] += mi[a * deg + x] * bl.v[x * deg + b];
-      fac[k][bl.r].push_back(Block{bl.r, bl.c, std::move(v)});
+      fac.back()[bl.r].push_back(Block{bl.r, bl.c, std::move(v)});
     }
+  }
+  if (fac.empty()) {
+    std::memset(out, 0, sizeof(double) * n * n);
+    for (long long i = 0; i < n; ++i) out[i * n + i] = 1.0;
+    return ASG_OK;
   }
   // Y = F (M^-1 L_1) (M^-1 L_2) ..., each row within its nonzero block range; then out = Y F^T
   std::vector<double> F(static_cast<size_t>(n) * n);
@@ -487,7 +501,7 @@ static asg_status coeff_matrix(int deg, int lev, double lo, double hi, int nterm
     b0[r] = c0[r] / deg;
     b1[r] = (c1[r] + deg - 1) / deg;
   }
-  for (int k = 0; k < nterms; ++k) {
+  for (size_t k = 0; k < fac.size(); ++k) {
     parallel_rows(n, [&](long long r0, long long r1) {
       for (long long r = r0; r < r1; ++r) {
         double* z = &Z[static_cast<size_t>(r) * n];

@@ -58,6 +58,19 @@ def test_native_term_mats_match_oracle(name, lev, deg):
             assert np.abs(a - b).max() <= 1e-13 * np.abs(b).max()
 
 
+@pytest.mark.parametrize("deg", [1, 2, 4, 6])
+def test_native_unit_mass_factors_are_exact_identities(deg):
+    """A unit-coefficient mass term is the LHS mass itself: its factor, and any chain of such
+    factors, is exactly the identity (the reference's M_w \\ M_w), so the plan's structure
+    detection sees identity dimensions whatever the transform's round-off."""
+    for pde in (pdes.continuity2(3, -1.0), pdes.continuity3(2, -1.0), pdes.diffusion2(3)):
+        for t_native, t in zip(pde.term_mats(deg), pde.terms):
+            for A, pts in zip(t_native, t):
+                if all(p.kind == "mass" for p in pts):
+                    assert np.array_equal(A, np.eye(A.shape[0]))
+    assert np.array_equal(N.term_matrix(deg, 0.0, 1.0, 3, [P.mass_term(), P.mass_term()]), np.eye(deg * 8))
+
+
 def _g_var(x):
     return 1.5 + np.sin(x)  # a non-constant coefficient, positive on the interval
 
