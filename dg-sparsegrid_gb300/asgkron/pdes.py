@@ -6,6 +6,7 @@ Each follows the reference's pdes/*.m file it names: domains, per-dimension part
 """
 import numpy as np
 
+from . import coeff as _coeff
 from . import grid as _grid
 from .operators import (boundary_trace, combine_dimensions, div_term, grad_term, mass_term, project_1d, pterm_matrix,
                         term_matrix)
@@ -48,8 +49,6 @@ class PDE:
         reference does.  The two agree to the transform's orthogonality round-off."""
         if builder not in ("numpy", "native"):
             raise ValueError("builder must be 'numpy' or 'native', not %r" % (builder,))
-        if builder == "native":
-            from . import coeff as _coeff
         cache = {}
         out = []
         for t in self.terms:
