@@ -131,3 +131,23 @@ def test_native_builder_rejects_bad_arguments():
         N.term_matrix(2, 0.0, 1.0, 2, [])
     with pytest.raises(ValueError, match="builder"):
         pdes.continuity2(2, -1.0).term_mats(2, builder="fortran")
+
+
+@pytest.mark.parametrize("name,pdename,lev,deg", [("continuity2_sg_l4_d3", "continuity2", 4, 3),
+                                                  ("continuity3_sg_l4_d3", "continuity3", 4, 3)])
+def test_native_operators_reproduce_gold_rk3(name, pdename, lev, deg):
+    """Five RK3 steps (the oracle's stepper and apply loop) on the native builder's operators,
+    built at max_lev 8 as the gold was, reproduce gold/generated-inputs/time_advance."""
+    opde = getattr(O, pdename)(lev, LF=0.0)
+    lv, cl, _ = O.hash_table_sparse_nd([d.lev for d in opde.dims], 8, "SG")
+    idx = O.element_idx1d(lv, cl)
+    _, blocks = O.operator_two_scale(deg, 8)
+    mats = getattr(pdes, pdename)(lev, 0.0).term_mats(deg, construction_level=8)
+    f = O.md_eval(opde, deg, opde.ic, idx, blocks, 0.0)
+    dt = opde.dt_fn(opde, 0.01)
+    ta = np.load(os.path.join(G, "time_advance.npz"))
+    for i in range(5):
+        f = O.rk3_step(lambda v: O.apply_A_rows(mats, idx, deg, v), f, i * dt, dt,
+                       lambda t: O.md_eval(opde, deg, opde.sources, idx, blocks, t))
+        g = ta["%s_t%d" % (name, i)]
+        assert np.linalg.norm(f - g) <= 1e-14 * np.linalg.norm(g), i
