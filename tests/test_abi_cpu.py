@@ -105,3 +105,55 @@ def test_global_matrix_idx_matches_definition():
     want = np.where(lev == 0, 1, 2 ** np.maximum(lev - 1, 0) + cell + 1)
     np.testing.assert_array_equal(A["element_local_index_D"][0], want)
     assert t.num_elems == 48  # continuity2 lev 4 (the CPU-runnable configuration)
+
+
+C_CALLER = r"""
+#include <stdio.h>
+#include "asgkron.h"
+
+int main(void) {
+  double x[10], w[10], H0[16], G0[16], op[64];
+  asg_partial_term div;
+  double sx = 0, sw = 0, sh = 0, so = 0;
+  int i;
+  if (asg_gauss_legendre_f64(10, -1.0, 1.0, x, w) != ASG_OK) return 2;
+  if (asg_multiwavelet_filters_f64(4, H0, G0) != ASG_OK) return 3;
+  div.kind = 1; div.LF = -1.0; div.bcl = 'P'; div.bcr = 'P'; div.g_quad = NULL; div.g_face = NULL;
+  if (asg_coeff_matrix_f64(2, 2, -1.0, 1.0, 1, &div, op) != ASG_OK) return 4;
+  if (asg_coeff_matrix_f64(0, 2, -1.0, 1.0, 1, &div, op) != ASG_ERR_INVALID) return 5;
+  for (i = 0; i < 10; ++i) { sx += x[i] * x[i]; sw += w[i]; }
+  for (i = 0; i < 16; ++i) sh += H0[i] * H0[i] + G0[i] * G0[i];
+  for (i = 0; i < 64; ++i) so += op[i] * (i + 1);
+  printf("%.17g %.17g %.17g %.17g\n", sx, sw, sh, so);
+  return 0;
+}
+"""
+
+
+def test_c_caller_links_the_library(tmp_path):
+    """A C99 program that includes only asgkron.h, links libasgkron.so and calls the host entry
+    points gets the results the Python binding gets: the boundary is plain C."""
+    import subprocess
+
+    import numpy as np
+    from asgkron import coeff, operators
+
+    src = tmp_path / "caller.c"
+    src.write_text(C_CALLER)
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(_lib._build.LIB_PATH)
+    asgkron.lib()  # built
+    r = subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-pedantic", "-I", os.path.join(ROOT, "include"),
+                        str(src), "-o", str(exe), "-L", libdir, "-lasgkron", "-Wl,-rpath," + libdir],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0, (r.returncode, r.stderr)
+    sx, sw, sh, so = (float(v) for v in r.stdout.split())
+    x, w = coeff.gauss_legendre(10)
+    H0, G0 = coeff.multiwavelet_filters(4)
+    op = coeff.term_matrix(2, -1.0, 1.0, 2, [operators.div_term(None, -1.0, "P", "P")])
+    assert abs(sx - np.sum(x * x)) <= 1e-15
+    assert abs(sw - 2.0) <= 1e-14
+    assert abs(sh - (np.sum(H0 * H0) + np.sum(G0 * G0))) <= 1e-13
+    assert abs(so - np.sum(op.ravel() * np.arange(1, 65))) <= 1e-12 * max(1.0, abs(so))
