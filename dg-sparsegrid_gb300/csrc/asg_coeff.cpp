@@ -403,43 +403,9 @@ void parallel_rows(long long n, F body) {
   for (auto& x : th) x.join();
 }
 
-}  // namespace
-
-extern "C" {
-
-asg_status asg_gauss_legendre_f64(int n, double a, double b, double* x, double* w) {
-  if (n < 1 || n > 4096 || !x || !w) return fail(ASG_ERR_INVALID, "gauss_legendre: n=%d (1..4096) and non-NULL x, w", n);
-  if (n == 1) {
-    x[0] = (a + b) / 2;
-    w[0] = b - a;
-    return ASG_OK;
-  }
-  gauss_legendre(n, a, b, x, w);
-  return ASG_OK;
-}
-
-asg_status asg_multiwavelet_filters_f64(int deg, double* H0, double* G0) {
-  if (deg < 1 || deg > 16 || !H0 || !G0) return fail(ASG_ERR_INVALID, "multiwavelet_filters: deg=%d (1..16) and non-NULL H0, G0", deg);
-  multiwavelet_filters(deg, H0, G0);
-  return ASG_OK;
-}
-
-asg_status asg_fmwt_matrix_f64(int deg, int lev, double* F) {
-  if (deg < 1 || deg > 16 || lev < 0 || (static_cast<long long>(deg) << lev) > 16384 || !F)
-    return fail(ASG_ERR_INVALID, "fmwt_matrix: deg=%d lev=%d (deg 1..16, deg*2^lev <= 16384, non-NULL F)", deg, lev);
-  const long long n = static_cast<long long>(deg) << lev;
-  try {
-    std::vector<int> c0(n), c1(n);
-    fmwt(deg, lev, F, c0.data(), c1.data());
-  } catch (const std::bad_alloc&) {
-    return fail(ASG_ERR_NOMEM, "fmwt_matrix: out of host memory");
-  }
-  return ASG_OK;
-}
-
-static asg_status coeff_matrix(int deg, int lev, double lo, double hi, int nterms, const asg_partial_term* terms,
-                               double* out) {
-  if (deg < 1 || deg > 16 || lev < 0 || (static_cast<long long>(deg) << lev) > 16384 || !out)
+asg_status coeff_matrix(int deg, int lev, double lo, double hi, int nterms, const asg_partial_term* terms,
+                        double* out) {
+  if (deg < 1 || deg > 16 || lev < 0 || lev > 14 || (static_cast<long long>(deg) << lev) > 16384 || !out)
     return fail(ASG_ERR_INVALID, "coeff_matrix: deg=%d lev=%d (deg 1..16, deg*2^lev <= 16384, non-NULL out)", deg, lev);
   if (!(hi > lo)) return fail(ASG_ERR_INVALID, "coeff_matrix: empty interval [%g, %g]", lo, hi);
   if (nterms < 1 || !terms) return fail(ASG_ERR_INVALID, "coeff_matrix: nterms=%d (>= 1 partial terms)", nterms);
@@ -542,6 +508,40 @@ static asg_status coeff_matrix(int deg, int lev, double lo, double hi, int nterm
       }
     }
   });
+  return ASG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+asg_status asg_gauss_legendre_f64(int n, double a, double b, double* x, double* w) {
+  if (n < 1 || n > 4096 || !x || !w) return fail(ASG_ERR_INVALID, "gauss_legendre: n=%d (1..4096) and non-NULL x, w", n);
+  if (n == 1) {
+    x[0] = (a + b) / 2;
+    w[0] = b - a;
+    return ASG_OK;
+  }
+  gauss_legendre(n, a, b, x, w);
+  return ASG_OK;
+}
+
+asg_status asg_multiwavelet_filters_f64(int deg, double* H0, double* G0) {
+  if (deg < 1 || deg > 16 || !H0 || !G0) return fail(ASG_ERR_INVALID, "multiwavelet_filters: deg=%d (1..16) and non-NULL H0, G0", deg);
+  multiwavelet_filters(deg, H0, G0);
+  return ASG_OK;
+}
+
+asg_status asg_fmwt_matrix_f64(int deg, int lev, double* F) {
+  if (deg < 1 || deg > 16 || lev < 0 || lev > 14 || (static_cast<long long>(deg) << lev) > 16384 || !F)
+    return fail(ASG_ERR_INVALID, "fmwt_matrix: deg=%d lev=%d (deg 1..16, deg*2^lev <= 16384, non-NULL F)", deg, lev);
+  const long long n = static_cast<long long>(deg) << lev;
+  try {
+    std::vector<int> c0(n), c1(n);
+    fmwt(deg, lev, F, c0.data(), c1.data());
+  } catch (const std::bad_alloc&) {
+    return fail(ASG_ERR_NOMEM, "fmwt_matrix: out of host memory");
+  }
   return ASG_OK;
 }
 

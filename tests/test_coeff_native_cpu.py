@@ -116,6 +116,8 @@ def test_native_builder_rejects_bad_arguments():
         N.fmwt_matrix(2, -1)
     with pytest.raises(AsgError, match="deg\\*2\\^lev"):
         N.fmwt_matrix(4, 13)
+    with pytest.raises(AsgError, match="lev=70"):
+        N.fmwt_matrix(1, 70)
     with pytest.raises(AsgError, match="n=0"):
         N.gauss_legendre(0)
     with pytest.raises(AsgError, match="empty interval"):
