@@ -467,6 +467,139 @@ def run_batched(args, rank, local):
         p.close()
 
 
+def batch_draws(count, max_level, seed=3):
+    """The batched generator's problems as (d, lev, deg, N), with every operator and f drawn
+    and discarded so that the random stream advances exactly as in run_batched."""
+    import numpy as np
+
+    import asgkron
+
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        d = int(rng.choice([2, 3, 4]))
+        lev = int(rng.integers(3, max_level + 1))
+        deg = int(rng.integers(2, 5))
+        N = asgkron.hash_table_sparse_nD([lev] * d, 8).idx1d().shape[0]
+        n = deg * 2 ** lev
+        for _ in range(d * d):
+            rng.normal(0.0, 1.0 / np.sqrt(deg), (n, n))
+        rng.standard_normal(N * deg ** d)
+        out.append((d, lev, deg, N))
+    return out
+
+
+def batch_costs(draws):
+    """Reference-model flops of each problem: all N^2 pairs x d terms x d factors x 2 deg^(d+1)."""
+    return [float(N) * N * d * d * 2.0 * deg ** (d + 1) for d, lev, deg, N in draws]
+
+
+def run_batched_sharded(args, rank, world, local):
+    """The batched configuration on ``world`` GPUs: the problems are split by cost
+    (asgkron.batch.partition_problems, no communication on the data path); each rank builds
+    its own problems (the same draws as run_batched), tunes and captures its batch, and
+    replays it.  value = all ranks' DOF / the slowest rank's time per replay (strong scaling:
+    the 256 problems are fixed)."""
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    import asgkron
+    from asgkron.batch import Batch, partition_problems
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    dist.init_process_group("nccl", device_id=dev)
+    try:
+        draws = batch_draws(args.batch_problems, args.batch_max_level)
+        mine = set(partition_problems(batch_costs(draws), world)[rank])
+        rng = np.random.default_rng(3)
+        plans, f32s = [], []
+        flops = 0.0
+        for k in range(args.batch_problems):  # the draws of run_batched, in its order
+            d = int(rng.choice([2, 3, 4]))
+            lev = int(rng.integers(3, args.batch_max_level + 1))
+            deg = int(rng.integers(2, 5))
+            idx = asgkron.hash_table_sparse_nD([lev] * d, 8).idx1d()
+            n = deg * 2 ** lev
+            mats = [[rng.normal(0.0, 1.0 / np.sqrt(deg), (n, n)) for _ in range(d)] for _ in range(d)]
+            f = rng.standard_normal(idx.shape[0] * deg ** d)
+            if k not in mine:
+                continue
+            p = asgkron.Plan.create(mats, idx, deg, structure="none")
+            p.term_mats = None
+            flops += p.stats()["flops_executed"]
+            plans.append(p)
+            f32s.append(torch.from_numpy(f).to(dev).float())
+        steps = max(1, min(args.steps, 20))
+        stream = torch.cuda.current_stream(dev)
+        ms = e2e_ms = 0.0
+        info = {}
+        if plans:
+            y32s = [torch.empty_like(f) for f in f32s]
+            b = Batch(plans)
+            b.set_io(f32s, y32s)
+            b.tune()
+            g = b.capture()
+            info = b.info()
+            for _ in range(max(3, args.warmup)):
+                g.replay()
+        torch.cuda.synchronize()
+        dist.barrier()
+        if plans:
+            s_ev, e_ev = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s_ev.record(stream)
+            for _ in range(steps):
+                g.replay()
+            e_ev.record(stream)
+        torch.cuda.synchronize()
+        dist.barrier()
+        if plans:
+            ms = s_ev.elapsed_time(e_ev) / steps
+            # end to end: pinned host f in, replay, y out, every step
+            fh = [f.cpu().pin_memory() for f in f32s]
+            yh = [torch.empty(f.shape, dtype=f.dtype).pin_memory() for f in f32s]
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(steps):
+                for h, d_ in zip(fh, f32s):
+                    d_.copy_(h, non_blocking=True)
+                g.replay()
+                for h, d_ in zip(yh, y32s):
+                    h.copy_(d_, non_blocking=True)
+                torch.cuda.synchronize()
+            e2e_ms = (time.perf_counter() - t0) / steps * 1e3
+        local_dof = sum(p.dof for p in plans)
+        red = torch.tensor([ms, e2e_ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(red, op=dist.ReduceOp.MAX)
+        tot = torch.tensor([float(local_dof), flops, float(len(plans))], dtype=torch.float64, device=dev)
+        dist.all_reduce(tot, op=dist.ReduceOp.SUM)
+        ms, e2e_ms = float(red[0]), float(red[1])
+        dof, flops_all, nprob = float(tot[0]), float(tot[1]), int(tot[2])
+        if rank == 0:
+            line = {
+                "metric": METRIC, "value": dof / (ms * 1e-3) / 1e9, "unit": UNIT, "n_gpus": world,
+                "steps": steps, "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True,
+                "scaling": "strong", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (dense N(0,1/deg) operators, f ~ N(0,1), seed 3)",
+                "config": {"workload": "batched: %d problems, d in {2,3,4}, SG lev 3..%d, deg 2..4, all pairs"
+                                       % (args.batch_problems, args.batch_max_level),
+                           "dof": int(dof), "problems": nprob, "flops_per_step": flops_all,
+                           "parallelism": "problem shards over %d ranks by cost, no data-path collective" % world,
+                           "launch": "one persistent launch per rank, replayed from a CUDA graph",
+                           "tuned_rank0": info},
+                "compute": {"gflops_per_s": flops_all / (ms * 1e-3) / 1e9},
+                "e2e": {"value": dof / (e2e_ms * 1e-3) / 1e9, "unit": UNIT, "h2d_bytes_per_step": int(4 * dof),
+                        "d2h_bytes_per_step": int(4 * dof), "ms_per_step": e2e_ms},
+                "gpu_launches": steps * 2 * world,
+            }
+            print(json.dumps(line), flush=True)
+        for p in plans:
+            p.close()
+    finally:
+        dist.destroy_process_group()
+
+
 def run_implicit(args, rank, local):
     """The implicit configuration alone (rank 0): diffusion2 SG 8, deg 4, ten backward-Euler
     steps, mixed and FP64 (see implicit_steps); one JSON line, time per step (lower is
@@ -542,7 +675,10 @@ def main():
         run_reference(args, rank)
         return
     if args.workload == "batched":
-        run_batched(args, rank, local)
+        if world > 1:
+            run_batched_sharded(args, rank, world, local)
+        else:
+            run_batched(args, rank, local)
         return
     if args.workload == "implicit":
         run_implicit(args, rank, local)

@@ -1,8 +1,28 @@
 """Many independent y_k = A_k f_k in one persistent launch (asg_batch_*), optionally captured
-into a CUDA graph."""
+into a CUDA graph; across ranks the problems are sharded with no communication
+(``partition_problems``)."""
 import ctypes as C
 
 from ._lib import check, lib
+
+
+def partition_problems(costs, nparts):
+    """Problem indices per rank, [[k, ...], ...]: longest-processing-time greedy (problems by
+    descending cost, ties by index, each to the least-loaded rank, ties to the lowest rank).
+    Every problem goes to exactly one rank and the largest load is at most the mean plus the
+    largest single cost.  Each rank's list is in ascending problem order."""
+    if nparts < 1:
+        raise ValueError("partition_problems: nparts=%d" % nparts)
+    costs = [float(c) for c in costs]
+    if any(c < 0 for c in costs):
+        raise ValueError("partition_problems: negative cost")
+    load = [0.0] * nparts
+    parts = [[] for _ in range(nparts)]
+    for k in sorted(range(len(costs)), key=lambda i: (-costs[i], i)):
+        r = min(range(nparts), key=lambda j: (load[j], j))
+        parts[r].append(k)
+        load[r] += costs[k]
+    return [sorted(p) for p in parts]
 
 
 class Batch:

@@ -105,3 +105,84 @@ def test_sharded_apply_two_gloo_ranks(tmp_path):
     err, ranges = open(out).read().split(" ", 1)
     assert float(err) <= 1e-14, (err, ranges)
     assert "[0," in ranges
+
+
+def test_partition_problems_covers_and_balances():
+    from asgkron.batch import partition_problems
+
+    rng = np.random.default_rng(7)
+    for count in (0, 1, 5, 64, 256):
+        costs = rng.lognormal(0.0, 2.0, count)
+        for nparts in (1, 2, 3, 8):
+            parts = partition_problems(costs, nparts)
+            assert len(parts) == nparts
+            flat = sorted(k for p in parts for k in p)
+            assert flat == list(range(count))  # each problem on exactly one rank
+            assert all(p == sorted(p) for p in parts)
+            if count:
+                loads = [sum(costs[k] for k in p) for p in parts]
+                assert max(loads) <= sum(costs) / nparts + max(costs) + 1e-9
+            assert parts == partition_problems(list(costs), nparts)  # deterministic
+    assert partition_problems([5.0, 1.0, 1.0, 1.0, 1.0, 1.0], 2) == [[0], [1, 2, 3, 4, 5]]
+    with pytest.raises(ValueError):
+        partition_problems([1.0], 0)
+    with pytest.raises(ValueError):
+        partition_problems([-1.0], 2)
+
+
+def test_batch_draws_follow_the_generator():
+    """bench.batch_draws advances the random stream as the batched workload draws its problems:
+    (d, lev, deg) of every problem equal an explicit replay of the draw order (scalars, d^2
+    operators, f), and N is the element count of the problem's table."""
+    import asgkron
+    import bench
+
+    draws = bench.batch_draws(6, 4)
+    rng = np.random.default_rng(3)
+    for d, lev, deg, N in draws:
+        assert (d, lev, deg) == (int(rng.choice([2, 3, 4])), int(rng.integers(3, 5)), int(rng.integers(2, 5)))
+        assert N == asgkron.hash_table_sparse_nD([lev] * d, 8).idx1d().shape[0]
+        n = deg * 2 ** lev
+        [rng.normal(0.0, 1.0 / np.sqrt(deg), (n, n)) for _ in range(d * d)]
+        rng.standard_normal(N * deg ** d)
+    assert bench.batch_draws(3, 4) == draws[:3]
+
+
+def _batch_worker(rank, world, port, out_path):
+    import torch.distributed as dist
+
+    sys.path[:0] = [ROOT, os.path.join(ROOT, "dg-sparsegrid_gb300")]
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        import bench
+        from asgkron.batch import partition_problems
+
+        draws = bench.batch_draws(24, 4)
+        costs = bench.batch_costs(draws)
+        mine = partition_problems(costs, world)[rank]
+        got = [None] * world
+        dist.all_gather_object(got, (mine, draws))
+        if rank == 0:
+            with open(out_path, "w") as fh:
+                fh.write(repr((got, costs)))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_batched_problem_shards_two_gloo_ranks(tmp_path):
+    """Two ranks draw the same problems and take disjoint, covering, cost-balanced shares of
+    them without exchanging any problem data (the batched configuration's sharding)."""
+    pytest.importorskip("torch")
+    import torch.multiprocessing as mp
+
+    out = str(tmp_path / "shards.txt")
+    mp.start_processes(_batch_worker, args=(2, _free_port(), out), nprocs=2, join=True, start_method="spawn")
+    import ast
+
+    got, costs = ast.literal_eval(open(out).read())
+    (m0, d0), (m1, d1) = got
+    assert d0 == d1
+    assert sorted(m0 + m1) == list(range(24)) and not set(m0) & set(m1)
+    l0, l1 = sum(costs[k] for k in m0), sum(costs[k] for k in m1)
+    assert max(l0, l1) <= sum(costs) / 2 + max(costs)
