@@ -153,3 +153,20 @@ def test_native_operators_reproduce_gold_rk3(name, pdename, lev, deg):
                        lambda t: O.md_eval(opde, deg, opde.sources, idx, blocks, t))
         g = ta["%s_t%d" % (name, i)]
         assert np.linalg.norm(f - g) <= 1e-14 * np.linalg.norm(g), i
+
+
+def test_native_builder_scalar_coefficients_and_null_arguments():
+    import ctypes as C
+
+    from asgkron._lib import ASG_ERR_INVALID, lib
+
+    pts = [P.div_term(lambda x: 2.0, -1.0, "N", "D"), P.grad_term(lambda x: -0.5, 0.0, "D", "N")]
+    a = P.term_matrix(3, -2.0, 1.0, 3, pts)
+    b = N.term_matrix(3, -2.0, 1.0, 3, pts)
+    assert np.abs(a - b).max() <= 5e-13 * np.abs(a).max()
+    out = np.empty((8, 8))
+    ptr = out.ctypes.data_as(C.POINTER(C.c_double))
+    assert lib().asg_coeff_matrix_f64(2, 2, 0.0, 1.0, 1, None, ptr) == ASG_ERR_INVALID
+    assert lib().asg_fmwt_matrix_f64(2, 2, None) == ASG_ERR_INVALID
+    assert lib().asg_gauss_legendre_f64(4, 0.0, 1.0, None, ptr) == ASG_ERR_INVALID
+    assert lib().asg_multiwavelet_filters_f64(2, ptr, None) == ASG_ERR_INVALID
