@@ -10,10 +10,12 @@
   threshold, its daughters (get_child_elements.m, methods 1 and 2) that are not in the
   table yet are appended, in discovery order, with coefficient value 1e-15.
 
-``rebuild_plan`` then builds the plan for the new table with the same 1-D operators (built
-at the maximum level, so every new 1-D index has its rows; adapt.m:417-437 rebuilds the
-coefficient matrices only when they were not).  Plan creation is the whole cost of an
-adaptation step on the device side: structure analysis, work list, uploads.
+``rebuild_plan`` then builds the plan for the new table.  Its operators are the plan's own
+(single partial terms are level-independent, so operators built at the maximum level serve
+every table) or, for chained partial terms, the ones ``PDE.rechain_term_mats`` forms at the
+new table's levels, as adapt.m:417-437 does through get_coeff_mats_rechain.m.  Plan creation
+is the whole cost of an adaptation step on the device side: structure analysis, work list,
+uploads.
 """
 import numpy as np
 
@@ -107,9 +109,17 @@ def adapt(table, fval, deg, max_lev, rel_threshold, coarsen=True, refine=True, m
     return AdaptResult(new, f.reshape(-1), removed, len(added_lev))
 
 
-def rebuild_plan(plan, table, pairs=None, **kw):
-    """A plan for the adapted table with the operators and work model of ``plan``."""
+def table_levels(table):
+    """Highest level present in each dimension (adapt.m:417-421)."""
+    lv = np.asarray(table.levels)
+    return [int(v) for v in lv.max(axis=0)] if lv.size else []
+
+
+def rebuild_plan(plan, table, pairs=None, term_mats=None, **kw):
+    """A plan for the adapted table with the work model of ``plan`` and its operators, or
+    ``term_mats`` (e.g. ``pde.rechain_term_mats(deg, table_levels(table))``)."""
     from .api import Plan
 
     structure = kw.pop("structure", plan.structure)
-    return Plan.create(plan.term_mats, table.idx1d(), plan.deg, pairs=pairs, structure=structure, **kw)
+    mats = plan.term_mats if term_mats is None else term_mats
+    return Plan.create(mats, table.idx1d(), plan.deg, pairs=pairs, structure=structure, **kw)

@@ -64,6 +64,31 @@ class PDE:
             out.append(row)
         return out
 
+    def rechain_term_mats(self, deg, levels, max_lev=8, cache=None):
+        """pde.terms{t}.terms_1D{d}.mat after adaptation (get_coeff_mats_rechain.m:7-60, with
+        max_lev_coeffs): every partial term is built once at max_lev (M \\ L, the native
+        builder), truncated to its leading deg 2^levels[d] rows and columns, and the truncated
+        factors are multiplied in order.  For single partial terms this equals building at
+        levels[d]; for chained (LDG) terms it is what the reference applies after an
+        adaptation step.  ``cache`` (a dict) keeps the max-level partial terms between calls."""
+        cache = {} if cache is None else cache
+        out = []
+        for ti, term in enumerate(self.terms):
+            row = []
+            for d, pts in enumerate(term):
+                lo, hi = self.bounds[d]
+                n = deg * 2 ** int(levels[d])
+                m = None
+                for q, pt in enumerate(pts):
+                    key = (ti, d, q, deg, max_lev)
+                    if key not in cache:
+                        cache[key] = _coeff.term_matrix(deg, lo, hi, max_lev, [pt])
+                    f = cache[key][:n, :n]
+                    m = f.copy() if m is None else m @ f
+                row.append(m)
+            out.append(row)
+        return out
+
     def _md(self, deg, funcs, idx1d, t):
         out = np.zeros(idx1d.shape[0] * deg ** self.num_dims)
         for fs in funcs:

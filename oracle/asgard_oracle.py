@@ -296,11 +296,11 @@ def coeff_matrix(deg, dim, pterm, coeff_level, t=0.0):
                 blk[2] = pRt * FCR @ p_R
                 blk[3] = Z
             colblk = [c - deg, c, c, c + deg]
-            use = [0, 1, 2, 3]
-            if i == 0:
-                use = [1, 2, 3]
-            elif i == N - 1:
-                use = [0, 1, 2]
+            # coeff_matrix.m:271-283 drops the left neighbour at i == 0 and the right one at
+            # i == N - 1; on a single cell both go (the reference's sparse(..., dof_1D, dof_1D)
+            # would reject the right one, and with max_lev_coeffs it truncates max-level
+            # matrices instead, which equals this single-cell build)
+            use = [b for b in (0, 1, 2, 3) if not (b == 0 and i == 0) and not (b == 3 and i == N - 1)]
             if pterm.IBCL == "P" or pterm.IBCR == "P":
                 if lev >= 1:
                     if i == 0:

@@ -14,7 +14,8 @@ once, in the container that has the reference checked out, and packs the subset 
 * ``permutations.npz``    -- ``gold/generated-inputs/permutations/*`` (``gold/gold_permute.m``)
 * ``quadrature.npz``      -- ``gold/generated-inputs/quadrature/*`` (``gold/gold_quadrature.m``)
 * ``transformations.npz`` -- ``operator_two_scale_*.dat``, ``multiwavelet_*.dat``, ``combine_dim_*.dat``
-* ``time_advance.npz``    -- RK3 and backward-Euler trajectories ``continuity{1,2,3,6}_*``, ``diffusion2_*`` ``_t{0..4}.dat``
+* ``time_advance.npz``    -- RK3 and backward-Euler trajectories ``continuity{1,2,3,6}_*``, ``diffusion2_*``
+                             and the adaptive ``continuity2_ad_*``, ``diffusion2_ad_implicit_*`` ``_t{0..4}.dat``
                              (``gold/gold_time_advance.m:252-364``)
 
 Run:  python tests/golden/make_golden.py [reference_root]
@@ -104,7 +105,9 @@ def main(ref_root):
                  # LDG diffusion with inhomogeneous Dirichlet data (gold_time_advance.m:40-51, 179-193, 203-234)
                  "diffusion2_sg_l2_d2", "diffusion2_sg_l3_d3", "diffusion2_sg_l4_d4", "diffusion2_sg_l4_5_d2",
                  "diffusion2_implicit_sg_l3_d3", "diffusion2_implicit_sg_l4_d3", "diffusion2_implicit_sg_l5_d3",
-                 "diffusion2_implicit_sg_l4_5_d2"):
+                 "diffusion2_implicit_sg_l4_5_d2",
+                 # adaptive runs (gold/gold_time_advance.m:21-34, 291-362)
+                 "continuity2_ad_sg_l3_d4", "diffusion2_ad_implicit_sg_l3_d4"):
         for t in range(5):
             path = os.path.join(gold, "time_advance", "%s_t%d.dat" % (stem, t))
             out["%s_t%d" % (stem, t)] = read_octave_text(path).reshape(-1)
