@@ -97,7 +97,7 @@ def main(ref_root):
     out = {}
     for stem in ("continuity1_sg_l2_d2", "continuity1_sg_l4_d3", "continuity1_fg_l2_d2",
                  "continuity2_sg_l2_d2", "continuity2_sg_l4_d3", "continuity2_fg_l2_d2",
-                 "continuity3_sg_l2_d2", "continuity3_sg_l4_d3",
+                 "continuity2_fg_l3_4_d3", "continuity3_sg_l2_d2", "continuity3_sg_l4_d3", "continuity3_sg_l3_4_2_d4",
                  "continuity6_sg_l2_d2", "continuity6_sg_l2_d3", "continuity6_sg_l2_3_2_3_3_2_d2",
                  # backward Euler (gold/gold_time_advance.m:156-173, 237-240)
                  "continuity1_implicit_l2_d2", "continuity1_implicit_l4_d3", "continuity2_implicit_l2_d2",

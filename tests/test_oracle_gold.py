@@ -202,6 +202,8 @@ def _replay(name, pdefn, lev, deg, grid="SG"):
     ("continuity2_fg_l2_d2", O.continuity2, 2, 2, "FG"),
     ("continuity3_sg_l2_d2", O.continuity3, 2, 2, "SG"),
     ("continuity3_sg_l4_d3", O.continuity3, 4, 3, "SG"),
+    ("continuity2_fg_l3_4_d3", O.continuity2, [3, 4], 3, "FG"),
+    ("continuity3_sg_l3_4_2_d4", O.continuity3, [3, 4, 2], 4, "SG"),
     ("continuity6_sg_l2_d2", O.continuity6, 2, 2, "SG"),
     ("continuity6_sg_l2_d3", O.continuity6, 2, 3, "SG"),
     ("continuity6_sg_l2_3_2_3_3_2_d2", O.continuity6, [2, 3, 2, 3, 3, 2], 2, "SG"),
