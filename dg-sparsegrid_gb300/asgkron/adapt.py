@@ -5,7 +5,10 @@
 * thresholds (adapt.m:15-18): refine where max|f_e| >= max|f| * rel, coarsen where
   max|f_e| <= 0.1 * that (and nothing happens when max|f| is zero);
 * coarsening (adapt.m:92-200): every element below the coarsening threshold is removed
-  with its coefficients; the others keep their order;
+  with its coefficients; the others keep their order.  adapt.m:108-110 admits every level
+  ("level must be >= 0 at present"); an earlier version, the one that wrote
+  gold/generated-inputs/adapt, coarsened only elements whose levels are all >= 1
+  (``min_coarsen_level=1``);
 * refinement (adapt.m:252-340): for each remaining element at or above the refinement
   threshold, its daughters (get_child_elements.m, methods 1 and 2) that are not in the
   table yet are appended, in discovery order, with coefficient value 1e-15.
@@ -73,8 +76,9 @@ class AdaptResult:
         self.added = added        # number of appended elements
 
 
-def adapt(table, fval, deg, max_lev, rel_threshold, coarsen=True, refine=True, method=1):
-    """One adaptation step of adapt.m on an element table and its coefficient vector."""
+def adapt(table, fval, deg, max_lev, rel_threshold, coarsen=True, refine=True, method=1, min_coarsen_level=0):
+    """One adaptation step of adapt.m on an element table and its coefficient vector.
+    Elements with a level below ``min_coarsen_level`` in some dimension are never removed."""
     levels = np.asarray(table.levels, dtype=np.int32)
     cells = np.asarray(table.cells, dtype=np.int32)
     N, d = levels.shape
@@ -87,7 +91,8 @@ def adapt(table, fval, deg, max_lev, rel_threshold, coarsen=True, refine=True, m
     if refine_thr <= 0:
         coarsen = refine = False
     emax = np.abs(f).max(axis=1) if N else np.zeros(0)
-    removed = np.nonzero(emax <= coarsen_thr)[0] if coarsen else np.zeros(0, dtype=np.int64)
+    removable = (emax <= coarsen_thr) & (levels.min(axis=1, initial=max_lev) >= min_coarsen_level)
+    removed = np.nonzero(removable)[0] if coarsen else np.zeros(0, dtype=np.int64)
     keep = np.ones(N, dtype=bool)
     keep[removed] = False
     levels, cells, f, emax = levels[keep], cells[keep], f[keep], emax[keep]

@@ -14,6 +14,7 @@ once, in the container that has the reference checked out, and packs the subset 
 * ``permutations.npz``    -- ``gold/generated-inputs/permutations/*`` (``gold/gold_permute.m``)
 * ``quadrature.npz``      -- ``gold/generated-inputs/quadrature/*`` (``gold/gold_quadrature.m``)
 * ``transformations.npz`` -- ``operator_two_scale_*.dat``, ``multiwavelet_*.dat``, ``combine_dim_*.dat``
+* ``adapt.npz``           -- ``gold/generated-inputs/adapt/continuity{1,2,3}_*`` (``gold/gold_adapt.m``)
 * ``time_advance.npz``    -- RK3 and backward-Euler trajectories ``continuity{1,2,3,6}_*``, ``diffusion2_*``
                              and the adaptive ``continuity2_ad_*``, ``diffusion2_ad_implicit_*`` ``_t{0..4}.dat``
                              (``gold/gold_time_advance.m:252-364``)
@@ -93,6 +94,13 @@ def main(ref_root):
         for path in sorted(glob.glob(os.path.join(gold, "transformations", pat))):
             out[os.path.basename(path)[:-4]] = read_octave_text(path)
     np.savez_compressed(os.path.join(HERE, "transformations.npz"), **out)
+    n += len(out)
+    out = {}
+    # adaptation of given vectors (gold/gold_adapt.m:1-14, 60-112): original, coarsened and
+    # refined vectors, and the tables as [levels, cells] rows
+    for path in sorted(glob.glob(os.path.join(gold, "adapt", "continuity*_l*_d*_*.dat"))):
+        out[os.path.basename(path)[:-4]] = read_octave_text(path)
+    np.savez_compressed(os.path.join(HERE, "adapt.npz"), **out)
     n += len(out)
     out = {}
     for stem in ("continuity1_sg_l2_d2", "continuity1_sg_l4_d3", "continuity1_fg_l2_d2",

@@ -1,4 +1,6 @@
-"""Adaptivity pinned to the reference's adaptive gold trajectories.
+"""Adaptivity pinned to the reference's adaptation gold (gold/generated-inputs/adapt: one
+coarsening and one refinement of given vectors, bit-exact) and its adaptive gold
+trajectories.
 
 The product's host pieces under test: the element rules of ``asgkron.adapt.adapt``
 (adapt.m), its element tables (hash_table_sparse_nD order) and the rechained operators of
@@ -136,3 +138,32 @@ def test_rechained_operators_match_truncated_oracle_chain(levels):
                 want = want @ O.pterm_matrix(deg, dim, pt, 6)[:n, :n]
             assert got[ti][d].shape == (n, n)
             assert np.abs(got[ti][d] - want).max() <= 1e-11 * max(1.0, np.abs(want).max()), (ti, d)
+
+
+@pytest.mark.parametrize("stem,lev,deg,d", [("continuity1_l4_d3", 4, 3, 1), ("continuity2_l5_d2", 5, 2, 2),
+                                            ("continuity3_l4_d4", 4, 4, 3)])
+def test_adapt_matches_reference_adapt_gold(stem, lev, deg, d):
+    """gold/gold_adapt.m: one coarsening and one refinement (threshold 1e-4, method 1,
+    max_lev 8) of a given vector on the SG table; the tables ([levels, cells] rows in
+    element order) and vectors are bit-exact.  That generator's adapt.m coarsened only
+    elements whose levels are all >= 1 (min_coarsen_level=1); with the current rule every
+    level-0 element below the threshold also goes."""
+    import asgkron
+    from asgkron.adapt import adapt
+
+    z = np.load(os.path.join(G, "adapt.npz"))
+    table = asgkron.hash_table_sparse_nD([lev] * d, 8)
+    orig = z[stem + "_orig"].reshape(-1)
+    for kind, co, rf in (("coarse", True, False), ("refine", False, True)):
+        r = adapt(table, orig, deg, 8, 1e-4, coarsen=co, refine=rf, min_coarsen_level=1)
+        got = np.hstack([np.asarray(r.table.levels), np.asarray(r.table.cells)]).astype(np.int64)
+        want = z["%s_%s_table" % (stem, kind)].reshape(-1, 2 * d).astype(np.int64)
+        assert np.array_equal(got, want), kind
+        assert np.array_equal(r.fval, z["%s_%s" % (stem, kind)].reshape(-1)), kind
+    # the current rule removes the level-0 elements below the threshold as well
+    r = adapt(table, orig, deg, 8, 1e-4, coarsen=True, refine=False)
+    lv = np.asarray(table.levels)
+    f = orig.reshape(lv.shape[0], -1)
+    keep = np.abs(f).max(axis=1) > 0.1 * 1e-4 * np.abs(orig).max()
+    assert r.table.num_elems == int(keep.sum())
+    assert np.array_equal(r.fval, f[keep].ravel())
