@@ -14,6 +14,8 @@ once, in the container that has the reference checked out, and packs the subset 
 * ``permutations.npz``    -- ``gold/generated-inputs/permutations/*`` (``gold/gold_permute.m``)
 * ``quadrature.npz``      -- ``gold/generated-inputs/quadrature/*`` (``gold/gold_quadrature.m``)
 * ``transformations.npz`` -- ``operator_two_scale_*.dat``, ``multiwavelet_*.dat``, ``combine_dim_*.dat``
+* ``pde.npz``             -- ``gold/generated-inputs/pde/{continuity2,continuity_3,continuity_6,diffusion_2}_*``
+                             (``gold/gold_pde.m``)
 * ``adapt.npz``           -- ``gold/generated-inputs/adapt/continuity{1,2,3}_*`` (``gold/gold_adapt.m``)
 * ``time_advance.npz``    -- RK3 and backward-Euler trajectories ``continuity{1,2,3,6}_*``, ``diffusion2_*``
                              and the adaptive ``continuity2_ad_*``, ``diffusion2_ad_implicit_*`` ``_t{0..4}.dat``
@@ -94,6 +96,14 @@ def main(ref_root):
         for path in sorted(glob.glob(os.path.join(gold, "transformations", pat))):
             out[os.path.basename(path)[:-4]] = read_octave_text(path)
     np.savez_compressed(os.path.join(HERE, "transformations.npz"), **out)
+    n += len(out)
+    out = {}
+    # PDE specifications evaluated at x = 0.1..0.5, t = 5 (gold/gold_pde.m): initial
+    # conditions, exact solutions, sources and dt of the configurations' PDEs
+    for pat in ("continuity2_*.dat", "continuity_3_*.dat", "continuity_6_*.dat", "diffusion_2_*.dat"):
+        for path in sorted(glob.glob(os.path.join(gold, "pde", pat))):
+            out[os.path.basename(path)[:-4]] = read_octave_text(path)
+    np.savez_compressed(os.path.join(HERE, "pde.npz"), **out)
     n += len(out)
     out = {}
     # adaptation of given vectors (gold/gold_adapt.m:1-14, 60-112): original, coarsened and

@@ -72,3 +72,37 @@ def test_boundary_vector_matches_oracle(lev, deg):
         got = pde.boundary_vector(deg, idx, t)
         want = O.boundary_condition_vector(O.diffusion2(lev), deg, idx.astype(np.int64), blocks, t)
         assert np.linalg.norm(got - want) <= 1e-14 * np.linalg.norm(want)
+
+
+@pytest.mark.parametrize("stem,name,lev", [("continuity2", "continuity2", 5), ("continuity_3", "continuity3", 5),
+                                           ("continuity_6", "continuity6", 3), ("diffusion_2", "diffusion2", 3)])
+def test_pde_specs_match_reference_pde_gold(stem, name, lev):
+    """gold/gold_pde.m evaluates each PDE's initial condition, sources (spatial parts at
+    x = 0.1..0.5, time factors at t = 5) and dt at CFL 1; the product's PDEs and the oracle's
+    agree to round-off.  Exact solutions are compared where the initial-condition functions
+    are the solution's (continuity2, diffusion2); continuity3/6 carry no solution."""
+    z = np.load(os.path.join(G, "pde.npz"))
+    x = np.array([0.1, 0.2, 0.3, 0.4, 0.5])
+    T = 5.0
+    prod = pdes.diffusion2(lev, case="reference") if name == "diffusion2" else getattr(pdes, name)(lev)
+    orac = getattr(O, name)(lev)
+    for spec, ic, sources, dt in ((prod, prod.ic, prod.sources, prod.dt(1.0)),
+                                  (orac, orac.ic, orac.sources, orac.dt_fn(orac, 1.0))):
+        def same(key, got):
+            want = z["%s_%s" % (stem, key)].reshape(-1)
+            got = np.asarray(got, dtype=np.float64).reshape(-1) * np.ones_like(want)
+            assert np.abs(got - want).max() <= 1e-14 * max(1.0, np.abs(want).max()), key
+
+        D = len(ic[0]) - 1
+        for d in range(D):
+            same("initial_dim%d" % d, ic[0][d](x, 0.0))
+            if name in ("continuity2", "diffusion2"):
+                same("exact_dim%d" % d, ic[0][d](x, T))
+        if name in ("continuity2", "diffusion2"):
+            same("exact_time", ic[0][-1](T))
+        assert len(sources) == sum(1 for k in z.files if k.startswith(stem + "_source") and k.endswith("_time"))
+        for s, src in enumerate(sources):
+            for d in range(D):
+                same("source%d_dim%d" % (s, d), src[d](x, T))
+            same("source%d_time" % s, src[-1](T))
+        same("dt", dt)
