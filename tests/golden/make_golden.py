@@ -14,6 +14,7 @@ once, in the container that has the reference checked out, and packs the subset 
 * ``permutations.npz``    -- ``gold/generated-inputs/permutations/*`` (``gold/gold_permute.m``)
 * ``quadrature.npz``      -- ``gold/generated-inputs/quadrature/*`` (``gold/gold_quadrature.m``)
 * ``transformations.npz`` -- ``operator_two_scale_*.dat``, ``multiwavelet_*.dat``, ``combine_dim_*.dat``
+* ``basis.npz``           -- ``gold/generated-inputs/basis/transform_blocks_*`` (``gold/gold_basis.m``)
 * ``pde.npz``             -- ``gold/generated-inputs/pde/{continuity2,continuity_3,continuity_6,diffusion_2}_*``
                              (``gold/gold_pde.m``)
 * ``adapt.npz``           -- ``gold/generated-inputs/adapt/continuity{1,2,3}_*`` (``gold/gold_adapt.m``)
@@ -96,6 +97,13 @@ def main(ref_root):
         for path in sorted(glob.glob(os.path.join(gold, "transformations", pat))):
             out[os.path.basename(path)[:-4]] = read_octave_text(path)
     np.savez_compressed(os.path.join(HERE, "transformations.npz"), **out)
+    n += len(out)
+    out = {}
+    # the transform's blocks (gold/gold_basis.m: OperatorTwoScale_wavelet2 at levels 2, 5
+    # and degrees 2, 5)
+    for path in sorted(glob.glob(os.path.join(gold, "basis", "transform_blocks_*.dat"))):
+        out[os.path.basename(path)[:-4]] = read_octave_text(path)
+    np.savez_compressed(os.path.join(HERE, "basis.npz"), **out)
     n += len(out)
     out = {}
     # PDE specifications evaluated at x = 0.1..0.5, t = 5 (gold/gold_pde.m): initial

@@ -19,6 +19,18 @@ def _npz(name):
 
 
 # ---------------------------------------------------------------- quadrature / basis
+@pytest.mark.parametrize("lev,deg", [(2, 2), (2, 5), (5, 2), (5, 5)])
+def test_transform_blocks_gold(lev, deg):
+    """OperatorTwoScale_wavelet2.m's blocks (the per-level pieces md_eval transforms with)
+    against gold/generated-inputs/basis/transform_blocks_l<lev>_d<deg>_<b>."""
+    z = _npz("basis.npz")
+    _, blocks = O.operator_two_scale(deg, lev)
+    assert len(blocks) == 2 * lev
+    for b, blk in enumerate(blocks):
+        want = z["transform_blocks_l%d_d%d_%d" % (lev, deg, b + 1)].reshape(blk.shape)
+        np.testing.assert_allclose(blk, want, rtol=0, atol=1e-15)
+
+
 def test_lgwt_gold():
     q = _npz("quadrature.npz")
     for (n, a, b, tag) in ((10, -1, 1, "10_neg1_1"), (32, -5, 2, "32_neg5_2")):
