@@ -13,7 +13,8 @@
   threshold, its daughters (get_child_elements.m, methods 1 and 2) that are not in the
   table yet are appended, in discovery order, with coefficient value 1e-15.
 
-``rebuild_plan`` then builds the plan for the new table.  Its operators are the plan's own
+``AdaptiveRun`` drives the reference's adaptive time loop around a caller's time step.
+``rebuild_plan`` builds the plan for a new table.  Its operators are the plan's own
 (single partial terms are level-independent, so operators built at the maximum level serve
 every table) or, for chained partial terms, the ones ``PDE.rechain_term_mats`` forms at the
 new table's levels, as adapt.m:417-437 does through get_coeff_mats_rechain.m.  Plan creation
@@ -128,3 +129,63 @@ def rebuild_plan(plan, table, pairs=None, term_mats=None, **kw):
     structure = kw.pop("structure", plan.structure)
     mats = plan.term_mats if term_mats is None else term_mats
     return Plan.create(mats, table.idx1d(), plan.deg, pairs=pairs, structure=structure, **kw)
+
+
+class AdaptiveRun:
+    """The reference's adaptive time loop on the host (gold/gold_time_advance.m:291-362,
+    adapt.m): the element table, the PDE's levels and the coefficient vector evolve here;
+    the time step is the caller's ``step(run, f, t) -> f`` on ``run.table`` with
+    ``run.term_mats()`` (a GPU stepper on a plan rebuilt by ``rebuild_plan``, or any other).
+
+    The PDE object is updated in place: its levels follow the table (adapt.m:417-425), so
+    its projections (initial condition, sources, boundary data) cover every element."""
+
+    def __init__(self, pde, deg, table, threshold, max_lev=8, method=1, min_coarsen_level=0):
+        self.pde, self.deg, self.threshold, self.max_lev = pde, deg, threshold, max_lev
+        self.method, self.min_coarsen_level = method, min_coarsen_level
+        self._pterms = {}
+        self.set_table(table)
+
+    def set_table(self, table):
+        self.table = table
+        self.levels = table_levels(table)
+        self.pde.levels = list(self.levels)
+        self.idx1d = table.idx1d()
+
+    def term_mats(self):
+        """The operators for the current table: partial terms rechained at its levels."""
+        return self.pde.rechain_term_mats(self.deg, self.levels, self.max_lev, self._pterms)
+
+    def adapt(self, f, coarsen, refine):
+        r = adapt(self.table, f, self.deg, self.max_lev, self.threshold, coarsen=coarsen, refine=refine,
+                  method=self.method, min_coarsen_level=self.min_coarsen_level)
+        self.set_table(r.table)
+        return r
+
+    def initial(self, t=0.0):
+        """The initial condition on an adapted table: refine and re-project until the table
+        stops growing, then coarsen and re-project (gold_time_advance.m:291-313)."""
+        f = self.pde.initial_condition(self.deg, self.idx1d, t)
+        while True:
+            n0 = f.size
+            r = self.adapt(f, coarsen=False, refine=True)
+            f = self.pde.initial_condition(self.deg, self.idx1d, t)
+            if r.fval.size == n0:
+                break
+        self.adapt(f, coarsen=True, refine=False)
+        return self.pde.initial_condition(self.deg, self.idx1d, t)
+
+    def advance(self, f, t, step):
+        """One step with adaptation (gold_time_advance.m:318-360): coarsen, advance, refine
+        from the advanced values; while elements were added, advance again from the
+        unstepped values extended to the refined table (new elements at 1e-15)."""
+        f = self.adapt(f, coarsen=True, refine=False).fval
+        block = self.deg ** len(self.levels)
+        while True:
+            f_un = np.asarray(f, dtype=np.float64).reshape(-1)
+            f = step(self, f_un, t)
+            r = self.adapt(f, coarsen=False, refine=True)
+            f_un = np.concatenate([f_un, np.full(r.added * block, NEW_ELEMENT_VALUE)])
+            if r.added == 0:
+                return step(self, f_un, t)
+            f = f_un

@@ -2,10 +2,11 @@
 coarsening and one refinement of given vectors, bit-exact) and its adaptive gold
 trajectories.
 
-The product's host pieces under test: the element rules of ``asgkron.adapt.adapt``
-(adapt.m), its element tables (hash_table_sparse_nD order) and the rechained operators of
-``PDE.rechain_term_mats`` (get_coeff_mats_rechain.m).  The oracle steps and projects (the
-checker), on each adapted table.
+The product's host pieces under test: ``asgkron.adapt.AdaptiveRun`` (the driver's adaptive
+loop), the element rules of ``adapt`` (adapt.m), the element tables (hash_table_sparse_nD
+order), the initial-condition projections on adapted tables and the rechained operators of
+``PDE.rechain_term_mats`` (get_coeff_mats_rechain.m).  The oracle takes the time steps (the
+checker) on each adapted table.
 
 * continuity2_ad_sg_l3_d4 follows gold/gold_time_advance.m:21-24, 291-362 exactly: the
   initial condition refined until the table stops growing and re-projected, then coarsened
@@ -25,96 +26,63 @@ import pytest
 from oracle import asgard_oracle as O
 
 G = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-NEW_ELEMENT_VALUE = 1e-15
 
 
-class Replay:
-    def __init__(self, name, lev, deg, thr, method, max_lev=8):
-        import asgkron
-        from asgkron import pdes
+def _run(name, lev, deg, thr):
+    """The product's AdaptiveRun on the PDE (product spec) and its starting SG table."""
+    import asgkron
+    from asgkron import pdes
+    from asgkron.adapt import AdaptiveRun
 
-        self.opde = O.continuity2(lev, LF=0.0) if name == "continuity2" else O.diffusion2(lev)
-        self.ppde = pdes.continuity2(lev, 0.0) if name == "continuity2" else pdes.diffusion2(lev, case="reference")
-        self.name, self.deg, self.thr, self.method, self.max_lev = name, deg, thr, method, max_lev
-        self.dt = self.opde.dt_fn(self.opde, 0.01)  # at the starting level, as the driver sets it
-        _, self.blocks = O.operator_two_scale(deg, max_lev)
-        self.cache = {}
-        self.set_table(asgkron.hash_table_sparse_nD([lev, lev], max_lev))
+    ppde = pdes.continuity2(lev, 0.0) if name == "continuity2" else pdes.diffusion2(lev, case="reference")
+    return AdaptiveRun(ppde, deg, asgkron.hash_table_sparse_nD([lev, lev], 8), thr)
 
-    def set_table(self, table):
-        from asgkron.adapt import table_levels
 
-        self.table = table
-        self.levels = table_levels(table)
-        for dim, lv in zip(self.opde.dims, self.levels):  # adapt.m:417-425
+def _oracle_step(name, lev, deg, method):
+    """The checker's time step on the run's current table: the oracle's apply loop on the
+    run's rechained operators, sources / Dirichlet data projected at the run's levels."""
+    opde = O.continuity2(lev, LF=0.0) if name == "continuity2" else O.diffusion2(lev)
+    dt = opde.dt_fn(opde, 0.01)  # at the starting level, as the driver sets it
+    _, blocks = O.operator_two_scale(deg, 8)
+
+    def step(run, f, t):
+        for dim, lv in zip(opde.dims, run.levels):
             dim.lev = lv
-        self.idx = table.idx1d().astype(np.int64)
-
-    def adapt(self, f, coarsen, refine):
-        from asgkron.adapt import adapt
-
-        r = adapt(self.table, f, self.deg, self.max_lev, self.thr, coarsen=coarsen, refine=refine)
-        self.set_table(r.table)
-        return r
-
-    def ic(self):
-        return O.md_eval(self.opde, self.deg, self.opde.ic, self.idx, self.blocks, 0.0)
-
-    def step(self, f, t):
-        mats = self.ppde.rechain_term_mats(self.deg, self.levels, self.max_lev, self.cache)
-        idx, deg = self.idx, self.deg
-        if self.name == "diffusion2":
-            src = lambda tt: O.boundary_condition_vector(self.opde, deg, idx, self.blocks, tt)
+        idx = run.idx1d.astype(np.int64)
+        mats = run.term_mats()
+        if name == "diffusion2":
+            src = lambda tt: O.boundary_condition_vector(opde, deg, idx, blocks, tt)
         else:
-            src = lambda tt: O.md_eval(self.opde, deg, self.opde.sources, idx, self.blocks, tt)
-        if self.method == "BE":
+            src = lambda tt: O.md_eval(opde, deg, opde.sources, idx, blocks, tt)
+        if method == "BE":
             _, A = O.apply_A_loop(mats, idx, deg, f, build_A=True)
-            return O.backward_euler_step(A, f, self.dt, src(t + self.dt))
-        return O.rk3_step(lambda v: O.apply_A_rows(mats, idx, deg, v), f, t, self.dt, src)
+            return O.backward_euler_step(A, f, dt, src(t + dt))
+        return O.rk3_step(lambda v: O.apply_A_rows(mats, idx, deg, v), f, t, dt, src)
 
-    def initial(self):
-        f = self.ic()
-        while True:  # refine until the table stops growing, re-projecting each time
-            n0 = f.size
-            r = self.adapt(f, coarsen=False, refine=True)
-            f = self.ic()
-            if r.fval.size == n0:
-                break
-        self.adapt(f, coarsen=True, refine=False)
-        return self.ic()
-
-    def advance(self, f, t):
-        """One driver step with adaptation: coarsen, then advance and refine until stable."""
-        f = self.adapt(f, coarsen=True, refine=False).fval
-        while True:
-            f_un = f
-            f = self.step(f_un, t)
-            r = self.adapt(f, coarsen=False, refine=True)
-            f_un = np.concatenate([f_un, np.full(r.added * self.deg ** 2, NEW_ELEMENT_VALUE)])
-            if r.added == 0:
-                return self.step(f_un, t)
-            f = f_un
+    return step, dt
 
 
 def test_adaptive_continuity2_rk3_gold():
     ta = np.load(os.path.join(G, "time_advance.npz"))
-    rp = Replay("continuity2", 3, 4, 1e-3, "RK3")
-    f = rp.initial()
+    run = _run("continuity2", 3, 4, 1e-3)
+    step, dt = _oracle_step("continuity2", 3, 4, "RK3")
+    f = run.initial()
     for i in range(5):
-        f = rp.advance(f, i * rp.dt)
+        f = run.advance(f, i * dt, step)
         g = ta["continuity2_ad_sg_l3_d4_t%d" % i]
         assert f.size == g.size, (i, f.size, g.size)
         assert np.linalg.norm(f - g) <= 1e-14 * np.linalg.norm(g), i
-    assert rp.table.num_elems == 112
+    assert run.table.num_elems == 112 and run.pde.levels == run.levels
 
 
 def test_adaptive_diffusion2_backward_euler_gold():
     ta = np.load(os.path.join(G, "time_advance.npz"))
-    rp = Replay("diffusion2", 3, 4, 1e-4, "BE")
-    f = rp.initial()
-    assert rp.table.num_elems == 15
+    run = _run("diffusion2", 3, 4, 1e-4)
+    step, dt = _oracle_step("diffusion2", 3, 4, "BE")
+    f = run.initial()
+    assert run.table.num_elems == 15
     for i in range(5):
-        f = rp.step(f, i * rp.dt)
+        f = step(run, f, i * dt)
         g = ta["diffusion2_ad_implicit_sg_l3_d4_t%d" % i]
         assert f.size == g.size
         assert np.linalg.norm(f - g) <= 1e-12 * np.linalg.norm(g), i
