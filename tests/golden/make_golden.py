@@ -14,6 +14,8 @@ once, in the container that has the reference checked out, and packs the subset 
 * ``permutations.npz``    -- ``gold/generated-inputs/permutations/*`` (``gold/gold_permute.m``)
 * ``quadrature.npz``      -- ``gold/generated-inputs/quadrature/*`` (``gold/gold_quadrature.m``)
 * ``transformations.npz`` -- ``operator_two_scale_*.dat``, ``multiwavelet_*.dat``, ``combine_dim_*.dat``
+* ``coefficients.npz``    -- ``gold/generated-inputs/coefficients/{continuity2,3,6,diffusion2}_coefficients_l*``
+                             (one level set each; ``gold/gold_coefficients.m``)
 * ``basis.npz``           -- ``gold/generated-inputs/basis/transform_blocks_*`` (``gold/gold_basis.m``)
 * ``pde.npz``             -- ``gold/generated-inputs/pde/{continuity2,continuity_3,continuity_6,diffusion_2}_*``
                              (``gold/gold_pde.m``)
@@ -97,6 +99,15 @@ def main(ref_root):
         for path in sorted(glob.glob(os.path.join(gold, "transformations", pat))):
             out[os.path.basename(path)[:-4]] = read_octave_text(path)
     np.savez_compressed(os.path.join(HERE, "transformations.npz"), **out)
+    n += len(out)
+    out = {}
+    # wavelet-space 1-D operators pde.terms{t}.terms_1D{d}.mat (gold/gold_coefficients.m,
+    # central flux), one level set per configuration PDE
+    for stem in ("continuity2_coefficients_l4_4_d3", "continuity3_coefficients_l2_3_2_d4",
+                 "continuity6_coefficients_l2_2_2_2_2_2_d4", "diffusion2_coefficients_l2_3_d5"):
+        for path in sorted(glob.glob(os.path.join(gold, "coefficients", stem + "_*_*.dat"))):
+            out[os.path.basename(path)[:-4]] = read_octave_text(path)
+    np.savez_compressed(os.path.join(HERE, "coefficients.npz"), **out)
     n += len(out)
     out = {}
     # the transform's blocks (gold/gold_basis.m: OperatorTwoScale_wavelet2 at levels 2, 5

@@ -170,3 +170,27 @@ def test_native_builder_scalar_coefficients_and_null_arguments():
     assert lib().asg_fmwt_matrix_f64(2, 2, None) == ASG_ERR_INVALID
     assert lib().asg_gauss_legendre_f64(4, 0.0, 1.0, None, ptr) == ASG_ERR_INVALID
     assert lib().asg_multiwavelet_filters_f64(2, ptr, None) == ASG_ERR_INVALID
+
+
+@pytest.mark.parametrize("name,levels,deg", [("continuity2", [4, 4], 3), ("continuity3", [2, 3, 2], 4),
+                                             ("continuity6", [2] * 6, 4), ("diffusion2", [2, 3], 5)])
+@pytest.mark.parametrize("builder", ["native", "numpy", "rechain"])
+def test_operators_match_reference_coefficient_gold(name, levels, deg, builder):
+    """pde.terms{t}.terms_1D{d}.mat of every term and dimension against
+    gold/generated-inputs/coefficients (gold_coefficients.m: central flux, max_lev_coeffs, so
+    chained terms are rechained at each dimension's level).  Tolerance: the transform's
+    orthogonality round-off, which grows with the degree (2.3e-13 at deg 5)."""
+    z = np.load(os.path.join(G, "coefficients.npz"))
+    pde = pdes.diffusion2(levels, case="reference") if name == "diffusion2" else getattr(pdes, name)(levels, 0.0)
+    if builder == "rechain":
+        mats = pde.rechain_term_mats(deg, levels, max_lev=8)
+    else:
+        mats = pde.term_mats(deg, builder=builder)
+    tol = 5e-13 if deg >= 5 else 1e-13
+    stem = "%s_coefficients_l%s_d%d" % (name, "_".join("%d" % v for v in levels), deg)
+    for t in range(len(pde.terms)):
+        for d in range(len(levels)):
+            want = z["%s_%d_%d" % (stem, t + 1, d + 1)]
+            got = mats[t][d]
+            assert got.shape == want.shape, (t, d)
+            assert np.abs(got - want).max() <= tol * np.abs(want).max(), (t, d)
