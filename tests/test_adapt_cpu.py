@@ -56,6 +56,7 @@ def test_adapt_coarsen_and_refine_rules():
 
 
 @pytest.mark.gpu
+@pytest.mark.gpu
 def test_rebuilt_plan_matches_oracle_after_adapt():
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
