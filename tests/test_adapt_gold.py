@@ -135,3 +135,29 @@ def test_adapt_matches_reference_adapt_gold(stem, lev, deg, d):
     keep = np.abs(f).max(axis=1) > 0.1 * 1e-4 * np.abs(orig).max()
     assert r.table.num_elems == int(keep.sum())
     assert np.array_equal(r.fval, f[keep].ravel())
+
+
+def test_adaptive_run_edge_cases():
+    """A zero vector leaves the table alone (adapt.m's refine_threshold <= 0 guard); a step
+    that adds nothing is taken once more from the unstepped values on the same table; the
+    PDE's levels follow the table."""
+    import asgkron
+    from asgkron import pdes
+    from asgkron.adapt import AdaptiveRun
+
+    pde = pdes.continuity2(2, 0.0)
+    table = asgkron.hash_table_sparse_nD([2, 2], 8)
+    run = AdaptiveRun(pde, 2, table, 1e-3)
+    n0 = run.table.num_elems
+    calls = []
+
+    def step(r, f, t):
+        calls.append((r.table.num_elems, f.size, t))
+        return np.zeros_like(f)
+
+    f = run.advance(np.zeros(n0 * 4), 0.5, step)
+    assert run.table.num_elems == n0 and f.size == n0 * 4
+    assert calls == [(n0, n0 * 4, 0.5), (n0, n0 * 4, 0.5)]
+    assert pde.levels == run.levels == [2, 2]
+    mats = run.term_mats()
+    assert [m.shape for m in mats[0]] == [(8, 8), (8, 8)]
