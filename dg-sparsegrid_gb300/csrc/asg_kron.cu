@@ -216,6 +216,7 @@ struct asg_kron_plan {
   long long work_elems = 0;
   std::vector<asg::KDev> dev;                 // device-order descriptors (uploaded on first use)
   asg::KDev* d_desc = nullptr;
+  std::mutex upload_mu;                       // serialises the first-use upload across host threads
 };
 
 using asg::fail;
@@ -227,9 +228,18 @@ asg_status kron_exec(const asg_kron_plan* cp, const T* const* A, const T* X, T* 
                      void* stream) {
   if (!cp || !A || !X || !Y) return fail(ASG_ERR_INVALID, "kron_batch: NULL argument");
   asg_kron_plan* p = const_cast<asg_kron_plan*>(cp);
-  if (!p->d_desc && !p->dev.empty()) {  // first execution uploads the descriptor table
-    ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_desc), p->dev.size() * sizeof(asg::KDev)));
-    ASG_CUDA(cudaMemcpy(p->d_desc, p->dev.data(), p->dev.size() * sizeof(asg::KDev), cudaMemcpyHostToDevice));
+  if (!p->dev.empty()) {  // the first execution uploads the descriptor table, once per plan
+    std::lock_guard<std::mutex> lock(p->upload_mu);
+    if (!p->d_desc) {
+      asg::KDev* d = nullptr;
+      ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&d), p->dev.size() * sizeof(asg::KDev)));
+      cudaError_t e = cudaMemcpy(d, p->dev.data(), p->dev.size() * sizeof(asg::KDev), cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) {
+        cudaFree(d);
+        return asg::cuda_fail(e, "kron_batch: descriptor upload");
+      }
+      p->d_desc = d;  // published only once the table is complete
+    }
   }
   if (work_bytes < static_cast<size_t>(p->work_elems) * sizeof(T))
     return fail(ASG_ERR_CAPACITY, "kron_batch: workspace needs %lld bytes", p->work_elems * (long long)sizeof(T));
@@ -474,22 +484,24 @@ __global__ void k_kron_level_static(const KChunk chunk, KBases<double> b) {
   }
 }
 
-std::once_flag g_scratch_once[kStaticMaxDevices];
+std::mutex g_scratch_mu;
 double* g_scratch_ptr[kStaticMaxDevices];
-cudaError_t g_scratch_err[kStaticMaxDevices];
 
-// The array's device address for the current device, looked up once per device.
+// The array's device address for the current device.  Only a successful lookup is cached: a
+// failed one (for instance one attempted during a stream capture) is retried on the next call.
 asg_status static_scratch(double** out) {
   int dev = 0;
   ASG_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kStaticMaxDevices)
     return fail(ASG_ERR_UNSUPPORTED, "kron_batch_static: device %d beyond the %d supported", dev, kStaticMaxDevices);
-  std::call_once(g_scratch_once[dev], [dev] {
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_ptr[dev]) {
     void* ptr = nullptr;
-    g_scratch_err[dev] = cudaGetSymbolAddress(&ptr, g_kron_scratch);
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_kron_scratch);
+    if (e != cudaSuccess || !ptr)
+      return cuda_fail(e != cudaSuccess ? e : cudaErrorInvalidSymbol, "cudaGetSymbolAddress(kron scratch)");
     g_scratch_ptr[dev] = static_cast<double*>(ptr);
-  });
-  if (g_scratch_err[dev] != cudaSuccess) return cuda_fail(g_scratch_err[dev], "cudaGetSymbolAddress(kron scratch)");
+  }
   *out = g_scratch_ptr[dev];
   return ASG_OK;
 }
@@ -526,8 +538,11 @@ extern "C" asg_status asg_kron_batch_static_f64(const asg_kron_plan* p, const do
       const int cnt = std::min(asg::kStaticChunk, p->level_start[l + 1] - q);
       std::memcpy(chunk.d, p->dev.data() + q, cnt * sizeof(asg::KDev));
       chunk.count = cnt;
-      asg::k_kron_level_static<<<cnt, 128, 0, s>>>(chunk, b);
-      cudaError_t e = cudaGetLastError();
+      // the launch's own return code: an earlier, unrelated error left in the runtime's
+      // last-error slot is neither reported nor cleared here
+      void* args[] = {&chunk, &b};
+      const cudaError_t e = cudaLaunchKernel(reinterpret_cast<const void*>(&asg::k_kron_level_static), dim3(cnt),
+                                             dim3(128), args, 0, s);
       if (e != cudaSuccess) return asg::cuda_fail(e, "kron_batch_static launch");
     }
   }

@@ -24,7 +24,8 @@ once, in the container that has the reference checked out, and packs the subset 
                              and the adaptive ``continuity2_ad_*``, ``diffusion2_ad_implicit_*`` ``_t{0..4}.dat``
                              (``gold/gold_time_advance.m:252-364``)
 
-Run:  python tests/golden/make_golden.py [reference_root]
+Run:  python tests/golden/make_golden.py <reference_root>
+      (or set ASG_REFERENCE_ROOT; the path of the DG-SparseGrid checkout is required)
 """
 import glob
 import os
@@ -154,4 +155,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("ASG_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: make_golden.py <reference_root>  (or set ASG_REFERENCE_ROOT)")
+    main(root)
