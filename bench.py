@@ -33,6 +33,13 @@ for _p in (ROOT, os.path.join(ROOT, "dg-sparsegrid_gb300")):
 METRIC = "apply_A GDOF/s & % roofline: FP32 vs FP64 on-GPU at <=1e-6 rel err"
 UNIT = "GDOF/s"
 WORKLOAD = "continuity6 SG lev4 deg4 (501 elements x 4096 DOF, 6 terms, all pairs)"
+DATA = "synthetic (continuity6 operators from the DG builder; f ~ N(0,1) seed 4)"
+L2_NOTE = "inputs (8.2 MB) below L2: L2 flushed (512 MB device write) before every timed GPU step"
+
+
+def workload_config(dof):
+    """The ``config`` both arms print (identical: the workload, not the implementation)."""
+    return {"workload": WORKLOAD, "dof": dof, "l2": L2_NOTE}
 FALLBACK_HBM_GBS = 6800.0
 
 
@@ -42,7 +49,8 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-rows", type=int, default=48, help="rows in the bounded CPU sample")
+    ap.add_argument("--ref-budget", type=float, default=150.0,
+                    help="reference arm: seconds of host work for warmup + steps (sets the rows per step)")
     ap.add_argument("--skip-variants", action="store_true")
     ap.add_argument("--workload", default="continuity6", choices=["continuity6", "batched", "implicit"],
                     help="batched: the 256-problem persistent-launch configuration; implicit: the "
@@ -137,82 +145,92 @@ class ClockSampler:
                 "reasons": reasons + note, "samples": len(sel)}
 
 
-def cpu_baseline(mats, idx, deg, f64, rows):
+def oracle_workload():
+    """The continuity6 workload (SG level 4, degree 4) built by the oracle alone: element table,
+    1-D indices and operators from the CPU restatement, no product code loaded."""
+    from oracle import asgard_oracle as O
+
+    pde = O.continuity6(4)
+    mats = O.build_term_mats(pde, 4)
+    levels, cells, _ = O.hash_table_sparse_nd([4] * 6, 4)
+    return mats, O.element_idx1d(levels, cells), 4
+
+
+def time_reference_rows(mats, idx, deg, f64, rows, cores):
+    """Seconds for the reference loop (oracle/apply_a_ref.c: every one of the N columns x 6
+    terms x the 6-mode chain) over the given whole rows, on ``cores`` threads."""
     from oracle import cref
 
+    t0 = time.perf_counter()
+    cref.apply_rows(mats, idx, deg, f64, rows=rows, nthreads=cores)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(f64, budget_s=12.0):
+    """The reference loop on the host cores over whole rows (all N columns each), as many rows
+    as fit in about ``budget_s`` seconds (the whole element set when it fits)."""
     import numpy as np
 
-    cores = os.cpu_count() or 1
-    sel = np.linspace(0, idx.shape[0] - 1, rows).astype(np.int32)
-    cref.apply_rows(mats, idx, deg, f64, rows=sel[:2], nthreads=cores)  # warm (build, page-in)
-    t0 = time.perf_counter()
-    cref.apply_rows(mats, idx, deg, f64, rows=sel, nthreads=cores)
-    dt = time.perf_counter() - t0
+    mats, idx, deg = oracle_workload()
+    N = idx.shape[0]
     B = deg ** idx.shape[1]
-    return {"value": rows * B / dt / 1e9, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": "%d of %d rows, reference loop (all pairs x 6 terms x 6-mode chain), FP64, %.2f s" %
-                      (rows, idx.shape[0], dt)}
+    cores = os.cpu_count() or 1
+    probe = np.arange(0, N, max(1, N // cores))[:cores].astype(np.int32)
+    time_reference_rows(mats, idx, deg, f64, probe[:2], cores)  # build, page-in
+    per_row = time_reference_rows(mats, idx, deg, f64, probe, cores) / probe.size
+    nrows = int(min(N, max(cores, budget_s / per_row)))
+    rows = np.linspace(0, N - 1, nrows).astype(np.int32)
+    dt = time_reference_rows(mats, idx, deg, f64, rows, cores)
+    return {"value": nrows * B / dt / 1e9, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": "%s: %d of %d whole rows (each over all %d columns x 6 terms x the 6-mode chain), FP64, "
+                      "%.2f s" % ("the whole element set" if nrows == N else "a row sample", nrows, N, N, dt)}
 
 
 def run_reference(args, rank):
-    """Time the CPU implementation of the path (C restatement of the reference loop) on the
-    host cores.  One step is a bounded sample of the workload: ``rows`` row elements x a
-    contiguous chunk of ``ncols`` column elements each, sized from a calibration step so that
-    warmup + steps stay within ~90 s; the rate is scaled to DOF of complete rows (a row needs
-    all N columns)."""
+    """Time the CPU implementation of the path on the host cores: the C restatement of the
+    reference loop (apply_A.m:102-236, all pairs, 6 terms, 6-mode chain, FP64, OpenMP over
+    rows).  Operators, element table and f come from the oracle alone (no product code).  A
+    step is one y = A f over the whole element set when warmup + steps fit in about
+    ``--ref-budget`` seconds, otherwise the same number of whole rows in every step (stated in
+    ``sample``)."""
     import numpy as np
 
     if rank != 0:
         return
-    from oracle import cref
-
-    pde, deg, idx, mats = build_workload()
+    mats, idx, deg = oracle_workload()
     N = idx.shape[0]
     B = deg ** idx.shape[1]
     f64 = np.random.default_rng(4).standard_normal(N * B)
     cores = os.cpu_count() or 1
-    rows = np.linspace(0, N - 1, min(N, max(cores, 1))).astype(np.int32)
-
-    def csr(ncols, shift):
-        rp = np.zeros(N + 1, dtype=np.int64)
-        cols = []
-        for r in rows:
-            c0 = (int(r) * 7 + shift) % N
-            cc = [(c0 + k) % N for k in range(ncols)]
-            cols.extend(cc)
-            rp[r + 1] = ncols
-        return np.cumsum(rp), np.array(cols, dtype=np.int32)
-
-    # calibrate: seconds per (row, column) pair with all threads busy
-    t0 = time.perf_counter()
-    cref.apply_rows(mats, idx, deg, f64, rows=rows, pairs0=csr(8, 0), nthreads=cores)
-    per_pair = (time.perf_counter() - t0) / (rows.size * 8)
+    probe = np.arange(0, N, max(1, N // cores))[:cores].astype(np.int32)
+    time_reference_rows(mats, idx, deg, f64, probe[:2], cores)  # build, page-in
+    per_row = time_reference_rows(mats, idx, deg, f64, probe, cores) / probe.size
     steps = max(1, args.steps)
     total = steps + max(args.warmup, 0)
-    t_step = min(2.0, max(0.005, 90.0 / total))
-    ncols = int(max(1, min(N, t_step / (per_pair * rows.size))))
-    pairs = [csr(ncols, k) for k in range(4)]
-    for k in range(max(args.warmup, 0)):
-        cref.apply_rows(mats, idx, deg, f64, rows=rows, pairs0=pairs[k % 4], nthreads=cores)
+    nrows = int(min(N, max(cores, args.ref_budget / total / per_row)))
+    rows = np.linspace(0, N - 1, nrows).astype(np.int32)
+    for _ in range(max(args.warmup, 0)):
+        time_reference_rows(mats, idx, deg, f64, rows, cores)
     t_all = 0.0
-    for k in range(steps):
-        t0 = time.perf_counter()
-        cref.apply_rows(mats, idx, deg, f64, rows=rows, pairs0=pairs[k % 4], nthreads=cores)
-        t_all += time.perf_counter() - t0
+    for _ in range(steps):
+        t_all += time_reference_rows(mats, idx, deg, f64, rows, cores)
     per_step = t_all / steps
-    row_equiv = rows.size * ncols / N
-    value = row_equiv * B / per_step / 1e9
-    sample = "%d rows x %d of %d columns per step (all 6 terms, 6-mode chain), FP64" % (rows.size, ncols, N)
+    value = nrows * B / per_step / 1e9
+    sample = ("the whole element set, %d rows x %d columns x 6 terms x the 6-mode chain, FP64" % (N, N) if nrows == N
+              else "%d of %d whole rows per step (each over all %d columns x 6 terms x the 6-mode chain), FP64"
+                   % (nrows, N, N))
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus, "steps": steps,
         "warmup": args.warmup, "ms_per_step": per_step * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (f ~ N(0,1), seed 4)",
-        "config": {"workload": WORKLOAD, "step": "bounded sample: " + sample,
-                   "implementation": "C restatement of apply_A.m's loop, OpenMP over rows "
-                                     "(the MATLAB reference cannot run on the box)",
-                   "l2": "host-only"},
+        "vs_baseline": None, "dtype": "f64", "data": DATA,
+        "config": workload_config(N * B),
+        "sample": sample,
+        "implementation": "C restatement of apply_A.m's loop (oracle/apply_a_ref.c), OpenMP over rows on %d host "
+                          "threads; operators and element table from the oracle (the MATLAB reference cannot run "
+                          "on the box)" % cores,
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "product_code_loaded": "asgkron" in sys.modules,
     }
     print(json.dumps(line), flush=True)
 
@@ -809,19 +827,18 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1:
-        cpu = cpu_baseline(mats, idx, deg, f64_h, max(1, args.cpu_rows))
+        cpu = cpu_baseline(f64_h)
 
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": apply_ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic (continuity6 operators from the DG builder; f ~ N(0,1) seed 4)",
-            "config": {"workload": WORKLOAD, "dof": dof, "work_model": "structured (zero blocks skipped, identity "
-                       "factors as copies; drop_tol %.0e)" % asgkron.DEFAULT_DROP_TOL,
-                       "entries": st["num_entries"], "kernel": asgkron._lib.KERNEL_NAMES[st["kernel_kind"]],
-                       "l2": "flushed before every step (512 MB write, outside the timed apply)",
-                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "vs_baseline": None, "dtype": "f32", "data": DATA,
+            "config": workload_config(dof),
+            "details": {"work_model": "structured (zero blocks skipped, identity factors as copies; drop_tol %.0e)"
+                                      % asgkron.DEFAULT_DROP_TOL,
+                        "entries": st["num_entries"], "kernel": asgkron._lib.KERNEL_NAMES[st["kernel_kind"]],
+                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
                          "algorithmic_bytes_per_launch": alg},

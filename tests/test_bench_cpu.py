@@ -28,11 +28,12 @@ def _check_reference_line(line, n_gpus):
     assert e2e["value"] == line["value"] and e2e["unit"] == line["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
     assert "workload" in line["config"]
+    assert line["product_code_loaded"] is False  # the arm runs the oracle's C loop on oracle-built inputs
 
 
 def test_reference_arm_json_line():
-    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "3"],
-                       cwd=ROOT, capture_output=True, text=True, timeout=600)
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1", "--warmup", "3",
+                        "--ref-budget", "4"], cwd=ROOT, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = _json_lines(r.stdout)
     assert len(lines) == 1, r.stdout
@@ -45,7 +46,7 @@ def test_reference_arm_under_torchrun_two_ranks():
         port = s.getsockname()[1]
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port),
-           "bench.py", "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "3"]
+           "bench.py", "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "3", "--ref-budget", "4"]
     r = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=900)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = _json_lines(r.stdout)
