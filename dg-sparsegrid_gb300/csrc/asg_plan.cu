@@ -826,6 +826,56 @@ asg_status asg_grad_ops_f32(asg_plan* p, const float* f, const float* r, float* 
   return asg::grad_ops<float>(p, f, r, G, ldg, stream);
 }
 
+asg_status asg_apply_T_host_f64(asg_plan* p, const double* h_ybar, double* h_fbar) {
+  if (!p) return fail(ASG_ERR_INVALID, "apply_T_host: NULL plan");
+  asg_status st = asg::build_transpose(p);
+  return st ? st : asg::apply_host<double>(p->tr, h_ybar, h_fbar);
+}
+
+asg_status asg_grad_ops_host_f64(asg_plan* p, const double* h_f, const double* h_r, double* const* h_G,
+                                 const int* ldg) {
+  if (!p || !h_f || !h_r || !h_G || !ldg) return fail(ASG_ERR_INVALID, "grad_ops_host: NULL argument");
+  const int TD = p->T * p->D;
+  const size_t n = static_cast<size_t>(p->N) * p->B;
+  const size_t vec = ((n * sizeof(double) + 255) / 256) * 256;
+  // staging: f, r and every requested gradient matrix (ldg x n1d, column-major), 256-byte aligned
+  std::vector<size_t> off(TD, 0);
+  size_t bytes = 2 * vec;
+  for (int tm = 0; tm < TD; ++tm) {
+    if (!h_G[tm] || p->op_off[tm] < 0) continue;
+    const int n1 = p->op_nb[tm] * p->P;
+    if (ldg[tm] < n1) return fail(ASG_ERR_INVALID, "grad_ops_host: ldg[%d]=%d < %d", tm, ldg[tm], n1);
+    off[tm] = bytes;
+    bytes += ((static_cast<size_t>(ldg[tm]) * n1 * sizeof(double) + 255) / 256) * 256;
+  }
+  if (!p->stream) ASG_CUDA(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
+  char* buf = nullptr;
+  ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&buf), bytes));
+  double* df = reinterpret_cast<double*>(buf);
+  double* dr = reinterpret_cast<double*>(buf + vec);
+  std::vector<double*> dG(TD, nullptr);
+  cudaError_t e = cudaMemcpyAsync(df, h_f, n * sizeof(double), cudaMemcpyHostToDevice, p->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dr, h_r, n * sizeof(double), cudaMemcpyHostToDevice, p->stream);
+  for (int tm = 0; tm < TD && e == cudaSuccess; ++tm) {
+    if (!off[tm]) continue;
+    dG[tm] = reinterpret_cast<double*>(buf + off[tm]);
+    const size_t gb = static_cast<size_t>(ldg[tm]) * p->op_nb[tm] * p->P * sizeof(double);
+    e = cudaMemcpyAsync(dG[tm], h_G[tm], gb, cudaMemcpyHostToDevice, p->stream);  // untouched entries kept
+  }
+  asg_status st = e == cudaSuccess ? ASG_OK : asg::cuda_fail(e, "grad_ops_host: copy in");
+  if (!st) st = asg::grad_ops<double>(p, df, dr, dG.data(), ldg, p->stream);
+  for (int tm = 0; tm < TD && !st; ++tm) {
+    if (!dG[tm]) continue;
+    const size_t gb = static_cast<size_t>(ldg[tm]) * p->op_nb[tm] * p->P * sizeof(double);
+    e = cudaMemcpyAsync(h_G[tm], dG[tm], gb, cudaMemcpyDeviceToHost, p->stream);
+    if (e != cudaSuccess) st = asg::cuda_fail(e, "grad_ops_host: copy out");
+  }
+  e = cudaStreamSynchronize(p->stream);
+  if (!st && e != cudaSuccess) st = asg::cuda_fail(e, "grad_ops_host: synchronize");
+  cudaFree(buf);
+  return st;
+}
+
 asg_status asg_apply_T_f64(asg_plan* p, const double* ybar, double* fbar, void* stream) {
   if (!p) return fail(ASG_ERR_INVALID, "apply_T: NULL plan");
   asg_status st = asg::build_transpose(p);

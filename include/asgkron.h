@@ -135,6 +135,13 @@ asg_status asg_grad_ops_f32(asg_plan* plan, const float* d_f, const float* d_r, 
  * MATLAB MEX gateway makes). */
 asg_status asg_apply_host_f64(asg_plan* plan, const double* h_f, double* h_y);
 asg_status asg_apply_host_f32(asg_plan* plan, const float* h_f, float* h_y);
+/* The adjoint and the operator gradients on host pointers (synchronous; the calls the adjoint
+ * MEX gateway makes).  h_G[t*d+k] are host column-major matrices with leading dimension
+ * ldg[t*d+k]; as in asg_grad_ops_f64, reached blocks are overwritten and the rest of each
+ * matrix is left as it was.  No reference counterpart (the prototype has no adjoint). */
+asg_status asg_apply_T_host_f64(asg_plan* plan, const double* h_ybar, double* h_fbar);
+asg_status asg_grad_ops_host_f64(asg_plan* plan, const double* h_f, const double* h_r, double* const* h_G,
+                                 const int* ldg);
 
 /* ---------------------------------------------------------------------------------------
  * Element tables and index maps (hash_table_sparse_nD.m, global_matrix.m, connect_nD.m)
