@@ -11,6 +11,7 @@
 #include <type_traits>
 
 #include "asg_internal.h"
+#include "asg_pipe.cuh"
 #include "asg_rows.cuh"
 
 namespace asg {
@@ -398,45 +399,6 @@ __global__ void __launch_bounds__(256) k_single_mode(ApplyArgs<T> a) {
 // products are summed in FP32 registers; groups are merged into the output tile with Kahan
 // compensation.  FP32 products use the paired FMA (fma.rn.f32x2).
 // ---------------------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                   smem_u32(dst)),
-               "l"(src), "r"(bytes), "r"(smem_u32(bar))
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// Bounded wait: true when the phase completed, false after ~2^31 cycles (~1 s).
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
-  if (mbar_test(bar, parity)) return true;
-  const long long t0 = clock64();
-  while (!mbar_test(bar, parity)) {
-    if (clock64() - t0 > (1LL << 31)) return false;
-  }
-  return true;
-}
-
-// Paired FP32 FMA (fma.rn.f32x2): two FMAs per instruction issue.
-__device__ __forceinline__ float2 ffma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-
 // g[a][c] += sum_b A[a][b] * x[b][c]   (contraction across the tile rows)
 template <typename T>
 __device__ __forceinline__ void tile_rows(T (&g)[4][4], const T* A, const T* xs, int s) {
@@ -464,9 +426,6 @@ __device__ __forceinline__ void tile_cols_s(T (&g)[4][4], const T* A, const T* x
   }
 }
 
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
 __device__ __forceinline__ void consumer_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
 
 // Base offset and row stride of a thread's P x P tile spanning dimensions (u, d-1): the
@@ -489,51 +448,6 @@ __device__ __forceinline__ void tile_place(int tid, int u, int D, const int* str
 // straight into it, the others through the transpose.  FP32 blocks arrive pair-duplicated
 // (see the plan's FP32 packing) so the paired FMA needs no register shuffling; groups merge
 // into the output tile with Kahan compensation.  Rows launch longest first (row_order).
-struct F32Tile {
-  float2 v[4][2];  // [tile row][column pair]
-};
-
-// g[a][c] += sum_b A[a][b] x[b][c]; A column b arrives as (A0b,A0b,A1b,A1b),(A2b,A2b,A3b,A3b)
-__device__ __forceinline__ void f32_rows(F32Tile& g, const float* Ad, const float* xs, int s) {
-#pragma unroll
-  for (int b = 0; b < 4; ++b) {
-    const float4 x = *reinterpret_cast<const float4*>(xs + b * s);
-    const float4 q0 = *reinterpret_cast<const float4*>(Ad + b * 8);
-    const float4 q1 = *reinterpret_cast<const float4*>(Ad + b * 8 + 4);
-    const float2 x01 = make_float2(x.x, x.y), x23 = make_float2(x.z, x.w);
-    const float2 a0 = make_float2(q0.x, q0.y), a1 = make_float2(q0.z, q0.w);
-    const float2 a2 = make_float2(q1.x, q1.y), a3 = make_float2(q1.z, q1.w);
-    g.v[0][0] = ffma2(a0, x01, g.v[0][0]); g.v[0][1] = ffma2(a0, x23, g.v[0][1]);
-    g.v[1][0] = ffma2(a1, x01, g.v[1][0]); g.v[1][1] = ffma2(a1, x23, g.v[1][1]);
-    g.v[2][0] = ffma2(a2, x01, g.v[2][0]); g.v[2][1] = ffma2(a2, x23, g.v[2][1]);
-    g.v[3][0] = ffma2(a3, x01, g.v[3][0]); g.v[3][1] = ffma2(a3, x23, g.v[3][1]);
-  }
-}
-// g[r][a] += sum_b A[a][b] x[r][b]; A column b arrives as (A0b,A1b,A2b,A3b)
-__device__ __forceinline__ void f32_cols(F32Tile& g, const float* Ap, const float* xs, int s) {
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const float4 x = *reinterpret_cast<const float4*>(xs + r * s);
-    const float xv[4] = {x.x, x.y, x.z, x.w};
-#pragma unroll
-    for (int b = 0; b < 4; ++b) {
-      const float4 q = *reinterpret_cast<const float4*>(Ap + b * 8);
-      const float2 xb = make_float2(xv[b], xv[b]);
-      g.v[r][0] = ffma2(make_float2(q.x, q.y), xb, g.v[r][0]);
-      g.v[r][1] = ffma2(make_float2(q.z, q.w), xb, g.v[r][1]);
-    }
-  }
-}
-__device__ __forceinline__ void kahan2(float2& s, float2& c, float2 v) {
-  float y = v.x - c.x, t = s.x + y;
-  c.x = (t - s.x) - y;
-  s.x = t;
-  y = v.y - c.y;
-  t = s.y + y;
-  c.y = (t - s.y) - y;
-  s.y = t;
-}
-
 template <typename T, int S, int MINB, bool CSMEM>
 __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
   constexpr int P = 4;

@@ -109,7 +109,32 @@ template <typename T>
 cudaError_t launch_grad(const GradArgs<T>& a, int P, cudaStream_t s);
 
 enum KernelKind { KK_CHAIN_WARP = 0, KK_CHAIN_CTA = 1, KK_SINGLE_MODE = 2, KK_SINGLE_TMA = 3, KK_SINGLE_TMA3 = 4,
-                  KK_SINGLE_TMA_ROWS = 5, KK_SINGLE_SMALL = 6 };
+                  KK_SINGLE_TMA_ROWS = 5, KK_SINGLE_SMALL = 6, KK_STREAM = 7 };
+
+// Streaming FP32 apply (deg 4, 4,096-value blocks, one applied factor per term): every CTA
+// walks its own work stream.  An entry is {column element j, row element, operator block
+// index, flags | applied dimension (bits 0-3)}.
+enum StreamFlags : int {
+  SF_SELF = 1 << 4,  // j is the row element: read the row's resident block
+  SF_ROW0 = 1 << 5,  // first entry of a row (its resident block is copied with this entry)
+  SF_ROW1 = 1 << 6,  // last entry of a row (y block written after it)
+  SF_GRP0 = 1 << 7,  // first entry of a group (entries of one applied dimension)
+  SF_GRP1 = 1 << 8,  // last entry of a group
+  SF_ZERO = 1 << 9   // a row without entries: its y block is written as zeros, nothing staged
+};
+struct StreamArgs {
+  const float* f;
+  float* y;
+  const float* ops_cols;  // FP32 blocks stored column by column (A0b,A1b,A2b,A3b), 16 values per block
+  const int4* ws;         // [nctas][ws_stride]: header {entry count}, then the entries; padded
+  int ws_stride;          // int4 per CTA: 1 + entries rounded up to 32
+  int nctas;
+  int* err;
+};
+// Dynamic shared memory and resident CTAs per SM of the streaming kernel (0 on error).
+size_t stream_smem();
+int stream_occupancy();
+cudaError_t launch_stream(const StreamArgs& a, cudaStream_t s);
 
 // Apply arguments (f and y unset) of a plan that runs the small-block single-mode kernel, for
 // kernels that call its row routine themselves (the fused GMRES cycle); false for other plans.
@@ -177,6 +202,11 @@ struct asg_plan {
   int* d_cta_ptr[2] = {nullptr, nullptr};
   int* d_cta_rows[2] = {nullptr, nullptr};
   float* d_ops_pair = nullptr;
+  float* d_ops_cols = nullptr;       // FP32 blocks column by column (deg 4 single-mode plans)
+  // streaming FP32 kernel: one padded work stream per CTA (4 ints per entry, header first)
+  std::vector<int> ws;
+  int ws_stride = 0, ws_ctas = 0;
+  int* d_ws = nullptr;
   // fused backward-Euler solve (small-block plans, built on first use), per basis precision
   // (0 FP64, 1 FP32): contiguous row ranges per CTA and chunks of their rows' entries per warp
   int fz_G[2] = {0, 0}, fz_max_rows[2] = {0, 0}, fz_max_slots[2] = {0, 0};

@@ -74,6 +74,8 @@ void free_device(asg_plan* p) {
     cudaFree(p->d_cta_rows[k]);
   }
   cudaFree(p->d_ops_pair);
+  cudaFree(p->d_ops_cols);
+  cudaFree(p->d_ws);
   for (int k = 0; k < 2; ++k) {
     cudaFree(p->d_fz_int[k]);
     cudaFree(p->d_fz_items[k]);
@@ -137,6 +139,14 @@ asg_status upload_ops(asg_plan* p) {
       }
     if (!p->d_ops_pair) ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_ops_pair), pr.size() * sizeof(float)));
     ASG_CUDA(cudaMemcpy(p->d_ops_pair, pr.data(), pr.size() * sizeof(float), cudaMemcpyHostToDevice));
+    // the same blocks column by column, (A0b, A1b, A2b, A3b) for b = 0..3: the streaming
+    // kernel's operator pairs (A0b, A1b), (A2b, A3b) for the paired FMA
+    std::vector<float> cols(h64.size());
+    for (size_t k = 0; k + 16 <= h64.size(); k += 16)
+      for (int b = 0; b < 4; ++b)
+        for (int r = 0; r < 4; ++r) cols[k + b * 4 + r] = static_cast<float>(h64[k + r * 4 + b]);
+    if (!p->d_ops_cols) ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_ops_cols), cols.size() * sizeof(float)));
+    ASG_CUDA(cudaMemcpy(p->d_ops_cols, cols.data(), cols.size() * sizeof(float), cudaMemcpyHostToDevice));
   }
   if (!p->d_ops64 && !h64.empty()) {
     ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_ops64), h64.size() * sizeof(double)));
@@ -146,6 +156,77 @@ asg_status upload_ops(asg_plan* p) {
     ASG_CUDA(cudaMemcpy(p->d_ops64, h64.data(), h64.size() * sizeof(double), cudaMemcpyHostToDevice));
     ASG_CUDA(cudaMemcpy(p->d_ops32, h32.data(), h32.size() * sizeof(float), cudaMemcpyHostToDevice));
   }
+  return ASG_OK;
+}
+
+// Work streams of the streaming FP32 kernel (one CTA per resident slot).  Rows go to CTAs by
+// longest-processing-time assignment of their cost: the 16 KB blocks a row gathers (its own
+// block once, plus one per off-diagonal entry) weighted 4, plus 1 per entry (consumer work).
+// A row's entries are ordered by applied dimension 0, 1, 2, 4 (through the transpose
+// buffers), then 3 and 5 (straight into the natural tile), each group in work-list order.
+// Expects p->ed filled.
+asg_status build_streams(asg_plan* p, int nsm) {
+  const int N = p->N;
+  const int occ = stream_occupancy();
+  if (occ <= 0) return fail(ASG_ERR_CUDA, "streaming apply kernel cannot be resident");
+  const int G = std::max(1, std::min(N, occ * nsm));
+  std::vector<long long> cost(N);
+  for (int i = 0; i < N; ++i) {
+    long long gathers = 1, n = p->row_ptr[i + 1] - p->row_ptr[i];
+    for (long long q = p->row_ptr[i]; q < p->row_ptr[i + 1]; ++q) gathers += p->ed[q].j != i;
+    cost[i] = 4 * gathers + n;
+  }
+  std::vector<int> by_cost(N);
+  for (int i = 0; i < N; ++i) by_cost[i] = i;
+  std::stable_sort(by_cost.begin(), by_cost.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+  std::vector<std::vector<int>> lists(G);
+  std::vector<std::pair<long long, int>> heap;  // (load, cta) min-heap
+  for (int c = 0; c < G; ++c) heap.push_back({0, c});
+  auto cmp = [](const std::pair<long long, int>& x, const std::pair<long long, int>& y) { return x > y; };
+  for (int i : by_cost) {
+    std::pop_heap(heap.begin(), heap.end(), cmp);
+    auto& top = heap.back();
+    lists[top.second].push_back(i);
+    top.first += cost[i];
+    std::push_heap(heap.begin(), heap.end(), cmp);
+  }
+  static const int kRank[6] = {0, 1, 2, 4, 3, 5};  // group position of applied dimension m
+  long long maxcount = 0;
+  std::vector<std::vector<int>> streams(G);
+  for (int c = 0; c < G; ++c) {
+    std::vector<int>& s = streams[c];
+    for (int i : lists[c]) {
+      if (p->row_ptr[i + 1] == p->row_ptr[i]) {  // no entries: y block of zeros
+        s.insert(s.end(), {i, i, 0, SF_ZERO});
+        continue;
+      }
+      std::vector<long long> q(p->row_ptr[i + 1] - p->row_ptr[i]);
+      for (size_t k = 0; k < q.size(); ++k) q[k] = p->row_ptr[i] + static_cast<long long>(k);
+      std::stable_sort(q.begin(), q.end(), [&](long long x, long long y) { return kRank[p->ed[x].m] < kRank[p->ed[y].m]; });
+      for (size_t k = 0; k < q.size(); ++k) {
+        const asg::EntryDesc& e = p->ed[q[k]];
+        if (e.aoff % 16 != 0 || e.aoff / 16 > (1LL << 30)) return fail(ASG_ERR_UNSUPPORTED, "operator block offset");
+        int fl = e.m;
+        if (e.j == i) fl |= SF_SELF;
+        if (k == 0) fl |= SF_ROW0;
+        if (k + 1 == q.size()) fl |= SF_ROW1;
+        if (k == 0 || p->ed[q[k - 1]].m != e.m) fl |= SF_GRP0;
+        if (k + 1 == q.size() || p->ed[q[k + 1]].m != e.m) fl |= SF_GRP1;
+        s.insert(s.end(), {e.j, i, static_cast<int>(e.aoff / 16), fl});
+      }
+    }
+    maxcount = std::max<long long>(maxcount, static_cast<long long>(s.size() / 4));
+  }
+  if (maxcount > (1LL << 28)) return fail(ASG_ERR_UNSUPPORTED, "work stream too long");
+  const int stride = 1 + static_cast<int>((maxcount + 31) / 32) * 32;
+  p->ws.assign(static_cast<size_t>(G) * stride * 4, 0);
+  for (int c = 0; c < G; ++c) {
+    int* dst = p->ws.data() + static_cast<size_t>(c) * stride * 4;
+    dst[0] = static_cast<int>(streams[c].size() / 4);
+    std::copy(streams[c].begin(), streams[c].end(), dst + 4);
+  }
+  p->ws_stride = stride;
+  p->ws_ctas = G;
   return ASG_OK;
 }
 
@@ -168,7 +249,7 @@ asg_status finalize(asg_plan* p) {
   for (int t = 0; t < T; ++t)
     if (__builtin_popcount(p->active[t]) != 1) single_terms = false;
   const bool single = single_terms && (P == 3 || P == 4) && B >= 32LL * P * P;
-  p->kernel_kind = single ? ((P == 4 && B == 4096) ? KK_SINGLE_TMA : KK_SINGLE_MODE)
+  p->kernel_kind = single ? ((P == 4 && B == 4096) ? KK_STREAM : KK_SINGLE_MODE)
                           : (B <= 256 ? (single_terms ? KK_SINGLE_SMALL : KK_CHAIN_WARP) : KK_CHAIN_CTA);
   p->row_order.clear();
   p->ed.clear();
@@ -200,11 +281,14 @@ asg_status finalize(asg_plan* p) {
     p->cta_ptr[k].clear();
     p->cta_rows[k].clear();
   }
+  int nsm = 0;
   if (single && P == 4 && B == 4096 && N > 0) {
-    int dev = 0, nsm = 0;
+    int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return cuda_fail(e, "device attributes");
+  }
+  if (single && P == 4 && B == 4096 && N > 0) {
     for (int k = 0; k < 2; ++k) {
       const int occ = single_tma_rows_occupancy(k == 0 ? 8 : 4);
       if (occ <= 0) return fail(ASG_ERR_CUDA, "persistent single-mode kernel cannot be resident");
@@ -232,7 +316,14 @@ asg_status finalize(asg_plan* p) {
       }
     }
   }
+  p->ws.clear();
+  p->ws_stride = p->ws_ctas = 0;
+  if (single && P == 4 && B == 4096 && N > 0) {
+    asg_status sst = build_streams(p, nsm);
+    if (sst) return sst;
+  }
   asg_status st;
+  if ((st = upload(&p->d_ws, p->ws))) return st;
   for (int k = 0; k < 2; ++k) {
     if ((st = upload(&p->d_cta_ptr[k], p->cta_ptr[k]))) return st;
     if ((st = upload(&p->d_cta_rows[k], p->cta_rows[k]))) return st;
@@ -494,9 +585,24 @@ asg_status apply_dev(asg_plan* p, const T* f, T* y, void* stream) {
   st = check_ptr(y, "y");
   if (st) return st;
   if (f == y) return fail(ASG_ERR_INVALID, "apply: f and y must not alias");
+  if (p->kernel_kind == KK_STREAM && sizeof(T) == 4) {
+    StreamArgs sa{};
+    sa.f = reinterpret_cast<const float*>(f);
+    sa.y = reinterpret_cast<float*>(y);
+    sa.ops_cols = p->d_ops_cols;
+    sa.ws = reinterpret_cast<const int4*>(p->d_ws);
+    sa.ws_stride = p->ws_stride;
+    sa.nctas = p->ws_ctas;
+    sa.err = p->d_err;
+    cudaError_t e = launch_stream(sa, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "apply kernel launch");
+    return ASG_OK;
+  }
   const T* ops = sizeof(T) == 8 ? reinterpret_cast<const T*>(p->d_ops64) : reinterpret_cast<const T*>(p->d_ops32);
   ApplyArgs<T> a = make_args<T>(p, f, y, ops);
-  cudaError_t e = launch_apply<T>(a, p->P, p->kernel_kind, static_cast<cudaStream_t>(stream));
+  // the streaming kernel is FP32 only: FP64 runs the bulk-copy pipeline of kind 3
+  const int kind = p->kernel_kind == KK_STREAM ? KK_SINGLE_TMA : p->kernel_kind;
+  cudaError_t e = launch_apply<T>(a, p->P, kind, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "apply kernel launch");
   return ASG_OK;
 }
@@ -787,6 +893,8 @@ asg_status asg_plan_update_ops(asg_plan* p, const double* const* ops, const int*
 asg_status asg_plan_set_kernel(asg_plan* p, int kind) {
   if (!p) return fail(ASG_ERR_INVALID, "plan_set_kernel: NULL plan");
   if (kind == asg::KK_CHAIN_WARP && p->B > 256) return fail(ASG_ERR_UNSUPPORTED, "warp chain kernel needs deg^d <= 256");
+  if (kind == asg::KK_STREAM && p->ws_ctas <= 0)
+    return fail(ASG_ERR_UNSUPPORTED, "streaming kernel needs deg 4, d 6 and one non-identity factor per term");
   if (kind == asg::KK_SINGLE_MODE || kind == asg::KK_SINGLE_TMA || kind == asg::KK_SINGLE_TMA3 ||
       kind == asg::KK_SINGLE_TMA_ROWS) {
     bool ok = kind != asg::KK_SINGLE_MODE ? (p->P == 4 && p->B == 4096)
@@ -800,7 +908,7 @@ asg_status asg_plan_set_kernel(asg_plan* p, int kind) {
     for (unsigned a : p->active) ok = ok && __builtin_popcount(a) == 1;
     if (!ok) return fail(ASG_ERR_UNSUPPORTED, "small single-mode kernel needs one applied factor per term, deg^d <= 256");
   }
-  if (kind < 0 || kind > 6) return fail(ASG_ERR_INVALID, "unknown kernel kind %d", kind);
+  if (kind < 0 || kind > 7) return fail(ASG_ERR_INVALID, "unknown kernel kind %d", kind);
   p->kernel_kind = kind;
   return ASG_OK;
 }
