@@ -121,6 +121,8 @@ SIGNATURES = {
     "asg_apply_host_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "asg_apply_host_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "asg_apply_T_host_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "asg_assemble_bsr_f64": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_int), C.c_void_p,
+                                       C.c_longlong, C.POINTER(C.c_longlong), C.c_void_p]),
     "asg_grad_ops_host_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_void_p),
                                         C.POINTER(C.c_int)]),
     "asg_hash_table_sparse_nd": (C.c_int, [C.c_int, C.POINTER(C.c_int), C.c_int, C.c_int, C.POINTER(C.c_int),

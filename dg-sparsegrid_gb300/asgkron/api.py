@@ -215,6 +215,25 @@ class Plan:
             raise TypeError("f must be float64 or float32")
         return out
 
+    def assemble_bsr(self, device=None):
+        """The operator the plan applies as a scipy.sparse.bsr_matrix (FP64), assembled on the GPU
+        (asg_assemble_bsr_f64; apply_A.m's build_A branch, apply_A.m:170-180,246-248)."""
+        import scipy.sparse as sp
+        import torch
+
+        nb = C.c_longlong(0)
+        check(lib().asg_assemble_bsr_f64(self._handle, None, None, None, 0, C.byref(nb), None))
+        rp = np.zeros(self.N + 1, dtype=np.int64)
+        cols = np.zeros(max(1, nb.value), dtype=np.int32)
+        check(lib().asg_assemble_bsr_f64(self._handle, rp.ctypes.data_as(C.POINTER(C.c_longlong)),
+                                         cols.ctypes.data_as(C.POINTER(C.c_int)), None, 0, C.byref(nb), None))
+        dev = device if device is not None else torch.device("cuda", torch.cuda.current_device())
+        blocks = torch.empty((max(1, nb.value), self.B, self.B), dtype=torch.float64, device=dev)
+        check(lib().asg_assemble_bsr_f64(self._handle, None, None, C.c_void_p(blocks.data_ptr()), nb.value,
+                                         C.byref(nb), C.c_void_p(torch.cuda.current_stream(dev).cuda_stream)))
+        data = blocks[:nb.value].cpu().numpy()
+        return sp.bsr_matrix((data, cols[:nb.value], rp), shape=(self.dof, self.dof))
+
     def close(self):
         if self._handle:
             lib().asg_plan_destroy(self._handle)

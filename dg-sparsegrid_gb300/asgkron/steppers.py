@@ -104,11 +104,30 @@ class RK3Stepper:
         return self._f_static
 
 
+# GMRES precision modes (asg_gmres_opts.mixed): the outer residual, its norm and x are FP64 in
+# all three; "matvec32" runs only the operator application in FP32 (the basis, the Arnoldi
+# dot products and norms, the Givens rotations and the solution update stay FP64);
+# "inner32" runs the whole inner cycle in FP32; "fp64" nothing.
+GMRES_MODES = {"fp64": 0, "inner32": 1, "matvec32": 2}
+
+
+def gmres_mode(mixed):
+    """asg_gmres_opts.mixed for ``mixed``: a mode name, True (= "matvec32") or False (= "fp64")."""
+    if mixed is True:
+        return GMRES_MODES["matvec32"]
+    if mixed is False or mixed is None:
+        return GMRES_MODES["fp64"]
+    if mixed not in GMRES_MODES:
+        raise ValueError("mixed must be True, False or one of %s" % sorted(GMRES_MODES))
+    return GMRES_MODES[mixed]
+
+
 def be_solve(plan, dt, b, x, restart=30, tol=1e-10, max_outer=60, inner_reduction=1e-5, mixed=True):
-    """Solve (I - dt A) x = b in place (FP64 CUDA tensors); returns the info dict."""
+    """Solve (I - dt A) x = b in place (FP64 CUDA tensors); returns the info dict.  ``mixed``
+    selects the precision of the GMRES cycles (see GMRES_MODES; True = "matvec32")."""
     import torch
 
-    opts = GmresOpts(int(restart), int(max_outer), float(tol), float(inner_reduction), 1 if mixed else 0)
+    opts = GmresOpts(int(restart), int(max_outer), float(tol), float(inner_reduction), gmres_mode(mixed))
     nbytes = C.c_size_t(0)
     check(lib().asg_be_workspace(plan.handle, C.byref(opts), C.byref(nbytes)))
     work = torch.empty(max(1, nbytes.value), dtype=torch.uint8, device=x.device)

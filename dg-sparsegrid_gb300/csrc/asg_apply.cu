@@ -445,15 +445,16 @@ __device__ __forceinline__ void tile_place(int tid, int u, int D, const int* str
 // group boundary the stage just consumed doubles as the transpose buffer (no separate
 // scratch).  The natural output tile of a thread spans dimensions (d-3, d-1): consecutive
 // threads sit 16 bytes apart in shared memory; terms on dimensions d-3 and d-1 accumulate
-// straight into it, the others through the transpose.  FP32 blocks arrive pair-duplicated
-// (see the plan's FP32 packing) so the paired FMA needs no register shuffling; groups merge
-// into the output tile with Kahan compensation.  Rows launch longest first (row_order).
+// straight into it, the others through the transpose.  FP32 blocks arrive column by column,
+// so one 128-bit shared load per operator column gives the paired FMA two pairs of operator
+// rows (the input value is duplicated in registers); groups merge into the output tile with
+// Kahan compensation.  Rows launch longest first (row_order).
 template <typename T, int S, int MINB, bool CSMEM>
 __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
   constexpr int P = 4;
   constexpr bool F32 = sizeof(T) == 4;
   constexpr bool CS = F32 && CSMEM;  // FP32 compensation tile in shared memory (else registers)
-  constexpr int AB = F32 ? 32 : 16;  // operator block values per stage
+  constexpr int AB = 16;  // operator block values per stage (FP32: column by column)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_abort;
   const int tid = threadIdx.x;
@@ -470,7 +471,7 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
   const int n = static_cast<int>(a.row_ptr[row + 1] - q0);
   const EntryDesc* ed = a.ed + q0;
   const uint32_t fbytes = static_cast<uint32_t>(B * sizeof(T)), abytes = AB * sizeof(T);
-  const T* opsrc = F32 ? reinterpret_cast<const T*>(a.ops_pair) : a.ops;
+  const T* opsrc = F32 ? reinterpret_cast<const T*>(a.ops_cols) : a.ops;
 
   if (tid == 0) {
     s_abort = 0;
@@ -533,7 +534,8 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
   bool direct = false, gave_up = false;
   int mlane = -1;
   // FP32: paired state, compensation in registers or shared memory; FP64: scalar state
-  F32Tile g32, n32, c32;
+  PairTile g32;  // a group's sums (pairs of operator rows)
+  F32Tile n32, c32;
   T g[P][P], nat[P][P];
 #pragma unroll
   for (int r = 0; r < P; ++r) {
@@ -580,7 +582,10 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
       if (direct) {
         if constexpr (F32) {
 #pragma unroll
-          for (int r = 0; r < P; ++r) merge_row(r, g32.v[r][0], g32.v[r][1]);
+          for (int r = 0; r < P; ++r) {
+            const float4 v = pt_row(g32, r, cur_m == D - 1);
+            merge_row(r, make_float2(v.x, v.y), make_float2(v.z, v.w));
+          }
         } else {
 #pragma unroll
           for (int r = 0; r < P; ++r)
@@ -595,7 +600,7 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
         for (int r = 0; r < P; ++r) {
           if constexpr (F32) {
             *reinterpret_cast<float4*>(scr + base_g + r * s_g) =
-                make_float4(g32.v[r][0].x, g32.v[r][0].y, g32.v[r][1].x, g32.v[r][1].y);
+                pt_row(g32, r, false);
           } else {
             Row<T, P> rr;
 #pragma unroll
@@ -644,9 +649,9 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
     const T* sp = stages + st * SST;
     if constexpr (F32) {
       if (m == D - 1)
-        f32_cols(g32, reinterpret_cast<const float*>(sp + B), reinterpret_cast<const float*>(sp + base_g), s_g);
+        pt_cols(g32, reinterpret_cast<const float*>(sp + B), reinterpret_cast<const float*>(sp + base_g), s_g);
       else
-        f32_rows(g32, reinterpret_cast<const float*>(sp + B), reinterpret_cast<const float*>(sp + base_g), s_g);
+        pt_rows(g32, reinterpret_cast<const float*>(sp + B), reinterpret_cast<const float*>(sp + base_g), s_g);
     } else {
       T A[P * P];
 #pragma unroll
@@ -689,7 +694,7 @@ template <typename T, int S, int MINB>
 __global__ void __launch_bounds__(288, MINB) k_single_tma_rows(ApplyArgs<T> a) {
   constexpr int P = 4;
   constexpr bool F32 = sizeof(T) == 4;
-  constexpr int AB = F32 ? 32 : 16;  // operator block values per stage
+  constexpr int AB = 16;  // operator block values per stage (FP32: column by column)
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_abort;
   const int tid = threadIdx.x;
@@ -701,7 +706,7 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma_rows(ApplyArgs<T> a) {
   uint64_t* empty = full + S;
   const int ri0 = a.cta_ptr[blockIdx.x], ri1 = a.cta_ptr[blockIdx.x + 1];
   const uint32_t fbytes = static_cast<uint32_t>(B * sizeof(T)), abytes = AB * sizeof(T);
-  const T* opsrc = F32 ? reinterpret_cast<const T*>(a.ops_pair) : a.ops;
+  const T* opsrc = F32 ? reinterpret_cast<const T*>(a.ops_cols) : a.ops;
 
   if (tid == 0) {
     s_abort = 0;
@@ -774,7 +779,8 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma_rows(ApplyArgs<T> a) {
     const EntryDesc* ed = a.ed + q0;
     int cur_m = -1, base_g = 0, s_g = 0, pend = -1, mlane = -1;
     bool direct = false;
-    F32Tile g32, n32, c32;
+    PairTile g32;  // a group's sums (pairs of operator rows)
+    F32Tile n32, c32;
     T gg[P][P], nat[P][P];
 #pragma unroll
     for (int r = 0; r < P; ++r) {
@@ -802,8 +808,9 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma_rows(ApplyArgs<T> a) {
           if constexpr (F32) {
 #pragma unroll
             for (int r = 0; r < P; ++r) {
-              kahan2(n32.v[r][0], c32.v[r][0], g32.v[r][0]);
-              kahan2(n32.v[r][1], c32.v[r][1], g32.v[r][1]);
+              const float4 v = pt_row(g32, r, cur_m == D - 1);
+              kahan2(n32.v[r][0], c32.v[r][0], make_float2(v.x, v.y));
+              kahan2(n32.v[r][1], c32.v[r][1], make_float2(v.z, v.w));
             }
           } else {
 #pragma unroll
@@ -819,7 +826,7 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma_rows(ApplyArgs<T> a) {
           for (int r = 0; r < P; ++r) {
             if constexpr (F32) {
               *reinterpret_cast<float4*>(scr + base_g + r * s_g) =
-                  make_float4(g32.v[r][0].x, g32.v[r][0].y, g32.v[r][1].x, g32.v[r][1].y);
+                  pt_row(g32, r, false);
             } else {
               Row<T, P> rr;
 #pragma unroll
@@ -869,9 +876,9 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma_rows(ApplyArgs<T> a) {
       const T* sp = stages + st * SST;
       if constexpr (F32) {
         if (m == D - 1)
-          f32_cols(g32, reinterpret_cast<const float*>(sp + B), reinterpret_cast<const float*>(sp + base_g), s_g);
+          pt_cols(g32, reinterpret_cast<const float*>(sp + B), reinterpret_cast<const float*>(sp + base_g), s_g);
         else
-          f32_rows(g32, reinterpret_cast<const float*>(sp + B), reinterpret_cast<const float*>(sp + base_g), s_g);
+          pt_rows(g32, reinterpret_cast<const float*>(sp + B), reinterpret_cast<const float*>(sp + base_g), s_g);
       } else {
         T A[P * P];
 #pragma unroll
@@ -1146,7 +1153,7 @@ cudaError_t ensure_smem(K kernel, size_t bytes, size_t max_bytes, bool& done) {
 // full/empty barriers.
 template <typename T>
 size_t rows_smem(int S, int B) {
-  return static_cast<size_t>(S) * (B + (sizeof(T) == 4 ? 32 : 16)) * sizeof(T) + 2 * S * sizeof(uint64_t);
+  return static_cast<size_t>(S) * (B + 16) * sizeof(T) + 2 * S * sizeof(uint64_t);
 }
 
 template <typename T, int P>
@@ -1180,9 +1187,9 @@ cudaError_t launch_p(const ApplyArgs<T>& a, int kind, cudaStream_t s) {
       // FP32: 3 stages + compensation tile (3 CTAs per SM), or 4 stages (2 per SM, kind 4);
       // FP64: 3 stages, 1 CTA per SM
       if (a.B != 256 * P * P) return cudaErrorInvalidValue;  // 8 consumer warps own one tile each
-      if (sizeof(T) == 4 && !a.ops_pair) return cudaErrorInvalidValue;
+      if (sizeof(T) == 4 && !a.ops_cols) return cudaErrorInvalidValue;
       auto smem_for = [&](int S, bool csmem) {
-        return static_cast<size_t>(S) * (a.B + (sizeof(T) == 4 ? 32 : 16)) * sizeof(T) +
+        return static_cast<size_t>(S) * (a.B + 16) * sizeof(T) +
                (csmem ? a.B * sizeof(float) : 0) + 2 * S * sizeof(uint64_t);
       };
       if constexpr (sizeof(T) == 4) {
@@ -1239,7 +1246,7 @@ cudaError_t launch_p(const ApplyArgs<T>& a, int kind, cudaStream_t s) {
   if constexpr (P == 4) {
     if (kind == KK_SINGLE_TMA_ROWS) {
       if (a.B != 256 * P * P || !a.cta_ptr || !a.cta_rows || a.nctas <= 0) return cudaErrorInvalidValue;
-      if (sizeof(T) == 4 && !a.ops_pair) return cudaErrorInvalidValue;
+      if (sizeof(T) == 4 && !a.ops_cols) return cudaErrorInvalidValue;
       constexpr int S0 = sizeof(T) == 4 ? 4 : 3;
       const size_t sm = rows_smem<T>(S0, a.B);
       auto kern = k_single_tma_rows<T, S0, sizeof(T) == 4 ? 2 : 1>;

@@ -59,6 +59,7 @@ struct ApplyArgs {
   int stride[kMaxDims];      // deg^(D-1-m): element-block stride of dimension m
   const EntryDesc* ed;       // [entries] single-mode descriptors (NULL for chain plans)
   const float* ops_pair;     // FP32 blocks in paired-FMA order (32 values per block), single-mode plans
+  const float* ops_cols;     // FP32 blocks column by column (A0b,A1b,A2b,A3b), 16 values, deg-4 single-mode plans
   const int* row_order;      // [N] launch order of rows (longest work first) or NULL
   int* err;                  // device status word (ASG_ERR_TIMEOUT after a bounded wait gave up)
   const int* cta_ptr;        // [nctas+1] persistent single-mode kernel: rows of CTA c are

@@ -249,7 +249,7 @@ asg_status finalize(asg_plan* p) {
   for (int t = 0; t < T; ++t)
     if (__builtin_popcount(p->active[t]) != 1) single_terms = false;
   const bool single = single_terms && (P == 3 || P == 4) && B >= 32LL * P * P;
-  p->kernel_kind = single ? ((P == 4 && B == 4096) ? KK_STREAM : KK_SINGLE_MODE)
+  p->kernel_kind = single ? ((P == 4 && B == 4096) ? KK_SINGLE_TMA : KK_SINGLE_MODE)
                           : (B <= 256 ? (single_terms ? KK_SINGLE_SMALL : KK_CHAIN_WARP) : KK_CHAIN_CTA);
   p->row_order.clear();
   p->ed.clear();
@@ -558,6 +558,7 @@ ApplyArgs<T> make_args(const asg_plan* p, const T* f, T* y, const T* ops) {
   a.ed = p->d_ed;
   a.err = p->d_err;
   a.ops_pair = p->d_ops_pair;
+  a.ops_cols = p->d_ops_cols;
   a.row_order = p->d_row_order;
   const int pk = sizeof(T) == 4 ? 1 : 0;
   a.cta_ptr = p->d_cta_ptr[pk];

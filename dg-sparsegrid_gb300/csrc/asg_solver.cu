@@ -117,13 +117,23 @@ struct GmresState {
   double rel;
 };
 // w = V_j - dt * (A V_j), skipped once the cycle is done
-template <typename TV>
-__global__ void k_shift_g(long long n, double dt, const TV* __restrict__ x, const TV* __restrict__ ax,
+template <typename TV, typename TA>
+__global__ void k_shift_g(long long n, double dt, const TV* __restrict__ x, const TA* __restrict__ ax,
                           double* __restrict__ w, const GmresState* __restrict__ st) {
   if (st->done) return;
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
        i += static_cast<long long>(gridDim.x) * blockDim.x)
     w[i] = static_cast<double>(x[i]) - dt * static_cast<double>(ax[i]);
+}
+// out = x rounded to TA (the operand of an operator application in another precision),
+// skipped once the cycle is done
+template <typename TV, typename TA>
+__global__ void k_round_g(long long n, const TV* __restrict__ x, TA* __restrict__ out,
+                          const GmresState* __restrict__ st) {
+  if (st->done) return;
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x)
+    out[i] = static_cast<TA>(x[i]);
 }
 // partial[j * gridDim.x + b] = block b's share of <w, V_j> (FP64), j = blockIdx.y
 template <typename TV>
@@ -298,14 +308,14 @@ constexpr int kFzThreads = 512;
 constexpr int kFzWarps = kFzThreads / 32;
 constexpr int kFzGivensWarps = 2;  // warps that run the Givens step while the others apply the operator
 
-template <typename TV>
+template <typename TV, typename TA>
 struct FusedArgs {
-  ApplyArgs<TV> a;             // the plan's apply arguments in the basis precision (f, y unused)
+  ApplyArgs<TA> a;             // the plan's apply arguments in the application precision (f, y unused)
   ApplyArgs<double> a64;       // and in FP64, for the outer residual
   long long n, ldv;
   double dt, tol, inner_reduction;
   int m, max_outer;
-  TV* V;                       // global copy of the vector the operator is applied to (n values)
+  TA* V;                       // global copy of the vector the operator is applied to (n values)
   double* partial;             // (2m + 2) rows of gridDim.x CTA partials
   const double* rhs;           // b
   double* x;                   // initial guess in, solution out
@@ -477,12 +487,14 @@ __device__ __forceinline__ void slot_reduce(const T* slots, const int* row_slot,
 }
 
 // The inner GMRES cycle (w, the dot products and their sums, the orthogonalisation updates,
-// the Givens rotations, R y = g and V y) runs in TV, the basis precision: FP32 for the mixed
-// solver, on the FP32 pipes (an FP32 basis holds the Arnoldi relation to FP32 accuracy
-// only, and the FP64 outer residual corrects), FP64 for the FP64 solver.  The outer
-// residual, its norm, b and x are FP64 in both.
-template <typename TV, int P, int MAXO>
-__global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constant__ FusedArgs<TV> c) {
+// the Givens rotations, R y = g and V y) runs in TV, the basis precision, and the operator
+// inside it in TA: FP32 / FP32 for the solver with an FP32 inner cycle, on the FP32 pipes (an
+// FP32 basis holds the Arnoldi relation to FP32 accuracy only, and the FP64 outer residual
+// corrects); FP64 / FP32 for the solver that keeps the Arnoldi dot products, norms and updates
+// in FP64 and runs only the operator in FP32; FP64 / FP64 for the FP64 solver.  The outer
+// residual, its norm, b and x are FP64 in all three.
+template <typename TV, typename TA, int P, int MAXO>
+__global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constant__ FusedArgs<TV, TA> c) {
   extern __shared__ __align__(16) unsigned char fz_smem[];
   __shared__ TV s_h[kMaxRestart], s_h2[kMaxRestart + 1];
   __shared__ TV s_g[kMaxRestart + 1], s_hc[kMaxRestart + 1], s_rc[kMaxRestart + 1], s_y[kMaxRestart];
@@ -510,7 +522,7 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
   sp += align16(static_cast<size_t>(Smax) * sizeof(TV));
   double* rs = reinterpret_cast<double*>(sp);
   sp += align16(static_cast<size_t>(Smax) * sizeof(double));
-  TV* slots = reinterpret_cast<TV*>(sp);
+  TA* slots = reinterpret_cast<TA*>(sp);
   double* slots64 = reinterpret_cast<double*>(sp);
   const int slot0 = c.blk_slot[b];
   TV* pv = reinterpret_cast<TV*>(c.partial);  // rows of TV partials
@@ -526,15 +538,15 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
   const TV dtv = static_cast<TV>(c.dt);
   // row routine: fiber rows for FP32, per-output rows for FP64 (the faster of the two in each
   // precision); the FP64 residual uses the same lane layout
-  using Lane = typename std::conditional<sizeof(TV) == 4, FiberLane<MAXO>, SmallLane<MAXO>>::type;
+  using Lane = typename std::conditional<sizeof(TA) == 4, FiberLane<MAXO>, SmallLane<MAXO>>::type;
   Lane sl;
-  if constexpr (sizeof(TV) == 4)
-    sl = fiber_lane<TV, P, MAXO>(c.a, lane);
+  if constexpr (sizeof(TA) == 4)
+    sl = fiber_lane<TA, P, MAXO>(c.a, lane);
   else
-    sl = small_lane<TV, P, MAXO>(c.a, lane);
+    sl = small_lane<TA, P, MAXO>(c.a, lane);
   int team = 1;  // lanes per element in the slot sums
   while (team < 32 && 2 * team * S <= kFzThreads) team <<= 1;
-  TV* axs = reinterpret_cast<TV*>(rs);  // A w' for the CTA's rows (rs is free during a cycle)
+  TA* axs = reinterpret_cast<TA*>(rs);  // A w' for the CTA's rows (rs is free during a cycle)
   {  // ||b||
     double acc = 0.0;
     for (int e = tid; e < S; e += kFzThreads) acc = fma(c.rhs[i0 + e], c.rhs[i0 + e], acc);
@@ -579,13 +591,13 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
     // Zs[k] = (I - dt A) v_k.  The operator is applied to w' (w after the first Gram-Schmidt
     // pass, published before the second barrier), and (I - dt A) v_{j+1} =
     // ((I - dt A) w' - sum_k h2_k Z_k) / ||w|| -- so no barrier only to publish v_{j+1}.
-    TV* W = c.V;  // global copy of the vector the operator is applied to next
+    TA* W = c.V;  // global copy of the vector the operator is applied to next
     {
       const double ib = 1.0 / rn;
       for (int e = tid; e < S; e += kFzThreads) {
         const TV v = static_cast<TV>(rs[e] * ib);
         Vs[e] = v;
-        W[i0 + e] = v;
+        W[i0 + e] = static_cast<TA>(v);
       }
     }
     for (int q = tid; q < (m + 1) * (m + 1); q += kFzThreads) s_Q[q] = q == 0 ? TV(1) : TV(0);
@@ -594,11 +606,11 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
       s_g[0] = static_cast<TV>(rn);
     }
     if (!(ok = gsync())) break;
-    apply_items<TV, P, MAXO>(c.a, W, c.items, it0, it1, slot0, slots, sl);
+    apply_items<TA, P, MAXO>(c.a, W, c.items, it0, it1, slot0, slots, sl);
     __syncthreads();
     slot_reduce(slots, c.row_slot, r0, slot0, S, B, team, axs);
     for (int e = tid; e < S; e += kFzThreads) {
-      const TV z = fma(-dtv, axs[e], Vs[e]);
+      const TV z = fma(-dtv, static_cast<TV>(axs[e]), Vs[e]);
       Zs[e] = z;
       ws[e] = z;
     }
@@ -620,7 +632,7 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
         TV acc = ws[e];
         for (int k = 0; k <= j; ++k) acc = fma(-s_h[k], Vs[k * Smax + e], acc);
         ws[e] = acc;
-        W[i0 + e] = acc;
+        W[i0 + e] = static_cast<TA>(acc);
       }
       __syncthreads();
       for (int k = warp; k <= j + 1; k += kFzWarps) {
@@ -698,7 +710,7 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
       if (warp < kFzGivensWarps) {
         if (!s_need) givens();
       } else {
-        apply_items<TV, P, MAXO>(c.a, W, c.items, it0, it1, slot0, slots, sl);
+        apply_items<TA, P, MAXO>(c.a, W, c.items, it0, it1, slot0, slots, sl);
       }
       __syncthreads();
       if (s_need) {  // the same decision in every CTA: explicit ||w' - V h2||^2, then the Givens step
@@ -724,7 +736,7 @@ __global__ void __launch_bounds__(kFzThreads, 1) k_be_fused(const __grid_constan
         TV* Zn = Zs + (j + 1) * Smax;
         for (int e = tid; e < S; e += kFzThreads) {
           const TV wp = ws[e];
-          TV v = wp, z = fma(-dtv, axs[e], wp);
+          TV v = wp, z = fma(-dtv, static_cast<TV>(axs[e]), wp);
           for (int k = 0; k <= j; ++k) {
             v = fma(-s_h2[k], Vs[k * Smax + e], v);
             z = fma(-s_h2[k], Zs[k * Smax + e], z);
@@ -790,14 +802,16 @@ namespace {
 size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 
 struct GmresLayout {
-  size_t v, w, r, ax64, axmv, h, y, partial, hcol, hh, cs, sn, g, state, total;
+  size_t v, vf, w, r, ax64, axmv, h, y, partial, hcol, hh, cs, sn, g, state, total;
 };
 
 // Leading dimension of the Krylov basis: every basis vector starts on a 32-byte boundary (the
 // operator application reads it with 16-byte loads, in either precision).
 long long basis_ld(long long n) { return (n + 3) / 4 * 4; }
 
-GmresLayout gmres_layout(long long n, int m, bool mixed) {
+// mode: ASG_GMRES_FP64, ASG_GMRES_FP32_INNER or ASG_GMRES_FP32_MATVEC (asgkron.h)
+GmresLayout gmres_layout(long long n, int m, int mode) {
+  const bool basis32 = mode == ASG_GMRES_FP32_INNER, apply32 = mode != ASG_GMRES_FP64;
   GmresLayout L{};
   size_t off = 0;
   auto take = [&](size_t bytes) {
@@ -805,11 +819,12 @@ GmresLayout gmres_layout(long long n, int m, bool mixed) {
     off += align256(bytes);
     return o;
   };
-  L.v = take(static_cast<size_t>(m + 1) * basis_ld(n) * (mixed ? sizeof(float) : sizeof(double)));
+  L.v = take(static_cast<size_t>(m + 1) * basis_ld(n) * (basis32 ? sizeof(float) : sizeof(double)));
+  L.vf = take(apply32 && !basis32 ? basis_ld(n) * sizeof(float) : 0);
   L.w = take(n * sizeof(double));
   L.r = take(n * sizeof(double));
   L.ax64 = take(n * sizeof(double));
-  L.axmv = take(n * (mixed ? sizeof(float) : sizeof(double)));
+  L.axmv = take(n * (apply32 ? sizeof(float) : sizeof(double)));
   L.h = take((m + 1) * sizeof(double));
   L.y = take((m + 1) * sizeof(double));
   L.partial = take(static_cast<size_t>(2 * m + 2) * asg::kRedBlocks * sizeof(double));
@@ -964,9 +979,9 @@ asg_status fused_schedule(asg_plan* p, int k) {
 
 // The fused solve (one cooperative launch) for plans on the small-block single-mode kernel
 // with deg 2..4 whose per-CTA slices fit in shared memory.
-template <typename TV, int P, int MAXO>
-cudaError_t launch_fused(const asg::FusedArgs<TV>& c, int G, size_t smem, cudaStream_t s) {
-  auto kern = asg::k_be_fused<TV, P, MAXO>;
+template <typename TV, typename TA, int P, int MAXO>
+cudaError_t launch_fused(const asg::FusedArgs<TV, TA>& c, int G, size_t smem, cudaStream_t s) {
+  auto kern = asg::k_be_fused<TV, TA, P, MAXO>;
   // the shared-memory limit, co-residency and cooperative-launch support, queried once per
   // instantiation and shared-memory size
   static size_t checked_smem = 0;
@@ -984,23 +999,23 @@ cudaError_t launch_fused(const asg::FusedArgs<TV>& c, int G, size_t smem, cudaSt
     checked_smem = smem;
   }
   if (resident < G) return cudaErrorNotSupported;
-  void* args[] = {const_cast<asg::FusedArgs<TV>*>(&c)};
+  void* args[] = {const_cast<asg::FusedArgs<TV, TA>*>(&c)};
   return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(kern), dim3(G), dim3(asg::kFzThreads), args, smem, s);
 }
 
-template <typename TV, int P>
-cudaError_t launch_fused_p(const asg::FusedArgs<TV>& c, int G, size_t smem, cudaStream_t s) {
-  // outputs (FP64, per-output rows) or fibers (FP32) per lane
+template <typename TV, typename TA, int P>
+cudaError_t launch_fused_p(const asg::FusedArgs<TV, TA>& c, int G, size_t smem, cudaStream_t s) {
+  // outputs (FP64 operator, per-output rows) or fibers (FP32 operator) per lane
   const int B = c.a.B, Lf = B / P;
-  if constexpr (sizeof(TV) == 4) {
-    if (Lf <= 32) return launch_fused<TV, P, 1>(c, G, smem, s);
-    if (Lf <= 64) return launch_fused<TV, P, 2>(c, G, smem, s);
-    return launch_fused<TV, P, 4>(c, G, smem, s);
+  if constexpr (sizeof(TA) == 4) {
+    if (Lf <= 32) return launch_fused<TV, TA, P, 1>(c, G, smem, s);
+    if (Lf <= 64) return launch_fused<TV, TA, P, 2>(c, G, smem, s);
+    return launch_fused<TV, TA, P, 4>(c, G, smem, s);
   } else {
-    if (B <= 32) return launch_fused<TV, P, 1>(c, G, smem, s);
-    if (B <= 64) return launch_fused<TV, P, 2>(c, G, smem, s);
-    if (B <= 128) return launch_fused<TV, P, 4>(c, G, smem, s);
-    return launch_fused<TV, P, 8>(c, G, smem, s);
+    if (B <= 32) return launch_fused<TV, TA, P, 1>(c, G, smem, s);
+    if (B <= 64) return launch_fused<TV, TA, P, 2>(c, G, smem, s);
+    if (B <= 128) return launch_fused<TV, TA, P, 4>(c, G, smem, s);
+    return launch_fused<TV, TA, P, 8>(c, G, smem, s);
   }
 }
 
@@ -1009,17 +1024,17 @@ int g_withhold = -1;  // asg_debug_withhold_arrival
 
 // The whole solve as one launch when the plan qualifies (*used = true; one synchronisation
 // to read the result); *used = false otherwise (the caller runs the host-driven solve).
-template <typename TV>
+template <typename TV, typename TA>
 asg_status be_solve_fused(asg_plan* plan, long long n, double dt, const double* b, double* x, const asg_gmres_opts* o,
                           asg_gmres_info* info, unsigned char* base, const GmresLayout& L, cudaStream_t s, bool* used) {
   *used = false;
-  asg::FusedArgs<TV> c{};
-  if (!asg::small_plan_args<TV>(plan, &c.a) || !asg::small_plan_args<double>(plan, &c.a64) || c.a.B > 256) return ASG_OK;
+  asg::FusedArgs<TV, TA> c{};
+  if (!asg::small_plan_args<TA>(plan, &c.a) || !asg::small_plan_args<double>(plan, &c.a64) || c.a.B > 256) return ASG_OK;
   if ((reinterpret_cast<uintptr_t>(b) | reinterpret_cast<uintptr_t>(x)) & 15) return ASG_OK;  // vector loads of x
   const int P = c.a.D >= 2 ? c.a.stride[c.a.D - 2] : c.a.B;
   if (P < 2 || P > 4) return ASG_OK;
   const int m = o->restart;
-  const int k = sizeof(TV) == 4 ? 1 : 0;
+  const int k = sizeof(TA) == 4 ? 1 : 0;  // the work schedule follows the operator's lane layout
   asg_status st = fused_schedule(plan, k);
   if (st) return st;
   const int G = plan->fz_G[k];
@@ -1032,7 +1047,7 @@ asg_status be_solve_fused(asg_plan* plan, long long n, double dt, const double* 
   c.inner_reduction = o->inner_reduction;
   c.m = m;
   c.max_outer = o->max_outer;
-  c.V = reinterpret_cast<TV*>(base + L.v);
+  c.V = reinterpret_cast<TA*>(base + L.v);
   c.partial = reinterpret_cast<double*>(base + L.partial);
   c.rhs = b;
   c.x = x;
@@ -1048,9 +1063,9 @@ asg_status be_solve_fused(asg_plan* plan, long long n, double dt, const double* 
   c.withhold = g_withhold;
   g_withhold = -1;
   ASG_CUDA(cudaMemsetAsync(c.state, 0, sizeof(asg::GmresState), s));
-  cudaError_t e = P == 2 ? launch_fused_p<TV, 2>(c, G, smem, s)
-                  : P == 3 ? launch_fused_p<TV, 3>(c, G, smem, s)
-                           : launch_fused_p<TV, 4>(c, G, smem, s);
+  cudaError_t e = P == 2 ? launch_fused_p<TV, TA, 2>(c, G, smem, s)
+                  : P == 3 ? launch_fused_p<TV, TA, 3>(c, G, smem, s)
+                           : launch_fused_p<TV, TA, 4>(c, G, smem, s);
   if (e == cudaErrorNotSupported) {
     cudaGetLastError();
     return ASG_OK;  // the CTAs cannot all be resident: the caller runs the host-driven solve
@@ -1073,17 +1088,18 @@ asg_status be_solve_fused(asg_plan* plan, long long n, double dt, const double* 
 }
 
 // One GMRES(m) cycle on (I - dt A) delta = r0 (r0 FP64, beta = ||r0||), adding delta to x64
-// in FP64.  TV is the basis and operator-application precision.  Stops early when the
-// residual estimate drops to rtol_abs.  *iters = Arnoldi steps taken, *resid = final residual
-// estimate.
-template <typename TV>
+// in FP64.  TV is the basis precision, TA the operator application's (a TV basis vector is
+// rounded to TA first when they differ).  Stops early when the residual estimate drops to
+// rtol_abs.  *iters = Arnoldi steps taken, *resid = final residual estimate.
+template <typename TV, typename TA>
 asg_status gmres_cycle(asg_plan* plan, long long n, double dt, const double* r0, double beta, double* x64, int m,
                        double rtol_abs, unsigned char* base, const GmresLayout& L, cudaStream_t s, int* iters,
                        double* resid) {
   TV* V = reinterpret_cast<TV*>(base + L.v);
   const long long ldv = basis_ld(n);
   double* w = reinterpret_cast<double*>(base + L.w);
-  TV* axmv = reinterpret_cast<TV*>(base + L.axmv);
+  TA* axmv = reinterpret_cast<TA*>(base + L.axmv);
+  TA* vf = reinterpret_cast<TA*>(base + L.vf);  // V_j rounded to TA (TA != TV only)
   double* h_dev = reinterpret_cast<double*>(base + L.h);
   double* y_dev = reinterpret_cast<double*>(base + L.y);
   double* partial = reinterpret_cast<double*>(base + L.partial);
@@ -1111,12 +1127,17 @@ asg_status gmres_cycle(asg_plan* plan, long long n, double dt, const double* r0,
   for (int j0 = 0; j0 < m; j0 += kChunk) {
     for (int j = j0; j < std::min(m, j0 + kChunk); ++j) {
       // w = V_j - dt * A V_j
-      asg_status ast = sizeof(TV) == 4 ? asg_apply_f32(plan, reinterpret_cast<const float*>(V + j * ldv),
+      const TA* vin = reinterpret_cast<const TA*>(V + j * ldv);
+      if (sizeof(TA) != sizeof(TV)) {
+        asg::k_round_g<TV, TA><<<gr, 256, 0, s>>>(n, V + j * ldv, vf, state);
+        vin = vf;
+      }
+      asg_status ast = sizeof(TA) == 4 ? asg_apply_f32(plan, reinterpret_cast<const float*>(vin),
                                                        reinterpret_cast<float*>(axmv), s)
-                                       : asg_apply_f64(plan, reinterpret_cast<const double*>(V + j * ldv),
+                                       : asg_apply_f64(plan, reinterpret_cast<const double*>(vin),
                                                        reinterpret_cast<double*>(axmv), s);
       if (ast) return ast;
-      asg::k_shift_g<TV><<<gr, 256, 0, s>>>(n, dt, V + j * ldv, axmv, w, state);
+      asg::k_shift_g<TV, TA><<<gr, 256, 0, s>>>(n, dt, V + j * ldv, axmv, w, state);
       for (int pass = 0; pass < 2; ++pass) {  // classical Gram-Schmidt, reorthogonalised (FP64)
         asg::k_dots_g<TV><<<dim3(nb, j + 1), asg::kRedThreads, 0, s>>>(n, w, V, ldv, partial, state);
         asg::k_dots_final_g<<<j + 1, 32, 0, s>>>(j + 1, nb, partial, h_dev, hcol, pass, state);
@@ -1140,14 +1161,14 @@ asg_status gmres_cycle(asg_plan* plan, long long n, double dt, const double* r0,
   return ASG_OK;
 }
 
-template <typename TV>
+template <typename TV, typename TA>
 asg_status be_solve(asg_plan* p, double dt, const double* b, double* x, const asg_gmres_opts* o, asg_gmres_info* info,
                     void* work, size_t work_bytes, void* stream) {
   asg_plan_stats ps{};
   asg_plan_stats_get(p, &ps);
   const long long n = ps.dof;
   const int m = o->restart;
-  const GmresLayout L = gmres_layout(n, m, sizeof(TV) == 4);
+  const GmresLayout L = gmres_layout(n, m, o->mixed);
   if (work_bytes < L.total) return fail(ASG_ERR_CAPACITY, "be_solve: workspace needs %zu bytes", L.total);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   unsigned char* base = static_cast<unsigned char*>(work);
@@ -1157,7 +1178,7 @@ asg_status be_solve(asg_plan* p, double dt, const double* b, double* x, const as
   const int gr = asg::grid_for(n);
   asg_status st = ASG_OK;
   bool used = false;
-  if ((st = be_solve_fused<TV>(p, n, dt, b, x, o, info, base, L, s, &used)) || used) return st;
+  if ((st = be_solve_fused<TV, TA>(p, n, dt, b, x, o, info, base, L, s, &used)) || used) return st;
   const int nb = asg::red_blocks(n);
   asg::k_norm2<<<nb, asg::kRedThreads, 0, s>>>(n, b, partial);
   const double bnorm = host_norm(partial, nb, s, &st);
@@ -1182,7 +1203,7 @@ asg_status be_solve(asg_plan* p, double dt, const double* b, double* x, const as
     const double target = std::max(o->tol * bnorm, rn * o->inner_reduction);
     int it = 0;
     double est = 0.0;
-    if ((st = gmres_cycle<TV>(p, n, dt, r, rn, x, m, target, base, L, s, &it, &est))) return st;
+    if ((st = gmres_cycle<TV, TA>(p, n, dt, r, rn, x, m, target, base, L, s, &it, &est))) return st;
     inf.inner_iters += it;
   }
   if (info) *info = inf;
@@ -1251,7 +1272,9 @@ asg_status asg_be_workspace(const asg_plan* plan, const asg_gmres_opts* opts, si
   if (opts->restart < 1 || opts->restart > asg::kMaxRestart) return fail(ASG_ERR_INVALID, "be_workspace: restart=%d", opts->restart);
   asg_plan_stats ps{};
   asg_plan_stats_get(plan, &ps);
-  *bytes = gmres_layout(ps.dof, opts->restart, opts->mixed != 0).total;
+  if (opts->mixed < ASG_GMRES_FP64 || opts->mixed > ASG_GMRES_FP32_MATVEC)
+    return fail(ASG_ERR_INVALID, "be_workspace: mixed=%d", opts->mixed);
+  *bytes = gmres_layout(ps.dof, opts->restart, opts->mixed).total;
   return ASG_OK;
 }
 
@@ -1259,10 +1282,17 @@ asg_status asg_be_solve(asg_plan* plan, double dt, const double* d_b, double* d_
                         asg_gmres_info* info, void* d_work, size_t work_bytes, void* stream) {
   if (!plan || !d_b || !d_x || !opts || !d_work) return fail(ASG_ERR_INVALID, "be_solve: NULL argument");
   if (opts->restart < 1 || opts->restart > asg::kMaxRestart || opts->max_outer < 0 || !(opts->tol > 0) ||
-      !(opts->inner_reduction > 0 && opts->inner_reduction < 1))
+      !(opts->inner_reduction > 0 && opts->inner_reduction < 1) || opts->mixed < ASG_GMRES_FP64 ||
+      opts->mixed > ASG_GMRES_FP32_MATVEC)
     return fail(ASG_ERR_INVALID, "be_solve: bad options");
-  return opts->mixed ? be_solve<float>(plan, dt, d_b, d_x, opts, info, d_work, work_bytes, stream)
-                     : be_solve<double>(plan, dt, d_b, d_x, opts, info, d_work, work_bytes, stream);
+  switch (opts->mixed) {
+    case ASG_GMRES_FP32_INNER:
+      return be_solve<float, float>(plan, dt, d_b, d_x, opts, info, d_work, work_bytes, stream);
+    case ASG_GMRES_FP32_MATVEC:
+      return be_solve<double, float>(plan, dt, d_b, d_x, opts, info, d_work, work_bytes, stream);
+    default:
+      return be_solve<double, double>(plan, dt, d_b, d_x, opts, info, d_work, work_bytes, stream);
+  }
 }
 
 asg_status asg_debug_withhold_arrival(int barrier) {

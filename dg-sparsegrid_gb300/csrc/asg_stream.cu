@@ -46,56 +46,6 @@ __device__ __forceinline__ void stream_tile(int tid, int u, int& base, int& s) {
   base = (tid >> sh) * s * 4 + (tid & ((1 << sh) - 1)) * 4;
 }
 
-// A group's sums as pairs of operator rows: v[c][p] = (y[2p][c], y[2p+1][c]) with y[r][c]
-// row r along the applied dimension m, column c along dimension 5.  For m = 5 the roles swap:
-// v[r][p] = (y[r][2p], y[r][2p+1]), the row r along dimension 3.
-struct PairTile {
-  float2 v[4][2];
-};
-__device__ __forceinline__ void zero_pt(PairTile& t) {
-#pragma unroll
-  for (int r = 0; r < 4; ++r) t.v[r][0] = t.v[r][1] = make_float2(0.f, 0.f);
-}
-__device__ __forceinline__ float2 dup(float x) { return make_float2(x, x); }
-
-// m != 5: y[a][c] += sum_b A[a][b] x[b][c]; x rows s apart, A column b = (A0b, A1b, A2b, A3b)
-__device__ __forceinline__ void pt_rows(PairTile& g, const float* A, const float* xs, int s) {
-#pragma unroll
-  for (int b = 0; b < 4; ++b) {
-    const float4 x = *reinterpret_cast<const float4*>(xs + b * s);
-    const float4 q = *reinterpret_cast<const float4*>(A + 4 * b);
-    const float2 a01 = make_float2(q.x, q.y), a23 = make_float2(q.z, q.w);
-    g.v[0][0] = ffma2(a01, dup(x.x), g.v[0][0]); g.v[0][1] = ffma2(a23, dup(x.x), g.v[0][1]);
-    g.v[1][0] = ffma2(a01, dup(x.y), g.v[1][0]); g.v[1][1] = ffma2(a23, dup(x.y), g.v[1][1]);
-    g.v[2][0] = ffma2(a01, dup(x.z), g.v[2][0]); g.v[2][1] = ffma2(a23, dup(x.z), g.v[2][1]);
-    g.v[3][0] = ffma2(a01, dup(x.w), g.v[3][0]); g.v[3][1] = ffma2(a23, dup(x.w), g.v[3][1]);
-  }
-}
-// m == 5: y[r][a] += sum_b A[a][b] x[r][b]; x rows s apart (natural rows along dimension 3)
-__device__ __forceinline__ void pt_cols(PairTile& g, const float* A, const float* xs, int s) {
-  float4 q[4];
-#pragma unroll
-  for (int b = 0; b < 4; ++b) q[b] = *reinterpret_cast<const float4*>(A + 4 * b);
-#pragma unroll
-  for (int r = 0; r < 4; ++r) {
-    const float4 x = *reinterpret_cast<const float4*>(xs + r * s);
-    const float xv[4] = {x.x, x.y, x.z, x.w};
-#pragma unroll
-    for (int b = 0; b < 4; ++b) {
-      g.v[r][0] = ffma2(make_float2(q[b].x, q[b].y), dup(xv[b]), g.v[r][0]);
-      g.v[r][1] = ffma2(make_float2(q[b].z, q[b].w), dup(xv[b]), g.v[r][1]);
-    }
-  }
-}
-// Row r (along the group's dimension; along dimension 3 for m == 5) of a group's sums, as the
-// four values of dimension 5.
-__device__ __forceinline__ float4 pt_row(const PairTile& g, int r, bool cols) {
-  if (cols) return make_float4(g.v[r][0].x, g.v[r][0].y, g.v[r][1].x, g.v[r][1].y);
-  const int p = r >> 1;
-  return (r & 1) ? make_float4(g.v[0][p].y, g.v[1][p].y, g.v[2][p].y, g.v[3][p].y)
-                 : make_float4(g.v[0][p].x, g.v[1][p].x, g.v[2][p].x, g.v[3][p].x);
-}
-
 // Named hardware barrier among the 256 consumer threads (the transpose buffers).
 __device__ __forceinline__ void consumers_sync() { asm volatile("bar.sync 15, 256;" ::: "memory"); }
 

@@ -146,6 +146,17 @@ asg_status asg_apply_T_host_f64(asg_plan* plan, const double* h_ybar, double* h_
 asg_status asg_grad_ops_host_f64(asg_plan* plan, const double* h_f, const double* h_r, double* const* h_G,
                                  const int* ldg);
 
+/* The operator as block-sparse rows (apply_A.m:170-180,246-248, opts.build_A: A(I,J) +=
+ * krond(...) over the terms).  Block (i, j) is deg^d x deg^d, the sum over the plan's terms of
+ * kron_k A_{t,k}[I_k(i), J_k(j)] (identity factors exact, products with a structurally zero
+ * factor block left out under ASG_STRUCT_DETECT): the matrix the kernels apply.  Writes the
+ * block count to *num_blocks and, when not NULL, the structure to host row_ptr[N+1] and
+ * cols[num_blocks] (0-based, columns ascending in each row); d_blocks == NULL stops there.
+ * Otherwise d_blocks (device, capacity blocks) receives each block row-major, FP64.
+ * deg^d <= 256.  Synchronous. */
+asg_status asg_assemble_bsr_f64(asg_plan* plan, long long* row_ptr, int* cols, double* d_blocks, long long capacity,
+                                long long* num_blocks, void* stream);
+
 /* ---------------------------------------------------------------------------------------
  * Element tables and index maps (hash_table_sparse_nD.m, global_matrix.m, connect_nD.m)
  * ------------------------------------------------------------------------------------- */
@@ -243,12 +254,22 @@ asg_status asg_rk3_step_f32(asg_plan* plan, float* d_f, double dt, const float* 
 asg_status asg_lincomb_f64(long long n, int ns, const double* d_coef, const double* const* d_vecs, double* d_out,
                            void* stream);
 
+/* Precision of the GMRES cycles inside iterative refinement (asg_gmres_opts.mixed).  The outer
+ * residual b - (I - dt A) x, its norm and x are FP64 in every mode. */
+enum {
+  ASG_GMRES_FP64 = 0,        /* everything FP64 */
+  ASG_GMRES_FP32_INNER = 1,  /* the whole inner cycle in FP32: operator, basis, dot products,
+                                norms, Givens rotations and R y = g */
+  ASG_GMRES_FP32_MATVEC = 2  /* only the operator application in FP32; the basis, the Arnoldi
+                                dot products and norms, the Givens rotations and the solution
+                                update in FP64 */
+};
 typedef struct {
   int restart;             /* GMRES(m) Krylov dimension per cycle, 1..64 */
   int max_outer;           /* refinement steps (each one GMRES cycle on the FP64 residual) */
   double tol;              /* stop when ||b - (I - dt A) x|| <= tol * ||b|| */
   double inner_reduction;  /* each cycle stops once its residual drops by this factor */
-  int mixed;               /* 1: FP32 operator application and basis inside GMRES; 0: all FP64 */
+  int mixed;               /* ASG_GMRES_* */
 } asg_gmres_opts;
 typedef struct {
   int outer_iters;
@@ -259,7 +280,7 @@ typedef struct {
 /* Backward Euler solve (I - dt A) x = b (backward_euler, time_advance.m:267-349, which
  * assembles A and uses a direct solve): matrix-free GMRES(m) inside iterative refinement.
  * The outer residual b - (I - dt A) x, its norm and x are FP64; each GMRES cycle runs in the
- * basis precision (FP32 with opts->mixed, else FP64).  Plans on the small-block kernel with
+ * precision opts->mixed selects (ASG_GMRES_*).  Plans on the small-block kernel with
  * deg 2..4 run the whole solve as one cooperative launch (one synchronisation); other plans
  * run it kernel by kernel.  d_x holds the initial guess on entry; d_b and d_x 16-byte
  * aligned.  ASG_ERR_TIMEOUT: a bounded grid-barrier wait of the one-launch solve gave up. */
