@@ -385,30 +385,27 @@ def precision_continuity3(dev, flush, stream):
     return out
 
 
-def run_batched(args, rank, local):
-    """Batching configuration: 256 independent problems, each d ~ U{2,3,4}, SG level ~ U{3..7},
-    degree ~ U{2..4} (seed 3), d terms of dense N(0, 1/deg) 1-D operators (no structure, so
-    every (pair, term) of all N^2 pairs is executed: the reference work model), f ~ N(0,1).
-    One step = one persistent launch over all problems (FP32, tuned, replayed from a CUDA
-    graph).  Baseline: the same problems as sequential FP64 single-problem launches.  The inputs of
-    the 256-problem draw (62 MB of f, 5.8 GB of work lists at 4 bytes per work entry) exceed L2, so
-    no flush is needed; config["l2"] reports the size of the draw actually run."""
+def batched_measure(dev, count, max_level, steps, warmup):
+    """Batching configuration: ``count`` independent problems, each d ~ U{2,3,4}, SG level ~
+    U{3..max_level}, degree ~ U{2..4} (seed 3), d terms of dense N(0, 1/deg) 1-D operators (no
+    structure, so every (pair, term) of all N^2 pairs is executed: the reference work model),
+    f ~ N(0,1).  One step = one persistent launch over all problems (FP32, tuned, replayed from
+    a CUDA graph).  Baseline: the same problems as sequential FP64 single-problem launches.  The
+    256-problem draw's inputs (62 MB of f, 5.8 GB of work lists at 4 bytes per work entry)
+    exceed L2, so no flush is needed.  Returns the measurements (dict)."""
     import numpy as np
     import torch
 
     import asgkron
     from asgkron.batch import Batch
 
-    if rank != 0:
-        return
-    dev = torch.device("cuda", local)
-    torch.cuda.set_device(dev)
     rng = np.random.default_rng(3)
     plans, f64s = [], []
     flops, wl_bytes = 0.0, 0
-    for _ in range(args.batch_problems):
+    t_build = time.perf_counter()
+    for _ in range(count):
         d = int(rng.choice([2, 3, 4]))
-        lev = int(rng.integers(3, args.batch_max_level + 1))
+        lev = int(rng.integers(3, max_level + 1))
         deg = int(rng.integers(2, 5))
         idx = asgkron.hash_table_sparse_nD([lev] * d, 8).idx1d()
         n = deg * 2 ** lev
@@ -420,6 +417,7 @@ def run_batched(args, rank, local):
         wl_bytes += 4 * st["num_entries"]  # one 4-byte (column, term) word per work entry
         plans.append(p)
         f64s.append(torch.from_numpy(rng.standard_normal(p.dof)).to(dev))
+    build_s = time.perf_counter() - t_build
     dof = sum(p.dof for p in plans)
     f32s = [f.float() for f in f64s]
     y32s = [torch.empty_like(f) for f in f32s]
@@ -429,8 +427,7 @@ def run_batched(args, rank, local):
     b.tune()
     g = b.capture()
     stream = torch.cuda.current_stream(dev)
-    steps = max(1, min(args.steps, 20))
-    for _ in range(max(3, args.warmup)):
+    for _ in range(max(3, warmup)):
         g.replay()
     torch.cuda.synchronize()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
@@ -466,30 +463,51 @@ def run_batched(args, rank, local):
             h.copy_(d_, non_blocking=True)
         torch.cuda.synchronize()
     e2e_ms = (time.perf_counter() - t0) / e2e_steps * 1e3
-    info = b.info()
+    out = {"problems": count, "max_level": max_level, "dof": dof, "ms": ms, "value": dof / (ms * 1e-3) / 1e9,
+           "gflops_per_s": flops / (ms * 1e-3) / 1e9, "flops_per_step": flops, "work_list_bytes": wl_bytes,
+           "tuned": b.info(), "build_s": build_s,
+           "fp64_sequential_launches": {"ms": ms64, "value": dof / (ms64 * 1e-3) / 1e9,
+                                        "gflops_per_s": flops / (ms64 * 1e-3) / 1e9},
+           "speedup_vs_fp64_sequential": ms64 / ms,
+           "fp32_rel_err_vs_fp64": {"max": max(errs), "median": statistics.median(errs)},
+           "e2e_ms": e2e_ms, "e2e_value": dof / (e2e_ms * 1e-3) / 1e9}
+    b.close()
+    for p in plans:
+        p.close()
+    return out
+
+
+def run_batched(args, rank, local):
+    """The batching configuration alone (rank 0): see batched_measure; one JSON line."""
+    import torch
+
+    if rank != 0:
+        return
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    steps = max(1, min(args.steps, 20))
+    r = batched_measure(dev, args.batch_problems, args.batch_max_level, steps, args.warmup)
+    wl = r["work_list_bytes"]
     line = {
-        "metric": METRIC, "value": dof / (ms * 1e-3) / 1e9, "unit": UNIT, "n_gpus": 1, "steps": steps,
-        "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": 1, "steps": steps,
+        "warmup": max(3, args.warmup), "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (dense N(0,1/deg) operators, f ~ N(0,1), seed 3)",
         "config": {"workload": "batched: %d problems, d in {2,3,4}, SG lev 3..%d, deg 2..4, all pairs"
                                % (args.batch_problems, args.batch_max_level),
-                   "dof": dof, "flops_per_step": flops, "l2": ("inputs larger than L2 (%.3g GB work lists)" if wl_bytes > 129e6 else
-                          "work lists within L2 (%.3g GB), no flush") % (wl_bytes / 1e9),
-                   "launch": "one persistent launch replayed from a CUDA graph", "tuned": info},
-        "compute": {"gflops_per_s": flops / (ms * 1e-3) / 1e9},
-        "variants": {"fp64_sequential_launches": {"count": len(plans), "ms": ms64, "value": dof / (ms64 * 1e-3) / 1e9,
-                                                       "gflops_per_s": flops / (ms64 * 1e-3) / 1e9},
-                     "speedup_vs_fp64_sequential": ms64 / ms,
-                     "fp32_rel_err_vs_fp64": {"max": max(errs), "median": statistics.median(errs)}},
-        "e2e": {"value": dof / (e2e_ms * 1e-3) / 1e9, "unit": UNIT, "h2d_bytes_per_step": 4 * dof,
-                "d2h_bytes_per_step": 4 * dof, "ms_per_step": e2e_ms},
+                   "dof": r["dof"], "flops_per_step": r["flops_per_step"],
+                   "l2": ("inputs larger than L2 (%.3g GB work lists)" if wl > 129e6 else
+                          "work lists within L2 (%.3g GB), no flush") % (wl / 1e9),
+                   "launch": "one persistent launch replayed from a CUDA graph", "tuned": r["tuned"]},
+        "compute": {"gflops_per_s": r["gflops_per_s"]},
+        "variants": {"fp64_sequential_launches": dict(r["fp64_sequential_launches"], count=args.batch_problems),
+                     "speedup_vs_fp64_sequential": r["speedup_vs_fp64_sequential"],
+                     "fp32_rel_err_vs_fp64": r["fp32_rel_err_vs_fp64"]},
+        "e2e": {"value": r["e2e_value"], "unit": UNIT, "h2d_bytes_per_step": 4 * r["dof"],
+                "d2h_bytes_per_step": 4 * r["dof"], "ms_per_step": r["e2e_ms"]},
         "gpu_launches": steps * 2,  # counter reset (memset node) + the persistent kernel per replay
     }
     print(json.dumps(line), flush=True)
-    b.close()
-    for p in plans:
-        p.close()
 
 
 def batch_draws(count, max_level, seed=3):
@@ -814,6 +832,7 @@ def main():
         variants["continuity2_lev4_deg2_fp64_graph"] = small_config_graph(dev)
         variants["implicit_diffusion2_lev8_deg4"] = implicit_steps(dev)
         variants["precision_continuity3_lev6_deg3"] = precision_continuity3(dev, flush, stream)
+        variants["batched_256_lev3_7"] = batched_measure(dev, 256, 7, max(1, min(args.steps, 5)), 3)
 
     # ---- roofline ------------------------------------------------------------------------
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")

@@ -108,6 +108,9 @@ SIGNATURES = {
     "asg_plan_stats_get": (C.c_int, [C.c_void_p, C.POINTER(PlanStats)]),
     "asg_plan_update_ops": (C.c_int, [C.c_void_p, C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.c_int)]),
     "asg_plan_set_kernel": (C.c_int, [C.c_void_p, C.c_int]),
+    "asg_plan_tune": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_float),
+                                C.POINTER(C.c_float)]),
+    "asg_plan_kernel_for": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
     "asg_plan_active": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint)]),
     "asg_plan_device_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "asg_apply_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

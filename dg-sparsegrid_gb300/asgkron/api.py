@@ -105,6 +105,27 @@ class Plan:
         check(lib().asg_plan_stats_get(self._handle, C.byref(s)))
         return {k: getattr(s, k) for k, _ in PlanStats._fields_}
 
+    def tune(self, dtype="float32", stream=None):
+        """asg_plan_tune: time every kernel family for this plan in one precision and keep the
+        fastest; returns {"kind", "name", "ms", "default_ms"}."""
+        import torch
+
+        prec = 1 if dtype in ("float32", torch.float32) else 0
+        k, ms, dms = C.c_int(0), C.c_float(0), C.c_float(0)
+        s = stream if stream is not None else torch.cuda.current_stream()
+        check(lib().asg_plan_tune(self._handle, prec, C.c_void_p(s.cuda_stream), C.byref(k), C.byref(ms), C.byref(dms)))
+        from ._lib import KERNEL_NAMES
+
+        return {"kind": k.value, "name": KERNEL_NAMES[k.value], "ms": ms.value, "default_ms": dms.value}
+
+    def kernel_for(self, dtype="float32"):
+        """The kernel kind applies in this precision run (tuned or the plan's default)."""
+        import torch
+
+        k = C.c_int(0)
+        check(lib().asg_plan_kernel_for(self._handle, 1 if dtype in ("float32", torch.float32) else 0, C.byref(k)))
+        return k.value
+
     def set_kernel(self, kind):
         check(lib().asg_plan_set_kernel(self._handle, int(kind)))
 

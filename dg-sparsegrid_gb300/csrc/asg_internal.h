@@ -154,6 +154,7 @@ struct asg_plan {
   int structure = 0;
   double drop_tol = 0.0;
   int kernel_kind = 0;
+  int tuned_kind[2] = {-1, -1};      // asg_plan_tune's choice per precision (0 FP64, 1 FP32), -1: none
   // host-side metadata
   std::vector<int> idx1d;            // N*D, 0-based
   std::vector<int> op_nb;            // T*D
@@ -220,4 +221,11 @@ struct asg_plan {
   void* d_io = nullptr;
   size_t d_io_bytes = 0;
   cudaStream_t stream = nullptr;
+  // host-pointer apply of the one-CTA-per-row kernels: rows in contiguous chunks (each chunk's
+  // rows longest first), so a chunk's y copies back while later chunks compute
+  static constexpr int kHostChunks = 4;
+  std::vector<int> hc_start;             // [chunks+1] row ranges
+  int* d_hc_perm = nullptr;              // [N] rows of each range, longest first
+  cudaStream_t cstream[2] = {nullptr, nullptr};
+  cudaEvent_t ev_in[kHostChunks] = {}, ev_done[kHostChunks] = {}, ev_out[2] = {};
 };

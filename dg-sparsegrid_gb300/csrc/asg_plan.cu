@@ -83,6 +83,15 @@ void free_device(asg_plan* p) {
   cudaFree(p->d_err);
   cudaFree(p->d_io);
   if (p->stream) cudaStreamDestroy(p->stream);
+  cudaFree(p->d_hc_perm);
+  for (int k = 0; k < 2; ++k) {
+    if (p->cstream[k]) cudaStreamDestroy(p->cstream[k]);
+    if (p->ev_out[k]) cudaEventDestroy(p->ev_out[k]);
+  }
+  for (int k = 0; k < asg_plan::kHostChunks; ++k) {
+    if (p->ev_in[k]) cudaEventDestroy(p->ev_in[k]);
+    if (p->ev_done[k]) cudaEventDestroy(p->ev_done[k]);
+  }
 }
 
 // Pack operator (t,m) into block-major order: block (a,b) holds the P x P sub-matrix
@@ -578,6 +587,15 @@ asg_status check_ptr(const void* ptr, const char* name) {
   return ASG_OK;
 }
 
+// The kernel family a precision runs: the tuned choice when asg_plan_tune made one, else the
+// plan's kind (whose FP64 side is kind 3 for the streaming kernel).
+template <typename T>
+int effective_kind(const asg_plan* p) {
+  const int t = p->tuned_kind[sizeof(T) == 4 ? 1 : 0];
+  const int k = t >= 0 ? t : p->kernel_kind;
+  return (k == KK_STREAM && sizeof(T) == 8) ? KK_SINGLE_TMA : k;
+}
+
 template <typename T>
 asg_status apply_dev(asg_plan* p, const T* f, T* y, void* stream) {
   if (!p) return fail(ASG_ERR_INVALID, "apply: NULL plan");
@@ -586,7 +604,8 @@ asg_status apply_dev(asg_plan* p, const T* f, T* y, void* stream) {
   st = check_ptr(y, "y");
   if (st) return st;
   if (f == y) return fail(ASG_ERR_INVALID, "apply: f and y must not alias");
-  if (p->kernel_kind == KK_STREAM && sizeof(T) == 4) {
+  const int kind = effective_kind<T>(p);
+  if (kind == KK_STREAM && sizeof(T) == 4) {
     StreamArgs sa{};
     sa.f = reinterpret_cast<const float*>(f);
     sa.y = reinterpret_cast<float*>(y);
@@ -601,10 +620,42 @@ asg_status apply_dev(asg_plan* p, const T* f, T* y, void* stream) {
   }
   const T* ops = sizeof(T) == 8 ? reinterpret_cast<const T*>(p->d_ops64) : reinterpret_cast<const T*>(p->d_ops32);
   ApplyArgs<T> a = make_args<T>(p, f, y, ops);
-  // the streaming kernel is FP32 only: FP64 runs the bulk-copy pipeline of kind 3
-  const int kind = p->kernel_kind == KK_STREAM ? KK_SINGLE_TMA : p->kernel_kind;
   cudaError_t e = launch_apply<T>(a, p->P, kind, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "apply kernel launch");
+  return ASG_OK;
+}
+
+// Row chunks of the host-pointer apply: kHostChunks contiguous ranges of about equal work,
+// each range's rows longest first (the one-CTA-per-row kernels launch a range as a row list).
+asg_status host_chunks(asg_plan* p) {
+  if (!p->hc_start.empty()) return ASG_OK;
+  const int N = p->N, K = asg_plan::kHostChunks;
+  const long long total = p->row_ptr[N];
+  std::vector<int> start(1, 0);
+  for (int c = 1; c < K; ++c) {
+    const long long target = total * c / K;
+    int r = start.back();
+    while (r < N && p->row_ptr[r] < target) ++r;
+    start.push_back(std::max(r, start.back()));
+  }
+  start.push_back(N);
+  std::vector<int> perm(N);
+  for (int i = 0; i < N; ++i) perm[i] = i;
+  for (int c = 0; c < K; ++c)
+    std::stable_sort(perm.begin() + start[c], perm.begin() + start[c + 1], [&](int x, int y) {
+      return p->row_ptr[x + 1] - p->row_ptr[x] > p->row_ptr[y + 1] - p->row_ptr[y];
+    });
+  asg_status st = upload(&p->d_hc_perm, perm);
+  if (st) return st;
+  for (int k = 0; k < 2; ++k) {
+    ASG_CUDA(cudaStreamCreateWithFlags(&p->cstream[k], cudaStreamNonBlocking));
+    ASG_CUDA(cudaEventCreateWithFlags(&p->ev_out[k], cudaEventDisableTiming));
+  }
+  for (int k = 0; k < K; ++k) {
+    ASG_CUDA(cudaEventCreateWithFlags(&p->ev_in[k], cudaEventDisableTiming));
+    ASG_CUDA(cudaEventCreateWithFlags(&p->ev_done[k], cudaEventDisableTiming));
+  }
+  p->hc_start = start;
   return ASG_OK;
 }
 
@@ -624,6 +675,40 @@ asg_status apply_host(asg_plan* p, const T* hf, T* hy) {
   }
   T* df = static_cast<T*>(p->d_io);
   T* dy = reinterpret_cast<T*>(reinterpret_cast<char*>(p->d_io) + ((n * sizeof(T) + 255) / 256) * 256);
+  // the one-CTA-per-row bulk-copy kernels run as row-chunk launches: f comes in over two copy
+  // streams, every chunk's y goes back (on the copy streams) while the next chunks compute
+  const int kind = effective_kind<T>(p);
+  const int K = asg_plan::kHostChunks;
+  if ((kind == KK_SINGLE_TMA || kind == KK_SINGLE_TMA3) && p->N >= 4 * K) {
+    asg_status st = host_chunks(p);
+    if (st) return st;
+    for (int c = 0; c < K; ++c) {  // f in K pieces, alternating copy streams
+      const size_t e0 = n * c / K, e1 = n * (c + 1) / K;
+      ASG_CUDA(cudaMemcpyAsync(df + e0, hf + e0, (e1 - e0) * sizeof(T), cudaMemcpyHostToDevice, p->cstream[c & 1]));
+      ASG_CUDA(cudaEventRecord(p->ev_in[c], p->cstream[c & 1]));
+    }
+    for (int c = 0; c < K; ++c) ASG_CUDA(cudaStreamWaitEvent(p->stream, p->ev_in[c], 0));
+    const T* ops = sizeof(T) == 8 ? reinterpret_cast<const T*>(p->d_ops64) : reinterpret_cast<const T*>(p->d_ops32);
+    for (int c = 0; c < K; ++c) {
+      const int r0 = p->hc_start[c], r1 = p->hc_start[c + 1];
+      if (r1 > r0) {
+        ApplyArgs<T> a = make_args<T>(p, df, dy, ops);
+        a.N = r1 - r0;  // one CTA per listed row
+        a.row_order = p->d_hc_perm + r0;
+        cudaError_t e = launch_apply<T>(a, p->P, kind, p->stream);
+        if (e != cudaSuccess) return cuda_fail(e, "apply kernel launch");
+      }
+      ASG_CUDA(cudaEventRecord(p->ev_done[c], p->stream));
+      cudaStream_t cs = p->cstream[c & 1];
+      ASG_CUDA(cudaStreamWaitEvent(cs, p->ev_done[c], 0));
+      const size_t e0 = static_cast<size_t>(r0) * p->B, e1 = static_cast<size_t>(r1) * p->B;
+      if (e1 > e0) ASG_CUDA(cudaMemcpyAsync(hy + e0, dy + e0, (e1 - e0) * sizeof(T), cudaMemcpyDeviceToHost, cs));
+    }
+    for (int k = 0; k < 2; ++k) ASG_CUDA(cudaEventRecord(p->ev_out[k], p->cstream[k]));
+    for (int k = 0; k < 2; ++k) ASG_CUDA(cudaEventSynchronize(p->ev_out[k]));
+    ASG_CUDA(cudaStreamSynchronize(p->stream));
+    return ASG_OK;
+  }
   ASG_CUDA(cudaMemcpyAsync(df, hf, n * sizeof(T), cudaMemcpyHostToDevice, p->stream));
   asg_status st = apply_dev<T>(p, df, dy, p->stream);
   if (st) return st;
@@ -647,6 +732,76 @@ template bool small_plan_args<double>(const asg_plan*, ApplyArgs<double>*);
 }  // namespace asg
 
 using asg::fail;
+
+
+namespace asg_tune {
+// The kernel families asg_plan_set_kernel accepts for this plan.
+std::vector<int> candidate_kinds(asg_plan* p) {
+  std::vector<int> out;
+  const int saved = p->kernel_kind;
+  const int t0 = p->tuned_kind[0], t1 = p->tuned_kind[1];
+  for (int k = 0; k <= 7; ++k) {
+    if (asg_plan_set_kernel(p, k) == ASG_OK) out.push_back(k);
+  }
+  p->kernel_kind = saved;
+  p->tuned_kind[0] = t0;
+  p->tuned_kind[1] = t1;
+  asg::fail(ASG_OK, "");  // the refusals above are not this call's error
+  return out;
+}
+
+template <typename T>
+asg_status tune_plan(asg_plan* p, cudaStream_t s, int* best_kind, float* best_ms, float* default_ms) {
+  const size_t n = static_cast<size_t>(p->N) * p->B;
+  T* buf = nullptr;
+  ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&buf), 2 * n * sizeof(T) + 256));
+  T* f = buf;
+  T* y = reinterpret_cast<T*>(reinterpret_cast<char*>(buf) + ((n * sizeof(T) + 255) / 256) * 256);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  asg_status st = ASG_OK;
+  cudaError_t ce = cudaMemsetAsync(f, 0, n * sizeof(T), s);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e0);
+  if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+  if (ce != cudaSuccess) st = asg::cuda_fail(ce, "plan_tune: setup");
+  const int prec = sizeof(T) == 4 ? 1 : 0;
+  const int def = asg::effective_kind<T>(p);
+  std::vector<int> kinds = st ? std::vector<int>() : candidate_kinds(p);
+  float best = 0.f, at_def = 0.f;
+  int arg = def;
+  for (int k : kinds) {
+    p->tuned_kind[prec] = k;
+    if (asg::effective_kind<T>(p) != k) continue;  // an FP32-only family in FP64
+    constexpr int kReps = 10;
+    for (int r = 0; r < 2 && !st; ++r) st = asg::apply_dev<T>(p, f, y, s);
+    if (!st && (ce = cudaEventRecord(e0, s)) != cudaSuccess) st = asg::cuda_fail(ce, "plan_tune");
+    for (int r = 0; r < kReps && !st; ++r) st = asg::apply_dev<T>(p, f, y, s);
+    if (!st && (ce = cudaEventRecord(e1, s)) != cudaSuccess) st = asg::cuda_fail(ce, "plan_tune");
+    if (!st && (ce = cudaEventSynchronize(e1)) != cudaSuccess) st = asg::cuda_fail(ce, "plan_tune");
+    float ms = 0.f;
+    if (!st && (ce = cudaEventElapsedTime(&ms, e0, e1)) != cudaSuccess) st = asg::cuda_fail(ce, "plan_tune");
+    if (st) break;
+    ms /= kReps;
+    if (k == def) at_def = ms;
+    if (best == 0.f || ms < best) {
+      best = ms;
+      arg = k;
+    }
+  }
+  p->tuned_kind[prec] = st ? -1 : arg;
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(buf);
+  if (st) return st;
+  int dev_status = 0;
+  if ((st = asg_plan_device_status(p, &dev_status))) return st;
+  if (dev_status != ASG_OK) return fail(dev_status, "plan_tune: a kernel reported a device-side timeout");
+  if (best_kind) *best_kind = arg;
+  if (best_ms) *best_ms = best;
+  if (default_ms) *default_ms = at_def;
+  return ASG_OK;
+}
+
+}  // namespace asg_tune
 
 extern "C" {
 
@@ -911,6 +1066,21 @@ asg_status asg_plan_set_kernel(asg_plan* p, int kind) {
   }
   if (kind < 0 || kind > 7) return fail(ASG_ERR_INVALID, "unknown kernel kind %d", kind);
   p->kernel_kind = kind;
+  p->tuned_kind[0] = p->tuned_kind[1] = -1;
+  return ASG_OK;
+}
+
+asg_status asg_plan_tune(asg_plan* p, int precision, void* stream, int* best_kind, float* best_ms, float* default_ms) {
+  if (!p) return fail(ASG_ERR_INVALID, "plan_tune: NULL plan");
+  if (precision != 0 && precision != 1) return fail(ASG_ERR_INVALID, "plan_tune: precision=%d", precision);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  return precision ? asg_tune::tune_plan<float>(p, s, best_kind, best_ms, default_ms)
+                   : asg_tune::tune_plan<double>(p, s, best_kind, best_ms, default_ms);
+}
+
+asg_status asg_plan_kernel_for(const asg_plan* p, int precision, int* kind) {
+  if (!p || !kind || (precision != 0 && precision != 1)) return fail(ASG_ERR_INVALID, "plan_kernel_for: bad argument");
+  *kind = precision ? asg::effective_kind<float>(p) : asg::effective_kind<double>(p);
   return ASG_OK;
 }
 

@@ -110,6 +110,17 @@ asg_status asg_plan_update_ops(asg_plan* plan, const double* const* ops, const i
  * The default is chosen by asg_plan_create; this exists for testing one family against
  * another and for launch-shape tuning. */
 asg_status asg_plan_set_kernel(asg_plan* plan, int kind);
+/* Autotuner (no reference counterpart): times every kernel family asg_plan_set_kernel accepts
+ * for this plan -- they differ in tile mapping, stages, CTAs per SM and rows per CTA -- on the
+ * plan's own shape in one precision (0 FP64, 1 FP32), 2 warm-up and 10 timed launches each
+ * on scratch vectors it allocates, and keeps the fastest for that precision (the plan's
+ * applies in that precision use it from then on; asg_plan_set_kernel clears the choice).
+ * Outputs (each may be NULL): the chosen kind, its time and the time of the kind used before,
+ * in ms per launch.  Synchronous. */
+asg_status asg_plan_tune(asg_plan* plan, int precision, void* stream, int* best_kind, float* best_ms,
+                         float* default_ms);
+/* The kernel family applies in this precision (0 FP64, 1 FP32) run. */
+asg_status asg_plan_kernel_for(const asg_plan* plan, int precision, int* kind);
 /* Synchronises and reads the plan's device status word: ASG_OK, or ASG_ERR_TIMEOUT when a
  * kernel's bounded shared-memory pipeline wait gave up (the y it wrote is then undefined).
  * The word is cleared after reading.  No reference counterpart: device-side waits are new. */

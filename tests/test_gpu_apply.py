@@ -269,3 +269,47 @@ def test_argument_errors(dev):
     small = [[m[:4, :4] for m in row] for row in mats]
     with pytest.raises(AsgError, match="ld="):
         _plan(small, idx, 2)
+
+
+@pytest.mark.parametrize("lev", [2, 3])
+def test_host_path_row_chunks_bitwise(dev, lev):
+    """The host-pointer apply of the bulk-copy kernels runs in row chunks (f in over two copy
+    streams, each chunk's y back while later chunks compute): bitwise the device apply, FP64 and
+    FP32, so the rows of every chunk are computed and copied back."""
+    pde, table, idx, mats = problem("continuity6", lev, 4)
+    p = _plan(mats, idx, 4, structure="detect")
+    f = np.random.default_rng(11).standard_normal(idx.shape[0] * 4096)
+    for dtype, npd in ((torch.float64, np.float64), (torch.float32, np.float32)):
+        y_dev = _apply(p, f, dev, dtype)
+        y_host = p.apply_host(f.astype(npd))
+        assert np.array_equal(y_host.astype(np.float64), y_dev)
+        assert np.array_equal(p.apply_host(f.astype(npd)), y_host)
+    p.close()
+
+
+@pytest.mark.parametrize("name,lev,deg", [("continuity6", 3, 4), ("continuity3", 4, 3), ("continuity2", 4, 2)])
+def test_tuner_choice_matches_default(dev, name, lev, deg):
+    """asg_plan_tune times the kernel families of the plan per precision and keeps the fastest:
+    the tuned plan's results equal the default's within the precision's tolerance (FP64 against
+    the oracle's rows as well), and set_kernel clears the choice."""
+    import asgkron
+
+    pde, table, idx, mats = problem(name, lev, deg)
+    N = idx.shape[0]
+    B = deg ** idx.shape[1]
+    f = np.random.default_rng(3).standard_normal(N * B)
+    p = _plan(mats, idx, deg)
+    y64, y32 = _apply(p, f, dev), _apply(p, f, dev, torch.float32)
+    default = p.stats()["kernel_kind"]
+    for dtype in (torch.float64, torch.float32):
+        r = p.tune(dtype)
+        assert r["ms"] > 0 and r["ms"] <= r["default_ms"] * 1.0001 and p.kernel_for(dtype) == r["kind"]
+    assert p.device_status() == 0
+    t64, t32 = _apply(p, f, dev), _apply(p, f, dev, torch.float32)
+    assert rel2(t64, y64) <= FP64_TOL and rel2(t32, y32) <= FP32_TOL and rel2(t32, t64) <= FP32_TOL
+    rows = np.arange(0, N, max(1, N // 5))
+    want = O.apply_A_rows(mats, idx.astype(np.int64), deg, f, rows=rows)
+    assert rel2(t64.reshape(N, B)[rows].ravel(), want) <= FP64_TOL
+    p.set_kernel(default)
+    assert p.kernel_for(torch.float64) in (default, asgkron._lib.KERNEL_SINGLE_TMA)
+    p.close()

@@ -139,3 +139,45 @@ def test_batch_rejects_large_blocks(dev):
     p = asgkron.Plan.create(mats, idx, 4)
     with pytest.raises(AsgError, match="deg\\^d=4096"):
         Batch([p])
+
+
+def test_batch_levels_6_7_vs_oracle(dev):
+    """The batched configuration's own draw (seed 3, levels 3..7): its first level-6 and first
+    level-7 problem in one FP32 persistent launch, sampled rows against the C restatement of
+    the reference loop (apply_A.m:102-236, all pairs, FP64)."""
+    import asgkron
+    from asgkron.batch import Batch
+    from oracle import cref
+
+    rng = np.random.default_rng(3)
+    picked = {}
+    for _ in range(256):  # the generator's order: d, level, degree, operators, f
+        d = int(rng.choice([2, 3, 4]))
+        lev = int(rng.integers(3, 8))
+        deg = int(rng.integers(2, 5))
+        table = asgkron.hash_table_sparse_nD([lev] * d, 8)
+        n = deg * 2 ** lev
+        mats = [[rng.normal(0.0, 1.0 / np.sqrt(deg), (n, n)) for _ in range(d)] for _ in range(d)]
+        f = rng.standard_normal(table.num_elems * deg ** d)
+        if lev in (6, 7) and lev not in picked:
+            picked[lev] = (table.idx1d(), mats, deg, f)
+        if len(picked) == 2:
+            break
+    assert sorted(picked) == [6, 7]
+    probs = [picked[6], picked[7]]
+    plans = [asgkron.Plan.create(m, idx, deg, structure="none") for idx, m, deg, _ in probs]
+    fs = [torch.from_numpy(f).to(dev).float() for *_, f in probs]
+    ys = [torch.empty_like(f) for f in fs]
+    b = Batch(plans)
+    b.set_io(fs, ys)
+    b.apply()
+    torch.cuda.synchronize()
+    for (idx, mats, deg, f), y in zip(probs, ys):
+        N = idx.shape[0]
+        rows = np.array([0, N // 3, N - 1], dtype=np.int32)
+        want = cref.apply_rows(mats, idx, deg, f, rows=rows)
+        got = y.double().cpu().numpy().reshape(N, -1)[rows].ravel()
+        assert rel2(got, want) <= 1e-6, (N, deg)
+    b.close()
+    for p in plans:
+        p.close()
