@@ -665,6 +665,68 @@ def run_implicit(args, rank, local):
     print(json.dumps(line), flush=True)
 
 
+def gather_stream(plan, f32, flush, stream, steps=50):
+    """The L2-to-SM rate of the plan's own gather pattern: every work entry's column block
+    streamed into shared memory with the apply's bulk copies and no arithmetic
+    (asg_probe_gather_f32), L2 flushed before each launch as for the apply.  Best stage count."""
+    import ctypes as C
+
+    import torch
+    from asgkron._lib import check, lib
+
+    out = torch.empty(plan.N, dtype=torch.float32, device=f32.device)
+    st = plan.stats()
+    gbytes = st["num_entries"] * plan.B * 4
+    res = {}
+    for stages in (2, 4, 8):
+        def launch():
+            check(lib().asg_probe_gather_f32(plan.handle, C.c_void_p(f32.data_ptr()), C.c_void_p(out.data_ptr()),
+                                             stages, C.c_void_p(stream.cuda_stream)))
+        for _ in range(3):
+            flush()
+            launch()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for s, e in ev:
+            flush()
+            s.record(stream)
+            launch()
+            e.record(stream)
+        torch.cuda.synchronize()
+        ms = sum(s.elapsed_time(e) for s, e in ev) / steps
+        res["stages_%d" % stages] = {"ms": ms, "gbs": gbytes / (ms * 1e-3) / 1e9}
+    best = min(res.values(), key=lambda r: r["ms"])
+    return {"gather_bytes_per_launch": gbytes, "ms": best["ms"], "gbs": best["gbs"], "by_stages": res}
+
+
+def fma_peaks(dev, stream):
+    """FP32 paired-FMA and FP64 FMA issue peaks of this GPU (asg_probe_fma: 152 x 8 CTAs of 256
+    threads, 8 independent chains each), TFLOP/s."""
+    import ctypes as C
+
+    import torch
+    from asgkron._lib import check, lib
+
+    out = torch.zeros(2, dtype=torch.float64, device=dev)
+    nsm = torch.cuda.get_device_properties(dev).multi_processor_count
+    res = {}
+    for prec, name, iters in ((1, "fp32_ffma2_tflops", 40000), (0, "fp64_dfma_tflops", 4000)):
+        flops = C.c_double(0)
+        def launch():
+            check(lib().asg_probe_fma(prec, nsm * 8, iters, C.c_void_p(out.data_ptr()), C.byref(flops),
+                                      C.c_void_p(stream.cuda_stream)))
+        launch()
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        for _ in range(3):
+            launch()
+        e.record(stream)
+        torch.cuda.synchronize()
+        res[name] = 3 * flops.value / (s.elapsed_time(e) * 1e-3) / 1e12
+    return res
+
+
 def graph_replay(plan, f, y, stream, n_apply=100, reps=10):
     """n_apply back-to-back applies captured in one CUDA graph (no flush between them: the
     operands stay in L2), replayed reps times; returns microseconds per apply."""
@@ -833,6 +895,35 @@ def main():
         variants["implicit_diffusion2_lev8_deg4"] = implicit_steps(dev)
         variants["precision_continuity3_lev6_deg3"] = precision_continuity3(dev, flush, stream)
         variants["batched_256_lev3_7"] = batched_measure(dev, 256, 7, max(1, min(args.steps, 5)), 3)
+        # the roofline denominators measured here: the plan's gather pattern and the FMA pipes
+        gs = gather_stream(plan, f32, flush, stream)
+        gs["apply_frac_of_gather_stream"] = gs["ms"] / apply_ms
+        variants["gather_stream"] = gs
+        peaks = fma_peaks(dev, stream)
+        rw = variants["fp32_reference_work_model"]
+        peaks["fp32_reference_work_model_frac"] = rw["gflops_per_s"] / 1e3 / peaks["fp32_ffma2_tflops"]
+        f64_flops = st["flops_executed"] / (fp64_ms * 1e-3) / 1e12
+        peaks["fp64_structured_tflops"] = f64_flops
+        peaks["fp64_structured_frac"] = f64_flops / peaks["fp64_dfma_tflops"]
+        variants["fma_peaks"] = peaks
+        # the autotuner on the headline plan (per precision; then back to the default)
+        variants["tuner"] = {"fp32": plan.tune("float32"), "fp64": plan.tune("float64")}
+        plan.set_kernel(st["kernel_kind"])
+        # end to end through the FP64 host-pointer call (what the MATLAB gateway makes)
+        f64h = np.ascontiguousarray(f64_h)
+        y64h = np.empty_like(f64h)
+        for _ in range(3):
+            plan.apply_host(f64h, y64h)
+        tot64 = 0.0
+        for _ in range(max(5, min(args.steps, 100))):
+            flush()
+            torch.cuda.synchronize()
+            t_a = time.perf_counter()
+            plan.apply_host(f64h, y64h)
+            tot64 += time.perf_counter() - t_a
+        e64 = tot64 / max(5, min(args.steps, 100)) * 1e3
+        variants["e2e_fp64_host"] = {"ms_per_step": e64, "value": dof / (e64 * 1e-3) / 1e9,
+                                     "h2d_bytes_per_step": 8 * dof, "d2h_bytes_per_step": 8 * dof}
 
     # ---- roofline ------------------------------------------------------------------------
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")

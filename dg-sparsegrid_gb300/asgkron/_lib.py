@@ -111,6 +111,8 @@ SIGNATURES = {
     "asg_plan_tune": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_float),
                                 C.POINTER(C.c_float)]),
     "asg_plan_kernel_for": (C.c_int, [C.c_void_p, C.c_int, C.POINTER(C.c_int)]),
+    "asg_probe_gather_f32": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p]),
+    "asg_probe_fma": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_double), C.c_void_p]),
     "asg_plan_active": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint)]),
     "asg_plan_device_status": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "asg_apply_f64": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -168,6 +168,18 @@ asg_status asg_grad_ops_host_f64(asg_plan* plan, const double* h_f, const double
 asg_status asg_assemble_bsr_f64(asg_plan* plan, long long* row_ptr, int* cols, double* d_blocks, long long capacity,
                                 long long* num_blocks, void* stream);
 
+/* Measurement kernels (no reference counterpart): what the roofline of the apply is taken
+ * against.  asg_probe_gather_f32 streams every work entry's column block of the plan from
+ * global memory into shared memory with the apply's bulk copies (one CTA per row, `stages`
+ * = 2, 4 or 8 blocks in flight, no arithmetic; one value per block summed into d_out[row],
+ * N floats): time it to get the L2-to-SM rate of the plan's own gather pattern.
+ * asg_probe_fma runs `blocks` x 256 threads of 8 independent FMA chains for `iters` rounds,
+ * precision 1 the FP32 paired FMA (fma.rn.f32x2), 0 FP64 (d_out: one value of that type),
+ * and reports the flops it executes: time it for the FP32 / FP64 issue peaks.  Both
+ * asynchronous on `stream`. */
+asg_status asg_probe_gather_f32(asg_plan* plan, const float* d_f, float* d_out, int stages, void* stream);
+asg_status asg_probe_fma(int precision, int blocks, int iters, void* d_out, double* flops, void* stream);
+
 /* ---------------------------------------------------------------------------------------
  * Element tables and index maps (hash_table_sparse_nD.m, global_matrix.m, connect_nD.m)
  * ------------------------------------------------------------------------------------- */
