@@ -221,11 +221,4 @@ struct asg_plan {
   void* d_io = nullptr;
   size_t d_io_bytes = 0;
   cudaStream_t stream = nullptr;
-  // host-pointer apply of the one-CTA-per-row kernels: rows in contiguous chunks (each chunk's
-  // rows longest first), so a chunk's y copies back while later chunks compute
-  static constexpr int kHostChunks = 4;
-  std::vector<int> hc_start;             // [chunks+1] row ranges
-  int* d_hc_perm = nullptr;              // [N] rows of each range, longest first
-  cudaStream_t cstream[2] = {nullptr, nullptr};
-  cudaEvent_t ev_in[kHostChunks] = {}, ev_done[kHostChunks] = {}, ev_out[2] = {};
 };

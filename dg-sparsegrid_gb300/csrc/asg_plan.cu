@@ -83,15 +83,7 @@ void free_device(asg_plan* p) {
   cudaFree(p->d_err);
   cudaFree(p->d_io);
   if (p->stream) cudaStreamDestroy(p->stream);
-  cudaFree(p->d_hc_perm);
-  for (int k = 0; k < 2; ++k) {
-    if (p->cstream[k]) cudaStreamDestroy(p->cstream[k]);
-    if (p->ev_out[k]) cudaEventDestroy(p->ev_out[k]);
-  }
-  for (int k = 0; k < asg_plan::kHostChunks; ++k) {
-    if (p->ev_in[k]) cudaEventDestroy(p->ev_in[k]);
-    if (p->ev_done[k]) cudaEventDestroy(p->ev_done[k]);
-  }
+
 }
 
 // Pack operator (t,m) into block-major order: block (a,b) holds the P x P sub-matrix
@@ -625,40 +617,6 @@ asg_status apply_dev(asg_plan* p, const T* f, T* y, void* stream) {
   return ASG_OK;
 }
 
-// Row chunks of the host-pointer apply: kHostChunks contiguous ranges of about equal work,
-// each range's rows longest first (the one-CTA-per-row kernels launch a range as a row list).
-asg_status host_chunks(asg_plan* p) {
-  if (!p->hc_start.empty()) return ASG_OK;
-  const int N = p->N, K = asg_plan::kHostChunks;
-  const long long total = p->row_ptr[N];
-  std::vector<int> start(1, 0);
-  for (int c = 1; c < K; ++c) {
-    const long long target = total * c / K;
-    int r = start.back();
-    while (r < N && p->row_ptr[r] < target) ++r;
-    start.push_back(std::max(r, start.back()));
-  }
-  start.push_back(N);
-  std::vector<int> perm(N);
-  for (int i = 0; i < N; ++i) perm[i] = i;
-  for (int c = 0; c < K; ++c)
-    std::stable_sort(perm.begin() + start[c], perm.begin() + start[c + 1], [&](int x, int y) {
-      return p->row_ptr[x + 1] - p->row_ptr[x] > p->row_ptr[y + 1] - p->row_ptr[y];
-    });
-  asg_status st = upload(&p->d_hc_perm, perm);
-  if (st) return st;
-  for (int k = 0; k < 2; ++k) {
-    ASG_CUDA(cudaStreamCreateWithFlags(&p->cstream[k], cudaStreamNonBlocking));
-    ASG_CUDA(cudaEventCreateWithFlags(&p->ev_out[k], cudaEventDisableTiming));
-  }
-  for (int k = 0; k < K; ++k) {
-    ASG_CUDA(cudaEventCreateWithFlags(&p->ev_in[k], cudaEventDisableTiming));
-    ASG_CUDA(cudaEventCreateWithFlags(&p->ev_done[k], cudaEventDisableTiming));
-  }
-  p->hc_start = start;
-  return ASG_OK;
-}
-
 template <typename T>
 asg_status apply_host(asg_plan* p, const T* hf, T* hy) {
   if (!p) return fail(ASG_ERR_INVALID, "apply_host: NULL plan");
@@ -675,40 +633,6 @@ asg_status apply_host(asg_plan* p, const T* hf, T* hy) {
   }
   T* df = static_cast<T*>(p->d_io);
   T* dy = reinterpret_cast<T*>(reinterpret_cast<char*>(p->d_io) + ((n * sizeof(T) + 255) / 256) * 256);
-  // the one-CTA-per-row bulk-copy kernels run as row-chunk launches: f comes in over two copy
-  // streams, every chunk's y goes back (on the copy streams) while the next chunks compute
-  const int kind = effective_kind<T>(p);
-  const int K = asg_plan::kHostChunks;
-  if ((kind == KK_SINGLE_TMA || kind == KK_SINGLE_TMA3) && p->N >= 4 * K) {
-    asg_status st = host_chunks(p);
-    if (st) return st;
-    for (int c = 0; c < K; ++c) {  // f in K pieces, alternating copy streams
-      const size_t e0 = n * c / K, e1 = n * (c + 1) / K;
-      ASG_CUDA(cudaMemcpyAsync(df + e0, hf + e0, (e1 - e0) * sizeof(T), cudaMemcpyHostToDevice, p->cstream[c & 1]));
-      ASG_CUDA(cudaEventRecord(p->ev_in[c], p->cstream[c & 1]));
-    }
-    for (int c = 0; c < K; ++c) ASG_CUDA(cudaStreamWaitEvent(p->stream, p->ev_in[c], 0));
-    const T* ops = sizeof(T) == 8 ? reinterpret_cast<const T*>(p->d_ops64) : reinterpret_cast<const T*>(p->d_ops32);
-    for (int c = 0; c < K; ++c) {
-      const int r0 = p->hc_start[c], r1 = p->hc_start[c + 1];
-      if (r1 > r0) {
-        ApplyArgs<T> a = make_args<T>(p, df, dy, ops);
-        a.N = r1 - r0;  // one CTA per listed row
-        a.row_order = p->d_hc_perm + r0;
-        cudaError_t e = launch_apply<T>(a, p->P, kind, p->stream);
-        if (e != cudaSuccess) return cuda_fail(e, "apply kernel launch");
-      }
-      ASG_CUDA(cudaEventRecord(p->ev_done[c], p->stream));
-      cudaStream_t cs = p->cstream[c & 1];
-      ASG_CUDA(cudaStreamWaitEvent(cs, p->ev_done[c], 0));
-      const size_t e0 = static_cast<size_t>(r0) * p->B, e1 = static_cast<size_t>(r1) * p->B;
-      if (e1 > e0) ASG_CUDA(cudaMemcpyAsync(hy + e0, dy + e0, (e1 - e0) * sizeof(T), cudaMemcpyDeviceToHost, cs));
-    }
-    for (int k = 0; k < 2; ++k) ASG_CUDA(cudaEventRecord(p->ev_out[k], p->cstream[k]));
-    for (int k = 0; k < 2; ++k) ASG_CUDA(cudaEventSynchronize(p->ev_out[k]));
-    ASG_CUDA(cudaStreamSynchronize(p->stream));
-    return ASG_OK;
-  }
   ASG_CUDA(cudaMemcpyAsync(df, hf, n * sizeof(T), cudaMemcpyHostToDevice, p->stream));
   asg_status st = apply_dev<T>(p, df, dy, p->stream);
   if (st) return st;

@@ -271,22 +271,6 @@ def test_argument_errors(dev):
         _plan(small, idx, 2)
 
 
-@pytest.mark.parametrize("lev", [2, 3])
-def test_host_path_row_chunks_bitwise(dev, lev):
-    """The host-pointer apply of the bulk-copy kernels runs in row chunks (f in over two copy
-    streams, each chunk's y back while later chunks compute): bitwise the device apply, FP64 and
-    FP32, so the rows of every chunk are computed and copied back."""
-    pde, table, idx, mats = problem("continuity6", lev, 4)
-    p = _plan(mats, idx, 4, structure="detect")
-    f = np.random.default_rng(11).standard_normal(idx.shape[0] * 4096)
-    for dtype, npd in ((torch.float64, np.float64), (torch.float32, np.float32)):
-        y_dev = _apply(p, f, dev, dtype)
-        y_host = p.apply_host(f.astype(npd))
-        assert np.array_equal(y_host.astype(np.float64), y_dev)
-        assert np.array_equal(p.apply_host(f.astype(npd)), y_host)
-    p.close()
-
-
 @pytest.mark.parametrize("name,lev,deg", [("continuity6", 3, 4), ("continuity3", 4, 3), ("continuity2", 4, 2)])
 def test_tuner_choice_matches_default(dev, name, lev, deg):
     """asg_plan_tune times the kernel families of the plan per precision and keeps the fastest:
