@@ -597,11 +597,13 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
         consumer_sync();
         T* scr = stages + pend * SST;
 #pragma unroll
-        for (int r = 0; r < P; ++r) {
+        for (int i = 0; i < P; ++i) {
           if constexpr (F32) {
-            *reinterpret_cast<float4*>(scr + base_g + r * s_g) =
-                pt_row(g32, r, false);
+            // rows of a group on dimension d-2 in a per-thread rotated order (bank-conflict free)
+            const int r = (i + (cur_m == D - 2 ? (tid >> 1) & 3 : 0)) & 3;
+            *reinterpret_cast<float4*>(scr + base_g + r * s_g) = pt_row_sel(g32, r);
           } else {
+            const int r = i;
             Row<T, P> rr;
 #pragma unroll
             for (int c = 0; c < P; ++c) rr.v[c] = g[r][c];
@@ -651,7 +653,8 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
       if (m == D - 1)
         pt_cols(g32, reinterpret_cast<const float*>(sp + B), reinterpret_cast<const float*>(sp + base_g), s_g);
       else
-        pt_rows(g32, reinterpret_cast<const float*>(sp + B), reinterpret_cast<const float*>(sp + base_g), s_g);
+        pt_rows_rot(g32, reinterpret_cast<const float*>(sp + B), reinterpret_cast<const float*>(sp + base_g), s_g,
+                    m == D - 2 ? (tid >> 1) & 3 : 0);
     } else {
       T A[P * P];
 #pragma unroll
@@ -823,11 +826,13 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma_rows(ApplyArgs<T> a) {
           consumer_sync();
           T* scr = stages + pend * SST;
 #pragma unroll
-          for (int r = 0; r < P; ++r) {
+          for (int i = 0; i < P; ++i) {
             if constexpr (F32) {
-              *reinterpret_cast<float4*>(scr + base_g + r * s_g) =
-                  pt_row(g32, r, false);
+              // rows of a group on dimension d-2 in a per-thread rotated order (bank-conflict free)
+              const int r = (i + (cur_m == D - 2 ? (tid >> 1) & 3 : 0)) & 3;
+              *reinterpret_cast<float4*>(scr + base_g + r * s_g) = pt_row_sel(g32, r);
             } else {
+              const int r = i;
               Row<T, P> rr;
 #pragma unroll
               for (int c = 0; c < P; ++c) rr.v[c] = gg[r][c];
@@ -878,7 +883,8 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma_rows(ApplyArgs<T> a) {
         if (m == D - 1)
           pt_cols(g32, reinterpret_cast<const float*>(sp + B), reinterpret_cast<const float*>(sp + base_g), s_g);
         else
-          pt_rows(g32, reinterpret_cast<const float*>(sp + B), reinterpret_cast<const float*>(sp + base_g), s_g);
+          pt_rows_rot(g32, reinterpret_cast<const float*>(sp + B), reinterpret_cast<const float*>(sp + base_g), s_g,
+                      m == D - 2 ? (tid >> 1) & 3 : 0);
       } else {
         T A[P * P];
 #pragma unroll

@@ -134,6 +134,22 @@ __device__ __forceinline__ void pt_rows(PairTile& g, const float* A, const float
     g.v[3][0] = ffma2(a01, dup(x.w), g.v[3][0]); g.v[3][1] = ffma2(a23, dup(x.w), g.v[3][1]);
   }
 }
+// pt_rows visiting the contraction index from `rot` (0..3) on: the same products summed in a
+// rotated order, so that threads whose tiles lie 64 bytes apart read different shared-memory
+// banks (the layout of a group on dimension d-2, where a thread's 16 values are contiguous)
+__device__ __forceinline__ void pt_rows_rot(PairTile& g, const float* A, const float* xs, int s, int rot) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int b = (i + rot) & 3;
+    const float4 x = *reinterpret_cast<const float4*>(xs + b * s);
+    const float4 q = *reinterpret_cast<const float4*>(A + 4 * b);
+    const float2 a01 = make_float2(q.x, q.y), a23 = make_float2(q.z, q.w);
+    g.v[0][0] = ffma2(a01, dup(x.x), g.v[0][0]); g.v[0][1] = ffma2(a23, dup(x.x), g.v[0][1]);
+    g.v[1][0] = ffma2(a01, dup(x.y), g.v[1][0]); g.v[1][1] = ffma2(a23, dup(x.y), g.v[1][1]);
+    g.v[2][0] = ffma2(a01, dup(x.z), g.v[2][0]); g.v[2][1] = ffma2(a23, dup(x.z), g.v[2][1]);
+    g.v[3][0] = ffma2(a01, dup(x.w), g.v[3][0]); g.v[3][1] = ffma2(a23, dup(x.w), g.v[3][1]);
+  }
+}
 // m == 5: y[r][a] += sum_b A[a][b] x[r][b]; x rows s apart (natural rows along dimension 3)
 __device__ __forceinline__ void pt_cols(PairTile& g, const float* A, const float* xs, int s) {
   float4 q[4];
@@ -157,6 +173,13 @@ __device__ __forceinline__ float4 pt_row(const PairTile& g, int r, bool cols) {
   const int p = r >> 1;
   return (r & 1) ? make_float4(g.v[0][p].y, g.v[1][p].y, g.v[2][p].y, g.v[3][p].y)
                  : make_float4(g.v[0][p].x, g.v[1][p].x, g.v[2][p].x, g.v[3][p].x);
+}
+
+// pt_row(g, r, false) for a row index known only at run time (selects, no local memory).
+__device__ __forceinline__ float4 pt_row_sel(const PairTile& g, int r) {
+  const float4 r0 = pt_row(g, 0, false), r1 = pt_row(g, 1, false), r2 = pt_row(g, 2, false),
+               r3 = pt_row(g, 3, false);
+  return r == 0 ? r0 : r == 1 ? r1 : r == 2 ? r2 : r3;
 }
 
 }  // namespace asg
