@@ -10,7 +10,8 @@ timed apply.
 
 Output: one JSON line (rank 0).  ``value`` is device-resident throughput of the FP32
 structured kernel; ``e2e`` is the same metric through the host-pointer C ABI call
-(asg_apply_host_f32: H2D of f from pinned memory, apply, D2H of y, synchronise);
+(asg_apply_host_f32: H2D of f from pinned memory, apply, synchronise; y is pinned, so the
+kernel stores it over the host link as rows finish instead of a D2H copy after the apply);
 ``roofline`` uses the compulsory-bytes model of the path; ``cpu_baseline`` times the C
 restatement of the reference loop on a bounded row sample on the host cores.
 ``--impl reference`` times that CPU implementation alone (the reference is MATLAB and

@@ -23,9 +23,9 @@ ASG_STRUCT_DETECT = 1
 ASG_GRID_SG = 0
 ASG_GRID_FG = 1
 KERNEL_CHAIN_WARP, KERNEL_CHAIN_CTA, KERNEL_SINGLE_MODE, KERNEL_SINGLE_TMA, KERNEL_SINGLE_TMA3 = 0, 1, 2, 3, 4
-KERNEL_SINGLE_TMA_ROWS, KERNEL_SINGLE_SMALL, KERNEL_STREAM = 5, 6, 7
+KERNEL_SINGLE_TMA_ROWS, KERNEL_SINGLE_SMALL, KERNEL_STREAM, KERNEL_SINGLE_TMA_X2 = 5, 6, 7, 8
 KERNEL_NAMES = ["warp_chain", "cta_chain", "single_mode", "single_mode_tma", "single_mode_tma_3cta", "single_mode_tma_rows",
-                "single_mode_small", "stream"]
+                "single_mode_small", "stream", "single_mode_tma_x2"]
 
 
 class AsgError(RuntimeError):

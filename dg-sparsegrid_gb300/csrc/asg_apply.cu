@@ -687,6 +687,189 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
   }
 }
 
+// k_single_tma in FP32 with two output tiles per consumer thread: 4 consumer warps (128
+// threads) and one producer warp.  Consumer thread t owns the tiles kind-3 threads t and t+128
+// own, so every output value sees kind 3's operations in kind 3's order (the results are
+// bitwise those of kind 3).  Per entry, the stage wait, the descriptor broadcast, the stage
+// release and the operator block's shared loads are paid once for two tiles, and a term
+// group's transpose synchronises 128 threads instead of 256.
+__device__ __forceinline__ void consumer_sync_x2() { asm volatile("bar.sync 1, 128;" ::: "memory"); }
+
+template <int S, int MINB>
+__global__ void __launch_bounds__(160, MINB) k_single_tma_x2(ApplyArgs<float> a) {
+  constexpr int P = 4, AB = 16, NCW = 4, NT = 2, HALF = 32 * NCW;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int s_abort;
+  const int tid = threadIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int B = a.B, D = a.D;
+  const int SST = B + AB;
+  float* stages = reinterpret_cast<float*>(smem_raw);
+  uint64_t* full = reinterpret_cast<uint64_t*>(stages + S * SST);
+  uint64_t* empty = full + S;
+  const int row = a.row_order ? a.row_order[blockIdx.x] : blockIdx.x;
+  const long long q0 = a.row_ptr[row];
+  const int n = static_cast<int>(a.row_ptr[row + 1] - q0);
+  const EntryDesc* ed = a.ed + q0;
+  const uint32_t fbytes = static_cast<uint32_t>(B * sizeof(float)), abytes = AB * sizeof(float);
+
+  if (tid == 0) {
+    s_abort = 0;
+    for (int k = 0; k < S; ++k) {
+      mbar_init(&full[k], 1);
+      mbar_init(&empty[k], NCW);
+    }
+    mbar_fence_init();
+  }
+  __syncthreads();
+  volatile int* abort_flag = &s_abort;
+
+  if (warp == NCW) {
+    // ---------------- producer warp (as in k_single_tma) ----------------
+    int kdone = 0;
+    bool stop = false;
+    for (int k0 = 0; k0 < n && !stop; k0 += 32) {
+      EntryDesc mine{};
+      if (k0 + lane < n) mine = ed[k0 + lane];
+      const int cnt = min(32, n - k0);
+      for (int l = 0; l < cnt; ++l) {
+        const int j = __shfl_sync(0xffffffffu, mine.j, l);
+        const long long aoff = __shfl_sync(0xffffffffu, mine.aoff, l);
+        const int k = k0 + l;
+        const int st = k % S;
+        bool ok = true;
+        if (k >= S) ok = mbar_wait_bounded(&empty[st], static_cast<uint32_t>(((k / S) - 1) & 1));
+        if (!__all_sync(0xffffffffu, ok)) {
+          if (lane == 0) *abort_flag = 1;
+          stop = true;
+          break;
+        }
+        if (lane == 0) {
+          float* dst = stages + st * SST;
+          fence_proxy_async();
+          mbar_expect_tx(&full[st], fbytes + abytes);
+          bulk_g2s(dst, a.f + static_cast<size_t>(j) * B, fbytes, &full[st]);
+          bulk_g2s(dst + B, a.ops_cols + aoff, abytes, &full[st]);
+        }
+        kdone = k + 1;
+        __syncwarp();
+      }
+    }
+    if (lane == 0) {
+      if (*abort_flag) atomicExch(a.err, static_cast<int>(ASG_ERR_TIMEOUT));
+      // every issued copy lands before the CTA's shared memory is released (bounded)
+      for (int k = max(0, kdone - S); k < kdone; ++k) {
+        const long long t0 = clock64();
+        while (!mbar_test(&full[k % S], static_cast<uint32_t>((k / S) & 1)) && clock64() - t0 < (1LL << 28)) {
+        }
+      }
+    }
+    return;
+  }
+
+  // ---------------- consumer warps: tiles tid and tid + 128 ----------------
+  int nat_base[NT], base_g[NT], nat_s = 0, s_g = 0;
+#pragma unroll
+  for (int q = 0; q < NT; ++q) tile_place(tid + q * HALF, D - 3, D, a.stride, nat_base[q], nat_s);
+  // the d-2 rotation of kind-3 thread t+128 equals that of thread t
+  const int rot = (tid >> 1) & 3;
+  int cur_m = -1, pend = -1, mlane = -1;
+  bool direct = false, gave_up = false;
+  PairTile g32[NT];
+  F32Tile n32[NT], c32[NT];
+#pragma unroll
+  for (int q = 0; q < NT; ++q)
+#pragma unroll
+    for (int r = 0; r < P; ++r)
+#pragma unroll
+      for (int cp = 0; cp < 2; ++cp) g32[q].v[r][cp] = n32[q].v[r][cp] = c32[q].v[r][cp] = make_float2(0.f, 0.f);
+
+  for (int k = 0; k <= n; ++k) {
+    int m = -1;
+    const int st = k % S;
+    if (k < n) {
+      if ((k & 31) == 0) mlane = (k + lane < n) ? ed[k + lane].m : -1;
+      m = __shfl_sync(0xffffffffu, mlane, k & 31);
+      if (!gave_up) {
+        const bool ok = mbar_wait_bounded(&full[st], static_cast<uint32_t>((k / S) & 1));
+        if (!__all_sync(0xffffffffu, ok)) {
+          gave_up = true;
+          *abort_flag = 1;
+        }
+      }
+    }
+    if (m != cur_m) {
+      if (direct) {
+        const bool cols = cur_m == D - 1;
+#pragma unroll
+        for (int q = 0; q < NT; ++q)
+#pragma unroll
+          for (int r = 0; r < P; ++r) {
+            const float4 v = pt_row(g32[q], r, cols);
+            kahan2(n32[q].v[r][0], c32[q].v[r][0], make_float2(v.x, v.y));
+            kahan2(n32[q].v[r][1], c32[q].v[r][1], make_float2(v.z, v.w));
+          }
+      } else if (cur_m >= 0) {
+        // transpose the group's sums onto the natural tiles through the stage just consumed
+        consumer_sync_x2();
+        float* scr = stages + pend * SST;
+        const int rr = cur_m == D - 2 ? rot : 0;
+#pragma unroll
+        for (int q = 0; q < NT; ++q)
+#pragma unroll
+          for (int i = 0; i < P; ++i) {
+            const int r = (i + rr) & 3;
+            *reinterpret_cast<float4*>(scr + base_g[q] + r * s_g) = pt_row_sel(g32[q], r);
+          }
+        consumer_sync_x2();
+#pragma unroll
+        for (int q = 0; q < NT; ++q)
+#pragma unroll
+          for (int r = 0; r < P; ++r) {
+            const float4 v = *reinterpret_cast<const float4*>(scr + nat_base[q] + r * nat_s);
+            kahan2(n32[q].v[r][0], c32[q].v[r][0], make_float2(v.x, v.y));
+            kahan2(n32[q].v[r][1], c32[q].v[r][1], make_float2(v.z, v.w));
+          }
+      }
+      cur_m = m;
+      if (m >= 0) {
+#pragma unroll
+        for (int q = 0; q < NT; ++q) zero_pt(g32[q]);
+        direct = (m == D - 1) || (m == D - 3);
+        if (m == D - 1) {
+#pragma unroll
+          for (int q = 0; q < NT; ++q) base_g[q] = nat_base[q];
+          s_g = nat_s;
+        } else {
+#pragma unroll
+          for (int q = 0; q < NT; ++q) tile_place(tid + q * HALF, m, D, a.stride, base_g[q], s_g);
+        }
+      }
+    }
+    if (pend >= 0) {
+      __syncwarp();
+      if (lane == 0 && !gave_up) mbar_arrive(&empty[pend]);
+      pend = -1;
+    }
+    if (m < 0) break;
+    const float* sp = stages + st * SST;
+    if (m == D - 1)
+      pt_cols2(g32[0], g32[1], sp + B, sp + base_g[0], sp + base_g[1], s_g);
+    else
+      pt_rows_rot2(g32[0], g32[1], sp + B, sp + base_g[0], sp + base_g[1], s_g, m == D - 2 ? rot : 0);
+    pend = st;
+  }
+  if (*abort_flag) return;  // y is undefined; the plan's status word reports the timeout
+#pragma unroll
+  for (int q = 0; q < NT; ++q) {
+    float* yr = a.y + static_cast<size_t>(row) * B + nat_base[q];
+#pragma unroll
+    for (int r = 0; r < P; ++r)
+      *reinterpret_cast<float4*>(yr + r * nat_s) =
+          make_float4(n32[q].v[r][0].x, n32[q].v[r][0].y, n32[q].v[r][1].x, n32[q].v[r][1].y);
+  }
+}
+
 // Persistent variant of k_single_tma: one CTA per resident slot walks a static list of rows
 // (longest-processing-time assignment made at plan creation, cta_ptr/cta_rows).  The
 // producer streams entries across row boundaries, so only a CTA's first copy pays the
@@ -1216,6 +1399,20 @@ cudaError_t launch_p(const ApplyArgs<T>& a, int kind, cudaStream_t s) {
       cudaError_t e = ensure_smem(kern, sm, sm, done);
       if (e != cudaSuccess) return e;
       kern<<<a.N, 288, sm, s>>>(a);
+      return cudaGetLastError();
+    }
+  }
+  if constexpr (P == 4 && sizeof(T) == 4) {
+    if (kind == KK_SINGLE_TMA_X2) {
+      // FP32, two tiles per consumer thread: 4 stages, 2 CTAs per SM
+      if (a.B != 256 * P * P || !a.ops_cols) return cudaErrorInvalidValue;
+      constexpr int S0 = 4;
+      const size_t sm = static_cast<size_t>(S0) * (a.B + 16) * sizeof(float) + 2 * S0 * sizeof(uint64_t);
+      auto kern = k_single_tma_x2<S0, 2>;
+      static bool done = false;
+      cudaError_t e = ensure_smem(kern, sm, sm, done);
+      if (e != cudaSuccess) return e;
+      kern<<<a.N, 160, sm, s>>>(a);
       return cudaGetLastError();
     }
   }

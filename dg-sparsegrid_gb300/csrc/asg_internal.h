@@ -110,7 +110,7 @@ template <typename T>
 cudaError_t launch_grad(const GradArgs<T>& a, int P, cudaStream_t s);
 
 enum KernelKind { KK_CHAIN_WARP = 0, KK_CHAIN_CTA = 1, KK_SINGLE_MODE = 2, KK_SINGLE_TMA = 3, KK_SINGLE_TMA3 = 4,
-                  KK_SINGLE_TMA_ROWS = 5, KK_SINGLE_SMALL = 6, KK_STREAM = 7 };
+                  KK_SINGLE_TMA_ROWS = 5, KK_SINGLE_SMALL = 6, KK_STREAM = 7, KK_SINGLE_TMA_X2 = 8 };
 
 // Streaming FP32 apply (deg 4, 4,096-value blocks, one applied factor per term): every CTA
 // walks its own work stream.  An entry is {column element j, row element, operator block

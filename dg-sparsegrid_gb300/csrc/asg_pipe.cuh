@@ -150,6 +150,28 @@ __device__ __forceinline__ void pt_rows_rot(PairTile& g, const float* A, const f
     g.v[3][0] = ffma2(a01, dup(x.w), g.v[3][0]); g.v[3][1] = ffma2(a23, dup(x.w), g.v[3][1]);
   }
 }
+// One contraction index of pt_rows on a tile: operator column b (pairs a01, a23) times x row b.
+__device__ __forceinline__ void pt_rank1(PairTile& g, float2 a01, float2 a23, float4 x) {
+  g.v[0][0] = ffma2(a01, dup(x.x), g.v[0][0]); g.v[0][1] = ffma2(a23, dup(x.x), g.v[0][1]);
+  g.v[1][0] = ffma2(a01, dup(x.y), g.v[1][0]); g.v[1][1] = ffma2(a23, dup(x.y), g.v[1][1]);
+  g.v[2][0] = ffma2(a01, dup(x.z), g.v[2][0]); g.v[2][1] = ffma2(a23, dup(x.z), g.v[2][1]);
+  g.v[3][0] = ffma2(a01, dup(x.w), g.v[3][0]); g.v[3][1] = ffma2(a23, dup(x.w), g.v[3][1]);
+}
+// pt_rows_rot on two tiles (x0s, x1s) with one read of each operator column: each tile sees
+// pt_rows_rot's operations in pt_rows_rot's order
+__device__ __forceinline__ void pt_rows_rot2(PairTile& g0, PairTile& g1, const float* A, const float* x0s,
+                                             const float* x1s, int s, int rot) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int b = (i + rot) & 3;
+    const float4 q = *reinterpret_cast<const float4*>(A + 4 * b);
+    const float4 x0 = *reinterpret_cast<const float4*>(x0s + b * s);
+    const float4 x1 = *reinterpret_cast<const float4*>(x1s + b * s);
+    const float2 a01 = make_float2(q.x, q.y), a23 = make_float2(q.z, q.w);
+    pt_rank1(g0, a01, a23, x0);
+    pt_rank1(g1, a01, a23, x1);
+  }
+}
 // m == 5: y[r][a] += sum_b A[a][b] x[r][b]; x rows s apart (natural rows along dimension 3)
 __device__ __forceinline__ void pt_cols(PairTile& g, const float* A, const float* xs, int s) {
   float4 q[4];
@@ -163,6 +185,26 @@ __device__ __forceinline__ void pt_cols(PairTile& g, const float* A, const float
     for (int b = 0; b < 4; ++b) {
       g.v[r][0] = ffma2(make_float2(q[b].x, q[b].y), dup(xv[b]), g.v[r][0]);
       g.v[r][1] = ffma2(make_float2(q[b].z, q[b].w), dup(xv[b]), g.v[r][1]);
+    }
+  }
+}
+// pt_cols on two tiles with one read of the operator block (each tile: pt_cols's order)
+__device__ __forceinline__ void pt_cols2(PairTile& g0, PairTile& g1, const float* A, const float* x0s,
+                                         const float* x1s, int s) {
+  float4 q[4];
+#pragma unroll
+  for (int b = 0; b < 4; ++b) q[b] = *reinterpret_cast<const float4*>(A + 4 * b);
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const float4 x0 = *reinterpret_cast<const float4*>(x0s + r * s);
+    const float4 x1 = *reinterpret_cast<const float4*>(x1s + r * s);
+    const float xv0[4] = {x0.x, x0.y, x0.z, x0.w}, xv1[4] = {x1.x, x1.y, x1.z, x1.w};
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      g0.v[r][0] = ffma2(make_float2(q[b].x, q[b].y), dup(xv0[b]), g0.v[r][0]);
+      g0.v[r][1] = ffma2(make_float2(q[b].z, q[b].w), dup(xv0[b]), g0.v[r][1]);
+      g1.v[r][0] = ffma2(make_float2(q[b].x, q[b].y), dup(xv1[b]), g1.v[r][0]);
+      g1.v[r][1] = ffma2(make_float2(q[b].z, q[b].w), dup(xv1[b]), g1.v[r][1]);
     }
   }
 }

@@ -580,12 +580,12 @@ asg_status check_ptr(const void* ptr, const char* name) {
 }
 
 // The kernel family a precision runs: the tuned choice when asg_plan_tune made one, else the
-// plan's kind (whose FP64 side is kind 3 for the streaming kernel).
+// plan's kind (whose FP64 side is kind 3 for the FP32-only kinds 7 and 8).
 template <typename T>
 int effective_kind(const asg_plan* p) {
   const int t = p->tuned_kind[sizeof(T) == 4 ? 1 : 0];
   const int k = t >= 0 ? t : p->kernel_kind;
-  return (k == KK_STREAM && sizeof(T) == 8) ? KK_SINGLE_TMA : k;
+  return ((k == KK_STREAM || k == KK_SINGLE_TMA_X2) && sizeof(T) == 8) ? KK_SINGLE_TMA : k;
 }
 
 template <typename T>
@@ -633,10 +633,21 @@ asg_status apply_host(asg_plan* p, const T* hf, T* hy) {
   }
   T* df = static_cast<T*>(p->d_io);
   T* dy = reinterpret_cast<T*>(reinterpret_cast<char*>(p->d_io) + ((n * sizeof(T) + 255) / 256) * 256);
+  // A page-locked, device-mapped y (cudaHostAlloc / cudaHostRegister) is written by the kernel
+  // itself: each row's block leaves over the host link as soon as the row is done, so the
+  // device-to-host transfer overlaps the apply instead of following it.  The kernels store y
+  // with plain stores, once per value, so the result is the same as through the copy.
+  cudaPointerAttributes at{};
+  T* ky = dy;
+  if (cudaPointerGetAttributes(&at, hy) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer &&
+      (reinterpret_cast<uintptr_t>(at.devicePointer) & 15) == 0)
+    ky = static_cast<T*>(at.devicePointer);
+  else
+    cudaGetLastError();  // clear a query error for host memory the runtime does not know
   ASG_CUDA(cudaMemcpyAsync(df, hf, n * sizeof(T), cudaMemcpyHostToDevice, p->stream));
-  asg_status st = apply_dev<T>(p, df, dy, p->stream);
+  asg_status st = apply_dev<T>(p, df, ky, p->stream);
   if (st) return st;
-  ASG_CUDA(cudaMemcpyAsync(hy, dy, n * sizeof(T), cudaMemcpyDeviceToHost, p->stream));
+  if (ky == dy) ASG_CUDA(cudaMemcpyAsync(hy, dy, n * sizeof(T), cudaMemcpyDeviceToHost, p->stream));
   ASG_CUDA(cudaStreamSynchronize(p->stream));
   return ASG_OK;
 }
@@ -664,7 +675,7 @@ std::vector<int> candidate_kinds(asg_plan* p) {
   std::vector<int> out;
   const int saved = p->kernel_kind;
   const int t0 = p->tuned_kind[0], t1 = p->tuned_kind[1];
-  for (int k = 0; k <= 7; ++k) {
+  for (int k = 0; k <= 8; ++k) {
     if (asg_plan_set_kernel(p, k) == ASG_OK) out.push_back(k);
   }
   p->kernel_kind = saved;
@@ -976,7 +987,7 @@ asg_status asg_plan_set_kernel(asg_plan* p, int kind) {
   if (kind == asg::KK_STREAM && p->ws_ctas <= 0)
     return fail(ASG_ERR_UNSUPPORTED, "streaming kernel needs deg 4, d 6 and one non-identity factor per term");
   if (kind == asg::KK_SINGLE_MODE || kind == asg::KK_SINGLE_TMA || kind == asg::KK_SINGLE_TMA3 ||
-      kind == asg::KK_SINGLE_TMA_ROWS) {
+      kind == asg::KK_SINGLE_TMA_ROWS || kind == asg::KK_SINGLE_TMA_X2) {
     bool ok = kind != asg::KK_SINGLE_MODE ? (p->P == 4 && p->B == 4096)
                                          : ((p->P == 3 || p->P == 4) && p->B >= 32 * p->P * p->P);
     for (unsigned a : p->active) ok = ok && __builtin_popcount(a) == 1;
@@ -988,7 +999,7 @@ asg_status asg_plan_set_kernel(asg_plan* p, int kind) {
     for (unsigned a : p->active) ok = ok && __builtin_popcount(a) == 1;
     if (!ok) return fail(ASG_ERR_UNSUPPORTED, "small single-mode kernel needs one applied factor per term, deg^d <= 256");
   }
-  if (kind < 0 || kind > 7) return fail(ASG_ERR_INVALID, "unknown kernel kind %d", kind);
+  if (kind < 0 || kind > 8) return fail(ASG_ERR_INVALID, "unknown kernel kind %d", kind);
   p->kernel_kind = kind;
   p->tuned_kind[0] = p->tuned_kind[1] = -1;
   return ASG_OK;

@@ -74,7 +74,8 @@ typedef struct {
   double flops_executed;       /* flops of the executed work model */
   long long op_bytes_f64;      /* packed operator bytes on the device (FP64 copy) */
   int kernel_kind;             /* 0 warp chain, 1 CTA chain, 2-6 single-mode fiber kernels,
-                                  7 streaming single-mode kernel */
+                                  7 streaming single-mode kernel, 8 kind 3 with two tiles
+                                  per thread */
   int active_modes_max;        /* max over terms of non-identity factors */
 } asg_plan_stats;
 
@@ -104,9 +105,10 @@ asg_status asg_plan_update_ops(asg_plan* plan, const double* const* ops, const i
  * shared memory and 3 CTAs per SM, 5 the kind-3 pipeline in persistent CTAs that each walk
  * a balanced list of rows, 6 the small-block single-mode kernel (deg^d <= 256; grouped lanes
  * per row, no shared-memory staging), 7 the streaming kernel: FP32 in one persistent CTA per
- * SM walking a balanced stream of rows, each row's own block resident; FP64 runs kind 3
- * (2-7 need one non-identity factor per term; 3-5 and 7 need deg 4, d 6; 7 is the default
- * there).
+ * SM walking a balanced stream of rows, each row's own block resident; FP64 runs kind 3,
+ * 8 kind 3 in FP32 with two output tiles per consumer thread (4 consumer warps; results
+ * bitwise those of kind 3); FP64 runs kind 3
+ * (2-8 need one non-identity factor per term; 3-5, 7 and 8 need deg 4, d 6).
  * The default is chosen by asg_plan_create; this exists for testing one family against
  * another and for launch-shape tuning. */
 asg_status asg_plan_set_kernel(asg_plan* plan, int kind);

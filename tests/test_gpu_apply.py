@@ -127,6 +127,12 @@ def test_continuity6_lev4_deg4_kernels_agree(dev):
     assert np.array_equal(_apply(p, f, dev), y_single)
     assert np.array_equal(_apply(p, f, dev, torch.float32), y32)
     assert p.device_status() == 0
+    # two tiles per consumer thread: kind 3's operations per value, bitwise equal in FP32;
+    # its FP64 side is kind 3
+    p.set_kernel(asgkron._lib.KERNEL_SINGLE_TMA_X2)
+    assert np.array_equal(_apply(p, f, dev, torch.float32), y32)
+    assert np.array_equal(_apply(p, f, dev), y_single)
+    assert p.device_status() == 0
     for kind in (asgkron._lib.KERNEL_SINGLE_TMA3, asgkron._lib.KERNEL_SINGLE_MODE):
         p.set_kernel(kind)
         assert rel2(_apply(p, f, dev), y_single) <= FP64_TOL
@@ -171,7 +177,7 @@ def test_small_block_single_mode_kernel(dev, name, lev, deg):
 def test_continuity6_small_levels_row_lists(dev, lev):
     """continuity6 deg 4 at levels with fewer elements than resident CTAs (one row per CTA)
     and with several rows per CTA: the streaming kernel (kind 7) agrees with kind 3 in FP32,
-    kinds 3 and 5 agree bitwise, FP64 matches the oracle."""
+    kinds 3, 5 and 8 agree bitwise, FP64 matches the oracle."""
     pde, table, idx, mats = problem("continuity6", lev, 4)
     N = idx.shape[0]
     f = np.random.default_rng(lev).standard_normal(N * 4096)
@@ -185,6 +191,9 @@ def test_continuity6_small_levels_row_lists(dev, lev):
     assert rel2(y_stream, y3) <= FP32_TOL
     p.set_kernel(5)
     assert np.array_equal(_apply(p, f, dev), y3)
+    assert np.array_equal(_apply(p, f, dev, torch.float32), y3s)
+    assert p.device_status() == 0
+    p.set_kernel(8)
     assert np.array_equal(_apply(p, f, dev, torch.float32), y3s)
     assert p.device_status() == 0
     rows = np.arange(0, N, max(1, N // 5))
@@ -224,6 +233,22 @@ def test_deterministic_linear_and_host_path(dev):
     assert np.array_equal(h, a)
     h32 = plan.apply_host(f1.astype(np.float32))
     assert h32.dtype == np.float32 and rel2(h32, a) <= FP32_TOL
+
+
+@pytest.mark.parametrize("name,lev,deg", [("continuity3", 4, 3), ("continuity6", 2, 4)])
+def test_host_path_pinned_output(dev, name, lev, deg):
+    """A page-locked y is written by the apply kernel itself (no device-to-host copy); the
+    result equals the pageable copy path and the device apply bitwise, in both precisions."""
+    pde, table, idx, mats = problem(name, lev, deg)
+    plan = _plan(mats, idx, deg)
+    f = np.random.default_rng(21).standard_normal(plan.dof)
+    for dt in (torch.float64, torch.float32):
+        fh = torch.from_numpy(f).to(dt).pin_memory()
+        yh = torch.full_like(fh, float("nan")).pin_memory()
+        plan.apply_host(fh.numpy(), yh.numpy())
+        pageable = plan.apply_host(fh.numpy().copy())
+        assert np.array_equal(yh.numpy(), pageable)
+        assert np.array_equal(yh.numpy(), _apply(plan, f, dev, dt).astype(yh.numpy().dtype))
 
 
 def test_apply_A_matlab_mirror(dev):
