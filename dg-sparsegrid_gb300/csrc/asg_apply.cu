@@ -428,14 +428,13 @@ __device__ __forceinline__ void tile_cols_s(T (&g)[4][4], const T* A, const T* x
 
 __device__ __forceinline__ void consumer_sync() { asm volatile("bar.sync 1, 256;" ::: "memory"); }
 
-// Base offset and row stride of a thread's P x P tile spanning dimensions (u, d-1): the
-// thread's other digits run over dimensions {0..d-2} \ {u}, the highest dimension fastest.
-__device__ __forceinline__ void tile_place(int tid, int u, int D, const int* stride, int& base, int& s) {
-  int pw = 1;
-  for (int k = 0; k < D - 2 - u; ++k) pw *= 4;
-  const int lo = tid % pw, hi = tid / pw;
-  s = stride[u];
-  base = hi * s * 4 + lo * 4;
+// Base offset and row stride of a thread's 4 x 4 tile spanning dimensions (u, d-1) of a
+// deg-4 block (dimension k has stride 4^(d-1-k)): the thread's other digits run over
+// dimensions {0..d-2} \ {u}, the highest dimension fastest.  Shifts and masks only.
+__device__ __forceinline__ void tile_place(int tid, int u, int D, int& base, int& s) {
+  const int sh = 2 * (D - 2 - u);  // the digits below dimension u, 2 bits each
+  s = 1 << (2 * (D - 1 - u));
+  base = ((tid >> sh) * s + (tid & ((1 << sh) - 1))) * 4;
 }
 
 // Warp-specialised pipeline: warps 0..7 consume (256 threads, one P x P output tile each),
@@ -445,16 +444,21 @@ __device__ __forceinline__ void tile_place(int tid, int u, int D, const int* str
 // group boundary the stage just consumed doubles as the transpose buffer (no separate
 // scratch).  The natural output tile of a thread spans dimensions (d-3, d-1): consecutive
 // threads sit 16 bytes apart in shared memory; terms on dimensions d-3 and d-1 accumulate
-// straight into it, the others through the transpose.  FP32 blocks arrive column by column,
-// so one 128-bit shared load per operator column gives the paired FMA two pairs of operator
-// rows (the input value is duplicated in registers); groups merge into the output tile with
-// Kahan compensation.  Rows launch longest first (row_order).
-template <typename T, int S, int MINB, bool CSMEM>
+// straight into it, the others through the transpose.  FP32 operator blocks arrive with each
+// column's values duplicated ((A0b,A0b,A1b,A1b), (A2b,A2b,A3b,A3b)), so the paired FMA takes
+// an operator value pair and two neighbouring inputs along d-1 straight from shared memory;
+// on dimension d-1 (the contraction runs along the float4) an input value is paired with
+// itself instead.  Groups merge into the output tile with Kahan compensation (paired adds).
+// With OWN the row's own f block stays resident: the row's diagonal entries, one per term,
+// read it and copy only their operator block.  Rows launch longest first (row_order).
+template <typename T, int S, int MINB, bool CSMEM, bool OWN>
 __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
   constexpr int P = 4;
   constexpr bool F32 = sizeof(T) == 4;
   constexpr bool CS = F32 && CSMEM;  // FP32 compensation tile in shared memory (else registers)
-  constexpr int AB = 16;  // operator block values per stage (FP32: column by column)
+  // operator block values per stage: FP32 32 (rows: duplicated columns (A0b,A0b,A1b,A1b),
+  // (A2b,A2b,A3b,A3b); dimension d-1: columns (A0b,A1b,A2b,A3b) + padding), FP64 16
+  constexpr int AB = F32 ? 32 : 16;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_abort;
   const int tid = threadIdx.x;
@@ -464,14 +468,18 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
   T* stages = reinterpret_cast<T*>(smem_raw);
   // FP32: the Kahan compensation of the output tiles lives in shared memory (B values)
   float* comp = reinterpret_cast<float*>(stages + S * SST);
-  uint64_t* full = reinterpret_cast<uint64_t*>(comp + (CS ? B : 0));
+  // OWN: the row's own f block, resident for the whole row: the row's diagonal entries (one
+  // per term) read it here and copy only their operator block
+  T* own = reinterpret_cast<T*>(comp + (CS ? B : 0));
+  uint64_t* full = reinterpret_cast<uint64_t*>(own + (OWN ? B : 0));
   uint64_t* empty = full + S;
+  uint64_t* own_full = empty + S;
   const int row = a.row_order ? a.row_order[blockIdx.x] : blockIdx.x;
   const long long q0 = a.row_ptr[row];
   const int n = static_cast<int>(a.row_ptr[row + 1] - q0);
   const EntryDesc* ed = a.ed + q0;
   const uint32_t fbytes = static_cast<uint32_t>(B * sizeof(T)), abytes = AB * sizeof(T);
-  const T* opsrc = F32 ? reinterpret_cast<const T*>(a.ops_cols) : a.ops;
+  const T* opsrc = F32 ? reinterpret_cast<const T*>(a.ops_pair) : a.ops;
 
   if (tid == 0) {
     s_abort = 0;
@@ -479,6 +487,7 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
       mbar_init(&full[k], 1);
       mbar_init(&empty[k], 8);
     }
+    mbar_init(own_full, 1);
     mbar_fence_init();
   }
   __syncthreads();
@@ -488,6 +497,11 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
     // ---------------- producer warp ----------------
     int kdone = 0;
     bool stop = false;
+    if (OWN && lane == 0 && n > 0) {
+      fence_proxy_async();
+      mbar_expect_tx(own_full, fbytes);
+      bulk_g2s(own, a.f + static_cast<size_t>(row) * B, fbytes, own_full);
+    }
     for (int k0 = 0; k0 < n && !stop; k0 += 32) {
       EntryDesc mine{};
       if (k0 + lane < n) mine = ed[k0 + lane];
@@ -506,9 +520,10 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
         }
         if (lane == 0) {
           T* dst = stages + st * SST;
+          const bool self = OWN && j == row;
           fence_proxy_async();
-          mbar_expect_tx(&full[st], fbytes + abytes);
-          bulk_g2s(dst, a.f + static_cast<size_t>(j) * B, fbytes, &full[st]);
+          mbar_expect_tx(&full[st], (self ? 0u : fbytes) + abytes);
+          if (!self) bulk_g2s(dst, a.f + static_cast<size_t>(j) * B, fbytes, &full[st]);
           bulk_g2s(dst + B, opsrc + aoff * (AB / 16), abytes, &full[st]);
         }
         kdone = k + 1;
@@ -523,18 +538,24 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
         while (!mbar_test(&full[k % S], static_cast<uint32_t>((k / S) & 1)) && clock64() - t0 < (1LL << 28)) {
         }
       }
+      if (OWN && n > 0) {
+        const long long t0 = clock64();
+        while (!mbar_test(own_full, 0u) && clock64() - t0 < (1LL << 28)) {
+        }
+      }
     }
     return;
   }
 
   // ---------------- consumer warps ----------------
   int nat_base, nat_s;
-  tile_place(tid, D - 3, D, a.stride, nat_base, nat_s);
+  tile_place(tid, D - 3, D, nat_base, nat_s);
   int cur_m = -1, base_g = 0, s_g = 0, pend = -1;
-  bool direct = false, gave_up = false;
+  bool direct = false, gave_up = false, own_ready = false;
   int mlane = -1;
+  unsigned selfmask = 0;
   // FP32: paired state, compensation in registers or shared memory; FP64: scalar state
-  PairTile g32;  // a group's sums (pairs of operator rows)
+  F32Tile g32;  // a group's sums (rows along its dimension, column pairs along d-1)
   F32Tile n32, c32;
   T g[P][P], nat[P][P];
 #pragma unroll
@@ -563,12 +584,20 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
     int m = -1;
     const int st = k % S;
     if (k < n) {
-      if ((k & 31) == 0) mlane = (k + lane < n) ? ed[k + lane].m : -1;
+      if ((k & 31) == 0) {
+        const bool in = k + lane < n;
+        mlane = in ? ed[k + lane].m : -1;
+        selfmask = __ballot_sync(0xffffffffu, OWN && in && ed[k + lane].j == row);
+      }
       // the dimension comes from the immutable descriptors: consumer control flow (and every
       // named barrier below) is uniform even after a timeout; later waits are skipped
       m = __shfl_sync(0xffffffffu, mlane, k & 31);
       if (!gave_up) {
-        const bool ok = mbar_wait_bounded(&full[st], static_cast<uint32_t>((k / S) & 1));
+        bool ok = mbar_wait_bounded(&full[st], static_cast<uint32_t>((k / S) & 1));
+        if (ok && !own_ready && ((selfmask >> (k & 31)) & 1u)) {
+          ok = mbar_wait_bounded(own_full, 0u);
+          own_ready = true;
+        }
         // a warp that gave up on a stage never releases a stage again: the producer then
         // cannot re-arm a stage whose copy may still be in flight; its own bounded wait on
         // the empty barrier expires and it waits for its issued copies before exiting
@@ -583,7 +612,7 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
         if constexpr (F32) {
 #pragma unroll
           for (int r = 0; r < P; ++r) {
-            const float4 v = pt_row(g32, r, cur_m == D - 1);
+            const float4 v = f32_row(g32, r);
             merge_row(r, make_float2(v.x, v.y), make_float2(v.z, v.w));
           }
         } else {
@@ -601,7 +630,7 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
           if constexpr (F32) {
             // rows of a group on dimension d-2 in a per-thread rotated order (bank-conflict free)
             const int r = (i + (cur_m == D - 2 ? (tid >> 1) & 3 : 0)) & 3;
-            *reinterpret_cast<float4*>(scr + base_g + r * s_g) = pt_row_sel(g32, r);
+            *reinterpret_cast<float4*>(scr + base_g + r * s_g) = f32_row_sel(g32, r);
           } else {
             const int r = i;
             Row<T, P> rr;
@@ -638,7 +667,7 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
           base_g = nat_base;
           s_g = nat_s;
         } else {
-          tile_place(tid, m, D, a.stride, base_g, s_g);
+          tile_place(tid, m, D, base_g, s_g);
         }
       }
     }
@@ -649,12 +678,13 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
     }
     if (m < 0) break;
     const T* sp = stages + st * SST;
+    const T* xp = (((selfmask >> (k & 31)) & 1u) ? own : sp) + base_g;  // the column's f tile
     if constexpr (F32) {
       if (m == D - 1)
-        pt_cols(g32, reinterpret_cast<const float*>(sp + B), reinterpret_cast<const float*>(sp + base_g), s_g);
+        f32_cols(g32, reinterpret_cast<const float*>(sp + B), reinterpret_cast<const float*>(xp), s_g);
       else
-        pt_rows_rot(g32, reinterpret_cast<const float*>(sp + B), reinterpret_cast<const float*>(sp + base_g), s_g,
-                    m == D - 2 ? (tid >> 1) & 3 : 0);
+        f32_rows_rot(g32, reinterpret_cast<const float*>(sp + B), reinterpret_cast<const float*>(xp), s_g,
+                     m == D - 2 ? (tid >> 1) & 3 : 0);
     } else {
       T A[P * P];
 #pragma unroll
@@ -665,9 +695,9 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
         for (int c = 0; c < P; ++c) A[r * P + c] = rr.v[c];
       }
       if (m == D - 1)
-        tile_cols_s<T>(g, A, sp + base_g, s_g);
+        tile_cols_s<T>(g, A, xp, s_g);
       else
-        tile_rows<T>(g, A, sp + base_g, s_g);
+        tile_rows<T>(g, A, xp, s_g);
     }
     pend = st;
   }
@@ -697,7 +727,7 @@ __device__ __forceinline__ void consumer_sync_x2() { asm volatile("bar.sync 1, 1
 
 template <int S, int MINB>
 __global__ void __launch_bounds__(160, MINB) k_single_tma_x2(ApplyArgs<float> a) {
-  constexpr int P = 4, AB = 16, NCW = 4, NT = 2, HALF = 32 * NCW;
+  constexpr int P = 4, AB = 32, NCW = 4, NT = 2, HALF = 32 * NCW;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int s_abort;
   const int tid = threadIdx.x;
@@ -705,8 +735,10 @@ __global__ void __launch_bounds__(160, MINB) k_single_tma_x2(ApplyArgs<float> a)
   const int B = a.B, D = a.D;
   const int SST = B + AB;
   float* stages = reinterpret_cast<float*>(smem_raw);
-  uint64_t* full = reinterpret_cast<uint64_t*>(stages + S * SST);
+  float* own = stages + S * SST;  // the row's own f block (diagonal entries read it here)
+  uint64_t* full = reinterpret_cast<uint64_t*>(own + B);
   uint64_t* empty = full + S;
+  uint64_t* own_full = empty + S;
   const int row = a.row_order ? a.row_order[blockIdx.x] : blockIdx.x;
   const long long q0 = a.row_ptr[row];
   const int n = static_cast<int>(a.row_ptr[row + 1] - q0);
@@ -719,6 +751,7 @@ __global__ void __launch_bounds__(160, MINB) k_single_tma_x2(ApplyArgs<float> a)
       mbar_init(&full[k], 1);
       mbar_init(&empty[k], NCW);
     }
+    mbar_init(own_full, 1);
     mbar_fence_init();
   }
   __syncthreads();
@@ -728,6 +761,11 @@ __global__ void __launch_bounds__(160, MINB) k_single_tma_x2(ApplyArgs<float> a)
     // ---------------- producer warp (as in k_single_tma) ----------------
     int kdone = 0;
     bool stop = false;
+    if (lane == 0 && n > 0) {
+      fence_proxy_async();
+      mbar_expect_tx(own_full, fbytes);
+      bulk_g2s(own, a.f + static_cast<size_t>(row) * B, fbytes, own_full);
+    }
     for (int k0 = 0; k0 < n && !stop; k0 += 32) {
       EntryDesc mine{};
       if (k0 + lane < n) mine = ed[k0 + lane];
@@ -746,10 +784,11 @@ __global__ void __launch_bounds__(160, MINB) k_single_tma_x2(ApplyArgs<float> a)
         }
         if (lane == 0) {
           float* dst = stages + st * SST;
+          const bool self = j == row;
           fence_proxy_async();
-          mbar_expect_tx(&full[st], fbytes + abytes);
-          bulk_g2s(dst, a.f + static_cast<size_t>(j) * B, fbytes, &full[st]);
-          bulk_g2s(dst + B, a.ops_cols + aoff, abytes, &full[st]);
+          mbar_expect_tx(&full[st], (self ? 0u : fbytes) + abytes);
+          if (!self) bulk_g2s(dst, a.f + static_cast<size_t>(j) * B, fbytes, &full[st]);
+          bulk_g2s(dst + B, a.ops_pair + 2 * aoff, abytes, &full[st]);
         }
         kdone = k + 1;
         __syncwarp();
@@ -763,6 +802,11 @@ __global__ void __launch_bounds__(160, MINB) k_single_tma_x2(ApplyArgs<float> a)
         while (!mbar_test(&full[k % S], static_cast<uint32_t>((k / S) & 1)) && clock64() - t0 < (1LL << 28)) {
         }
       }
+      if (n > 0) {
+        const long long t0 = clock64();
+        while (!mbar_test(own_full, 0u) && clock64() - t0 < (1LL << 28)) {
+        }
+      }
     }
     return;
   }
@@ -770,12 +814,13 @@ __global__ void __launch_bounds__(160, MINB) k_single_tma_x2(ApplyArgs<float> a)
   // ---------------- consumer warps: tiles tid and tid + 128 ----------------
   int nat_base[NT], base_g[NT], nat_s = 0, s_g = 0;
 #pragma unroll
-  for (int q = 0; q < NT; ++q) tile_place(tid + q * HALF, D - 3, D, a.stride, nat_base[q], nat_s);
+  for (int q = 0; q < NT; ++q) tile_place(tid + q * HALF, D - 3, D, nat_base[q], nat_s);
   // the d-2 rotation of kind-3 thread t+128 equals that of thread t
   const int rot = (tid >> 1) & 3;
   int cur_m = -1, pend = -1, mlane = -1;
-  bool direct = false, gave_up = false;
-  PairTile g32[NT];
+  bool direct = false, gave_up = false, own_ready = false;
+  unsigned selfmask = 0;
+  F32Tile g32[NT];
   F32Tile n32[NT], c32[NT];
 #pragma unroll
   for (int q = 0; q < NT; ++q)
@@ -788,10 +833,18 @@ __global__ void __launch_bounds__(160, MINB) k_single_tma_x2(ApplyArgs<float> a)
     int m = -1;
     const int st = k % S;
     if (k < n) {
-      if ((k & 31) == 0) mlane = (k + lane < n) ? ed[k + lane].m : -1;
+      if ((k & 31) == 0) {
+        const bool in = k + lane < n;
+        mlane = in ? ed[k + lane].m : -1;
+        selfmask = __ballot_sync(0xffffffffu, in && ed[k + lane].j == row);
+      }
       m = __shfl_sync(0xffffffffu, mlane, k & 31);
       if (!gave_up) {
-        const bool ok = mbar_wait_bounded(&full[st], static_cast<uint32_t>((k / S) & 1));
+        bool ok = mbar_wait_bounded(&full[st], static_cast<uint32_t>((k / S) & 1));
+        if (ok && !own_ready && ((selfmask >> (k & 31)) & 1u)) {
+          ok = mbar_wait_bounded(own_full, 0u);
+          own_ready = true;
+        }
         if (!__all_sync(0xffffffffu, ok)) {
           gave_up = true;
           *abort_flag = 1;
@@ -800,12 +853,11 @@ __global__ void __launch_bounds__(160, MINB) k_single_tma_x2(ApplyArgs<float> a)
     }
     if (m != cur_m) {
       if (direct) {
-        const bool cols = cur_m == D - 1;
 #pragma unroll
         for (int q = 0; q < NT; ++q)
 #pragma unroll
           for (int r = 0; r < P; ++r) {
-            const float4 v = pt_row(g32[q], r, cols);
+            const float4 v = f32_row(g32[q], r);
             kahan2(n32[q].v[r][0], c32[q].v[r][0], make_float2(v.x, v.y));
             kahan2(n32[q].v[r][1], c32[q].v[r][1], make_float2(v.z, v.w));
           }
@@ -819,7 +871,7 @@ __global__ void __launch_bounds__(160, MINB) k_single_tma_x2(ApplyArgs<float> a)
 #pragma unroll
           for (int i = 0; i < P; ++i) {
             const int r = (i + rr) & 3;
-            *reinterpret_cast<float4*>(scr + base_g[q] + r * s_g) = pt_row_sel(g32[q], r);
+            *reinterpret_cast<float4*>(scr + base_g[q] + r * s_g) = f32_row_sel(g32[q], r);
           }
         consumer_sync_x2();
 #pragma unroll
@@ -834,7 +886,7 @@ __global__ void __launch_bounds__(160, MINB) k_single_tma_x2(ApplyArgs<float> a)
       cur_m = m;
       if (m >= 0) {
 #pragma unroll
-        for (int q = 0; q < NT; ++q) zero_pt(g32[q]);
+        for (int q = 0; q < NT; ++q) zero_f32(g32[q]);
         direct = (m == D - 1) || (m == D - 3);
         if (m == D - 1) {
 #pragma unroll
@@ -842,7 +894,7 @@ __global__ void __launch_bounds__(160, MINB) k_single_tma_x2(ApplyArgs<float> a)
           s_g = nat_s;
         } else {
 #pragma unroll
-          for (int q = 0; q < NT; ++q) tile_place(tid + q * HALF, m, D, a.stride, base_g[q], s_g);
+          for (int q = 0; q < NT; ++q) tile_place(tid + q * HALF, m, D, base_g[q], s_g);
         }
       }
     }
@@ -853,10 +905,11 @@ __global__ void __launch_bounds__(160, MINB) k_single_tma_x2(ApplyArgs<float> a)
     }
     if (m < 0) break;
     const float* sp = stages + st * SST;
+    const float* xs = ((selfmask >> (k & 31)) & 1u) ? own : sp;  // the column's f block
     if (m == D - 1)
-      pt_cols2(g32[0], g32[1], sp + B, sp + base_g[0], sp + base_g[1], s_g);
+      f32_cols2(g32[0], g32[1], sp + B, xs + base_g[0], xs + base_g[1], s_g);
     else
-      pt_rows_rot2(g32[0], g32[1], sp + B, sp + base_g[0], sp + base_g[1], s_g, m == D - 2 ? rot : 0);
+      f32_rows_rot2(g32[0], g32[1], sp + B, xs + base_g[0], xs + base_g[1], s_g, m == D - 2 ? rot : 0);
     pend = st;
   }
   if (*abort_flag) return;  // y is undefined; the plan's status word reports the timeout
@@ -955,7 +1008,7 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma_rows(ApplyArgs<T> a) {
 
   // ---------------- consumer warps ----------------
   int nat_base, nat_s;
-  tile_place(tid, D - 3, D, a.stride, nat_base, nat_s);
+  tile_place(tid, D - 3, D, nat_base, nat_s);
   int g = 0;
   bool gave_up = false;
   for (int ri = ri0; ri < ri1; ++ri) {
@@ -1051,7 +1104,7 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma_rows(ApplyArgs<T> a) {
             base_g = nat_base;
             s_g = nat_s;
           } else {
-            tile_place(tid, m, D, a.stride, base_g, s_g);
+            tile_place(tid, m, D, base_g, s_g);
           }
         }
       }
@@ -1372,19 +1425,20 @@ cudaError_t launch_p(const ApplyArgs<T>& a, int kind, cudaStream_t s) {
   }
   if constexpr (P == 4) {
     if (kind == KK_SINGLE_TMA || kind == KK_SINGLE_TMA3) {
-      // FP32: 4 stages, 2 or 3 CTAs per SM (kind 3 / kind 4); FP64: 3 stages, 1 CTA per SM
-      // FP32: 3 stages + compensation tile (3 CTAs per SM), or 4 stages (2 per SM, kind 4);
-      // FP64: 3 stages, 1 CTA per SM
+      // kind 3: FP32 4 stages (2 CTAs per SM), FP64 3 stages (1 CTA per SM), each with the
+      // row's own f block resident; kind 4 (FP32): 3 stages and the compensation tile in
+      // shared memory, no resident block (3 CTAs per SM)
       if (a.B != 256 * P * P) return cudaErrorInvalidValue;  // 8 consumer warps own one tile each
-      if (sizeof(T) == 4 && !a.ops_cols) return cudaErrorInvalidValue;
-      auto smem_for = [&](int S, bool csmem) {
-        return static_cast<size_t>(S) * (a.B + 16) * sizeof(T) +
-               (csmem ? a.B * sizeof(float) : 0) + 2 * S * sizeof(uint64_t);
+      if (sizeof(T) == 4 && !a.ops_pair) return cudaErrorInvalidValue;
+      constexpr int AB = sizeof(T) == 4 ? 32 : 16;  // operator values per stage
+      auto smem_for = [&](int S, bool csmem, bool own) {
+        return static_cast<size_t>(S) * (a.B + AB) * sizeof(T) + (csmem ? a.B * sizeof(float) : 0) +
+               (own ? a.B * sizeof(T) : 0) + (2 * S + 1) * sizeof(uint64_t);
       };
       if constexpr (sizeof(T) == 4) {
         if (kind == KK_SINGLE_TMA3) {
-          const size_t sm = smem_for(3, true);
-          auto kern = k_single_tma<T, 3, 3, true>;
+          const size_t sm = smem_for(3, true, false);
+          auto kern = k_single_tma<T, 3, 3, true, false>;
           static bool done = false;
           cudaError_t e = ensure_smem(kern, sm, sm, done);
           if (e != cudaSuccess) return e;
@@ -1393,8 +1447,8 @@ cudaError_t launch_p(const ApplyArgs<T>& a, int kind, cudaStream_t s) {
         }
       }
       constexpr int S0 = sizeof(T) == 4 ? 4 : 3;
-      const size_t sm = smem_for(S0, false);
-      auto kern = k_single_tma<T, S0, sizeof(T) == 4 ? 2 : 1, false>;
+      const size_t sm = smem_for(S0, false, true);
+      auto kern = k_single_tma<T, S0, sizeof(T) == 4 ? 2 : 1, false, true>;
       static bool done = false;
       cudaError_t e = ensure_smem(kern, sm, sm, done);
       if (e != cudaSuccess) return e;
@@ -1405,9 +1459,9 @@ cudaError_t launch_p(const ApplyArgs<T>& a, int kind, cudaStream_t s) {
   if constexpr (P == 4 && sizeof(T) == 4) {
     if (kind == KK_SINGLE_TMA_X2) {
       // FP32, two tiles per consumer thread: 4 stages, 2 CTAs per SM
-      if (a.B != 256 * P * P || !a.ops_cols) return cudaErrorInvalidValue;
+      if (a.B != 256 * P * P || !a.ops_pair) return cudaErrorInvalidValue;
       constexpr int S0 = 4;
-      const size_t sm = static_cast<size_t>(S0) * (a.B + 16) * sizeof(float) + 2 * S0 * sizeof(uint64_t);
+      const size_t sm = (static_cast<size_t>(S0) * (a.B + 32) + a.B) * sizeof(float) + (2 * S0 + 1) * sizeof(uint64_t);
       auto kern = k_single_tma_x2<S0, 2>;
       static bool done = false;
       cudaError_t e = ensure_smem(kern, sm, sm, done);

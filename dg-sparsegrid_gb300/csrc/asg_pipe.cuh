@@ -85,28 +85,107 @@ __device__ __forceinline__ void f32_rows(F32Tile& g, const float* Ad, const floa
 }
 // g[r][a] += sum_b A[a][b] x[r][b]; A column b arrives as (A0b,A1b,A2b,A3b)
 __device__ __forceinline__ void f32_cols(F32Tile& g, const float* Ap, const float* xs, int s) {
+  float4 q[4];
+#pragma unroll
+  for (int b = 0; b < 4; ++b) q[b] = *reinterpret_cast<const float4*>(Ap + b * 8);
 #pragma unroll
   for (int r = 0; r < 4; ++r) {
     const float4 x = *reinterpret_cast<const float4*>(xs + r * s);
     const float xv[4] = {x.x, x.y, x.z, x.w};
 #pragma unroll
     for (int b = 0; b < 4; ++b) {
-      const float4 q = *reinterpret_cast<const float4*>(Ap + b * 8);
       const float2 xb = make_float2(xv[b], xv[b]);
-      g.v[r][0] = ffma2(make_float2(q.x, q.y), xb, g.v[r][0]);
-      g.v[r][1] = ffma2(make_float2(q.z, q.w), xb, g.v[r][1]);
+      g.v[r][0] = ffma2(make_float2(q[b].x, q[b].y), xb, g.v[r][0]);
+      g.v[r][1] = ffma2(make_float2(q[b].z, q[b].w), xb, g.v[r][1]);
     }
   }
 }
-// Kahan-compensated s += v on a column pair (c carries the compensation).
+// Paired subtraction a - b (sub.rn.f32x2).
+__device__ __forceinline__ float2 fsub2(float2 a, float2 b) {
+  float2 d;
+  asm("{\n .reg .b64 ra, rb, rd;\n mov.b64 ra, {%2, %3};\n mov.b64 rb, {%4, %5};\n"
+      " sub.rn.f32x2 rd, ra, rb;\n mov.b64 {%0, %1}, rd;\n}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+// Kahan-compensated s += v on a column pair (c carries the compensation), on paired adds:
+// y = v - c, t = s + y, c = (t - s) - y, s = t, each rounded to nearest as in scalar Kahan.
 __device__ __forceinline__ void kahan2(float2& s, float2& c, float2 v) {
-  float y = v.x - c.x, t = s.x + y;
-  c.x = (t - s.x) - y;
-  s.x = t;
-  y = v.y - c.y;
-  t = s.y + y;
-  c.y = (t - s.y) - y;
-  s.y = t;
+  const float2 y = fsub2(v, c);
+  const float2 t = __fadd2_rn(s, y);
+  c = fsub2(fsub2(t, s), y);
+  s = t;
+}
+
+// f32_rows visiting the contraction index from `rot` (0..3) on: each output sums the same
+// products in the order pt_rows_rot uses (threads whose tiles lie 64 bytes apart then read
+// different shared-memory banks)
+__device__ __forceinline__ void f32_rank1(F32Tile& g, float4 q0, float4 q1, float4 x) {
+  const float2 x01 = make_float2(x.x, x.y), x23 = make_float2(x.z, x.w);
+  const float2 a0 = make_float2(q0.x, q0.y), a1 = make_float2(q0.z, q0.w);
+  const float2 a2 = make_float2(q1.x, q1.y), a3 = make_float2(q1.z, q1.w);
+  g.v[0][0] = ffma2(a0, x01, g.v[0][0]); g.v[0][1] = ffma2(a0, x23, g.v[0][1]);
+  g.v[1][0] = ffma2(a1, x01, g.v[1][0]); g.v[1][1] = ffma2(a1, x23, g.v[1][1]);
+  g.v[2][0] = ffma2(a2, x01, g.v[2][0]); g.v[2][1] = ffma2(a2, x23, g.v[2][1]);
+  g.v[3][0] = ffma2(a3, x01, g.v[3][0]); g.v[3][1] = ffma2(a3, x23, g.v[3][1]);
+}
+__device__ __forceinline__ void f32_rows_rot(F32Tile& g, const float* Ad, const float* xs, int s, int rot) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int b = (i + rot) & 3;
+    const float4 x = *reinterpret_cast<const float4*>(xs + b * s);
+    const float4 q0 = *reinterpret_cast<const float4*>(Ad + b * 8);
+    const float4 q1 = *reinterpret_cast<const float4*>(Ad + b * 8 + 4);
+    f32_rank1(g, q0, q1, x);
+  }
+}
+// f32_rows_rot on two tiles with one read of each duplicated operator column
+__device__ __forceinline__ void f32_rows_rot2(F32Tile& g0, F32Tile& g1, const float* Ad, const float* x0s,
+                                              const float* x1s, int s, int rot) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int b = (i + rot) & 3;
+    const float4 q0 = *reinterpret_cast<const float4*>(Ad + b * 8);
+    const float4 q1 = *reinterpret_cast<const float4*>(Ad + b * 8 + 4);
+    const float4 x0 = *reinterpret_cast<const float4*>(x0s + b * s);
+    const float4 x1 = *reinterpret_cast<const float4*>(x1s + b * s);
+    f32_rank1(g0, q0, q1, x0);
+    f32_rank1(g1, q0, q1, x1);
+  }
+}
+// f32_cols on two tiles with one read of the operator block
+__device__ __forceinline__ void f32_cols2(F32Tile& g0, F32Tile& g1, const float* Ap, const float* x0s,
+                                          const float* x1s, int s) {
+  float4 q[4];
+#pragma unroll
+  for (int b = 0; b < 4; ++b) q[b] = *reinterpret_cast<const float4*>(Ap + b * 8);
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const float4 x0 = *reinterpret_cast<const float4*>(x0s + r * s);
+    const float4 x1 = *reinterpret_cast<const float4*>(x1s + r * s);
+    const float xv0[4] = {x0.x, x0.y, x0.z, x0.w}, xv1[4] = {x1.x, x1.y, x1.z, x1.w};
+#pragma unroll
+    for (int b = 0; b < 4; ++b) {
+      g0.v[r][0] = ffma2(make_float2(q[b].x, q[b].y), make_float2(xv0[b], xv0[b]), g0.v[r][0]);
+      g0.v[r][1] = ffma2(make_float2(q[b].z, q[b].w), make_float2(xv0[b], xv0[b]), g0.v[r][1]);
+      g1.v[r][0] = ffma2(make_float2(q[b].x, q[b].y), make_float2(xv1[b], xv1[b]), g1.v[r][0]);
+      g1.v[r][1] = ffma2(make_float2(q[b].z, q[b].w), make_float2(xv1[b], xv1[b]), g1.v[r][1]);
+    }
+  }
+}
+// Row r of a tile as the four values along dimension d-1
+__device__ __forceinline__ float4 f32_row(const F32Tile& g, int r) {
+  return make_float4(g.v[r][0].x, g.v[r][0].y, g.v[r][1].x, g.v[r][1].y);
+}
+// f32_row for a row index known only at run time (selects, no local memory)
+__device__ __forceinline__ float4 f32_row_sel(const F32Tile& g, int r) {
+  const float4 r0 = f32_row(g, 0), r1 = f32_row(g, 1), r2 = f32_row(g, 2), r3 = f32_row(g, 3);
+  return r == 0 ? r0 : r == 1 ? r1 : r == 2 ? r2 : r3;
+}
+__device__ __forceinline__ void zero_f32(F32Tile& t) {
+#pragma unroll
+  for (int r = 0; r < 4; ++r) t.v[r][0] = t.v[r][1] = make_float2(0.f, 0.f);
 }
 
 // A group's sums as pairs of operator rows: v[c][p] = (y[2p][c], y[2p+1][c]) with y[r][c]
