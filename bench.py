@@ -53,6 +53,9 @@ def parse_args():
     ap.add_argument("--ref-budget", type=float, default=150.0,
                     help="reference arm: seconds of host work for warmup + steps (sets the rows per step)")
     ap.add_argument("--skip-variants", action="store_true")
+    ap.add_argument("--replicas", action="store_true",
+                    help="with several GPUs: run independent copies of the one-GPU workload (weak scaling) instead "
+                         "of splitting its rows across the GPUs")
     ap.add_argument("--workload", default="continuity6", choices=["continuity6", "batched", "implicit"],
                     help="batched: the 256-problem persistent-launch configuration; implicit: the "
                          "backward-Euler diffusion2 configuration (each its own JSON line)")
@@ -357,6 +360,63 @@ def implicit_steps(dev, nsteps=10):
                                                      torch.linalg.norm(finals["fp64"]))
     out["dof"] = plan.dof
     plan.close()
+    return out
+
+
+def adaptive_plan_updates(dev, nsteps=5):
+    """Plan maintenance under adaptivity: the continuity2 adaptive run (SG level 3, degree 4,
+    central flux, relative threshold 1e-3, RK3 at CFL 0.01: the setup of the reference's
+    continuity2_ad_sg_l3_d4 gold run, 20 -> 112 elements), every step on the GPU (FP64 RK3).
+    Each adapted table needs a plan: "rebuild" creates one from the table's rechained operators
+    (asg_plan_create); "update" keeps one plan made from the maximum-level operators and swaps
+    its table in place (asg_plan_update_elements).  Reports host milliseconds per plan change
+    (synchronised) and the difference of the final states."""
+    import numpy as np
+    import torch
+
+    import asgkron
+    from asgkron import pdes
+    from asgkron.adapt import AdaptiveRun, operator_extent, update_plan
+    from asgkron.steppers import RK3Stepper
+
+    out = {}
+    finals = {}
+    for mode in ("rebuild", "update"):
+        pde = pdes.continuity2(3, 0.0)
+        run = AdaptiveRun(pde, 4, asgkron.hash_table_sparse_nD([3, 3], 8), 1e-3)
+        dt = pdes.continuity2(3, 0.0).dt(0.01)
+        st = {"plan": None, "ms": [], "tables": 0}
+
+        def step(r, fv, t):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            if mode == "rebuild":
+                if st["plan"] is not None:
+                    st["plan"].close()
+                st["plan"] = asgkron.Plan.create(r.term_mats(), r.idx1d, 4)
+            elif st["plan"] is None:
+                top = r.pde.rechain_term_mats(4, [8, 8], 8, r._pterms)
+                st["plan"] = asgkron.Plan.create(top, r.idx1d, 4, op_blocks=operator_extent(top, 4))
+            else:
+                st["plan"] = update_plan(st["plan"], r.table, term_mats=r.term_mats())
+            torch.cuda.synchronize()
+            st["ms"].append((time.perf_counter() - t0) * 1e3)
+            st["tables"] += 1
+            x = torch.from_numpy(np.ascontiguousarray(fv)).to(dev)
+            RK3Stepper(st["plan"], pde, r.idx1d).step(x, t, dt)
+            return x.cpu().numpy()
+
+        f = run.initial()
+        for i in range(nsteps):
+            f = run.advance(f, i * dt, step)
+        finals[mode] = f
+        ms = st["ms"]
+        out[mode] = {"plan_changes": st["tables"], "first_ms": ms[0],
+                     "mean_ms_after_first": sum(ms[1:]) / max(1, len(ms) - 1), "elements_final": run.table.num_elems}
+        st["plan"].close()
+    out["speedup_after_first"] = out["rebuild"]["mean_ms_after_first"] / out["update"]["mean_ms_after_first"]
+    out["final_state_rel_diff"] = float(np.linalg.norm(finals["rebuild"] - finals["update"]) /
+                                        np.linalg.norm(finals["rebuild"]))
     return out
 
 
@@ -774,6 +834,98 @@ def small_config_graph(dev):
     return out
 
 
+def run_sharded(args, rank, world, local):
+    """The headline workload on ``world`` GPUs with y = A f split by output element (strong
+    scaling: the total work is the one-GPU workload).  Rows are split into contiguous ranges
+    balanced by work entries; every rank builds the row-slice plan of its range, holds f for
+    its rows, and per step exchanges exactly the halo blocks its rows read (one NCCL
+    all-to-all into buffers allocated once) and applies its slice.  value = all DOF over the
+    slowest rank's step time; e2e adds each rank's host copies of its f rows and y rows."""
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    import asgkron
+    from asgkron.shard import ShardedApply, partition_rows, row_plan
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist.init_process_group("nccl", device_id=dev)
+    pde, deg, idx, mats = build_workload()
+    N, D = idx.shape
+    B = deg ** D
+    dof = N * B
+    full = asgkron.Plan.create(mats, idx, deg)
+    cost = full.row_entries()
+    full.close()
+    ranges = partition_rows(cost, world)
+    r0, r1 = ranges[rank]
+    plan = row_plan(mats, idx, deg, (r0, r1))
+    sh = ShardedApply(plan, ranges, B)
+    f_all = np.random.default_rng(4).standard_normal(dof).astype(np.float32)
+    f_local = torch.from_numpy(f_all[r0 * B:r1 * B].copy()).to(dev)
+    y = torch.empty(plan.dof, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    flush_buf = torch.empty(512 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    for _ in range(max(3, args.warmup)):
+        flush_buf.fill_(1)
+        sh.apply(f_local, y)
+    sampler = ClockSampler(local)
+    dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.time()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for s_, e_ in ev:
+        flush_buf.fill_(1)
+        s_.record(stream)
+        sh.apply(f_local, y)
+        e_.record(stream)
+    torch.cuda.synchronize()
+    dist.barrier()
+    t1 = time.time()
+    clocks = sampler.stop(t0, t1)
+    ms = sum(s_.elapsed_time(e_) for s_, e_ in ev) / len(ev)
+    t = torch.tensor([ms], device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    step_ms = float(t.item())
+    # end to end: each rank's f rows in from pinned host memory, exchange, apply, y rows out
+    fh = torch.from_numpy(f_all[r0 * B:r1 * B].copy()).pin_memory()
+    yh = torch.empty(plan.dof, dtype=torch.float32).pin_memory()
+    e2e_steps = max(1, min(args.steps, 200))
+    for _ in range(3):
+        f_local.copy_(fh, non_blocking=True)
+        yh.copy_(sh.apply(f_local, y), non_blocking=True)
+    torch.cuda.synchronize()
+    dist.barrier()
+    ta = time.perf_counter()
+    for _ in range(e2e_steps):
+        f_local.copy_(fh, non_blocking=True)
+        yh.copy_(sh.apply(f_local, y), non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_local = (time.perf_counter() - ta) / e2e_steps * 1e3
+    t = torch.tensor([e2e_local], device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    e2e_ms = float(t.item())
+    halo = torch.tensor([float(sh.halo.size)], device=dev)
+    dist.all_reduce(halo)
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": dof / (step_ms * 1e-3) / 1e9, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+            "scaling": "strong", "vs_baseline": None, "dtype": "f32", "data": DATA, "config": workload_config(dof),
+            "details": {"parallelism": "row slices over %d ranks (balanced by work entries), halo all-to-all per "
+                                       "step" % world,
+                        "ranges": [[int(a), int(b)] for a, b in ranges],
+                        "halo_blocks_total": int(halo.item()), "all_gather_blocks_would_be": (world - 1) * N},
+            "e2e": {"value": dof / (e2e_ms * 1e-3) / 1e9, "unit": UNIT, "h2d_bytes_per_step": 4 * dof,
+                    "d2h_bytes_per_step": 4 * dof, "ms_per_step": e2e_ms},
+            "gpu_launches": args.steps * world,
+            "clocks": clocks,
+        }), flush=True)
+    plan.close()
+    dist.destroy_process_group()
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_env()
@@ -788,6 +940,9 @@ def main():
         return
     if args.workload == "implicit":
         run_implicit(args, rank, local)
+        return
+    if world > 1 and not args.replicas:
+        run_sharded(args, rank, world, local)
         return
     import numpy as np
     import torch
@@ -895,6 +1050,7 @@ def main():
         variants["continuity2_lev4_deg2_fp64_graph"] = small_config_graph(dev)
         variants["implicit_diffusion2_lev8_deg4"] = implicit_steps(dev)
         variants["precision_continuity3_lev6_deg3"] = precision_continuity3(dev, flush, stream)
+        variants["adaptive_plan_updates_continuity2"] = adaptive_plan_updates(dev)
         variants["batched_256_lev3_7"] = batched_measure(dev, 256, 7, max(1, min(args.steps, 5)), 3)
         # the roofline denominators measured here: the plan's gather pattern and the FMA pipes
         gs = gather_stream(plan, f32, flush, stream)

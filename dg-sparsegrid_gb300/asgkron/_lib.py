@@ -51,6 +51,10 @@ class PlanDesc(C.Structure):
     ]
 
 
+class PlanExt(C.Structure):
+    _fields_ = [("row_begin", C.c_int), ("row_end", C.c_int), ("op_blocks", C.POINTER(C.c_int))]
+
+
 class PartialTermDesc(C.Structure):
     _fields_ = [
         ("kind", C.c_int),
@@ -107,6 +111,10 @@ SIGNATURES = {
     "asg_plan_destroy": (C.c_int, [C.c_void_p]),
     "asg_plan_stats_get": (C.c_int, [C.c_void_p, C.POINTER(PlanStats)]),
     "asg_plan_update_ops": (C.c_int, [C.c_void_p, C.POINTER(C.POINTER(C.c_double)), C.POINTER(C.c_int)]),
+    "asg_plan_create_ex": (C.c_int, [C.POINTER(PlanDesc), C.POINTER(PlanExt), C.POINTER(C.c_void_p)]),
+    "asg_plan_halo": (C.c_int, [C.c_void_p, _I, C.c_longlong, C.POINTER(C.c_longlong)]),
+    "asg_plan_row_entries": (C.c_int, [C.c_void_p, C.POINTER(C.c_longlong)]),
+    "asg_plan_update_elements": (C.c_int, [C.c_void_p, C.c_int, _I, C.POINTER(C.c_longlong), _I]),
     "asg_plan_set_kernel": (C.c_int, [C.c_void_p, C.c_int]),
     "asg_plan_tune": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_float),
                                 C.POINTER(C.c_float)]),

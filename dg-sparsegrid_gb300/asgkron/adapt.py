@@ -14,7 +14,8 @@
   table yet are appended, in discovery order, with coefficient value 1e-15.
 
 ``AdaptiveRun`` drives the reference's adaptive time loop around a caller's time step.
-``rebuild_plan`` builds the plan for a new table.  Its operators are the plan's own
+``rebuild_plan`` builds the plan for a new table; ``update_plan`` instead replaces the table
+of an existing plan in place when the operators keep their values.  Its operators are the plan's own
 (single partial terms are level-independent, so operators built at the maximum level serve
 every table) or, for chained partial terms, the ones ``PDE.rechain_term_mats`` forms at the
 new table's levels, as adapt.m:417-437 does through get_coeff_mats_rechain.m.  Plan creation
@@ -121,14 +122,43 @@ def table_levels(table):
     return [int(v) for v in lv.max(axis=0)] if lv.size else []
 
 
-def rebuild_plan(plan, table, pairs=None, term_mats=None, **kw):
-    """A plan for the adapted table with the work model of ``plan`` and its operators, or
-    ``term_mats`` (e.g. ``pde.rechain_term_mats(deg, table_levels(table))``)."""
+def operator_extent(term_mats, deg):
+    """Blocks per side of the operators on each dimension (their full extent: operators built at
+    the maximum level cover every table the run can reach)."""
+    return [min(int(row[m].shape[0]) for row in term_mats) // deg for m in range(len(term_mats[0]))]
+
+
+def rebuild_plan(plan, table, pairs=None, term_mats=None, reserve=False, **kw):
+    """A new plan for the adapted table with the work model of ``plan`` and its operators, or
+    ``term_mats`` (e.g. ``pde.rechain_term_mats(deg, table_levels(table))``).  ``reserve``
+    packs the operators' full extent, so that ``update_plan`` can follow later tables."""
     from .api import Plan
 
     structure = kw.pop("structure", plan.structure)
     mats = plan.term_mats if term_mats is None else term_mats
-    return Plan.create(mats, table.idx1d(), plan.deg, pairs=pairs, structure=structure, **kw)
+    ob = operator_extent(mats, plan.deg) if reserve else None
+    return Plan.create(mats, table.idx1d(), plan.deg, pairs=pairs, structure=structure, op_blocks=ob, **kw)
+
+
+def update_plan(plan, table, pairs=None, term_mats=None):
+    """The plan for the adapted table on the same operator values (single partial terms: the
+    operator of a coarser level is the leading block of a finer one, so values never change,
+    only the extent the table reaches): the element table and work list are replaced in place
+    (asg_plan_update_elements; the operators' analysis, packing and device copies are kept).
+    When the table reaches beyond the plan's packed operators, a new plan is built from
+    ``term_mats`` (default: the plan's own), reserving their full extent.  Returns the plan to
+    use (``plan`` itself, or the new one; the old one is then closed)."""
+    from ._lib import ASG_ERR_CAPACITY, AsgError
+
+    try:
+        plan.update_elements(table.idx1d(), pairs)
+        return plan
+    except AsgError as e:
+        if e.status != ASG_ERR_CAPACITY:
+            raise
+    new = rebuild_plan(plan, table, pairs=pairs, term_mats=term_mats, reserve=True)
+    plan.close()
+    return new
 
 
 class AdaptiveRun:

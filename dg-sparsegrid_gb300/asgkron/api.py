@@ -10,7 +10,7 @@ import ctypes as C
 
 import numpy as np
 
-from ._lib import (ASG_STRUCT_DETECT, ASG_STRUCT_NONE, PlanDesc, PlanStats, check, lib)
+from ._lib import (ASG_STRUCT_DETECT, ASG_STRUCT_NONE, PlanDesc, PlanExt, PlanStats, check, lib)
 
 # |entry| <= DEFAULT_DROP_TOL * max|op| is treated as an exact zero by the structure
 # analysis.  The wavelet-space mass factors differ from the identity by ~1e-15 relative
@@ -82,18 +82,78 @@ class Plan:
         self._desc = desc
         self._handle = C.c_void_p()
 
-    def _create(self, deg):
+    def _create(self, deg, rows=None, op_blocks=None):
         self._desc.deg = int(deg)
         self.deg = int(deg)
-        check(lib().asg_plan_create(C.byref(self._desc), C.byref(self._handle)))
         self.B = self.deg ** self.D
-        self.dof = self.N * self.B
+        self.rows = None
+        if rows is None and op_blocks is None:
+            check(lib().asg_plan_create(C.byref(self._desc), C.byref(self._handle)))
+        else:
+            ext = PlanExt()
+            r0, r1 = (0, self.N) if rows is None else (int(rows[0]), int(rows[1]))
+            ext.row_begin, ext.row_end = r0, r1
+            if op_blocks is not None:
+                ob = np.ascontiguousarray(np.asarray(op_blocks, dtype=np.int32))
+                if ob.shape != (self.D,):
+                    raise ValueError("op_blocks must hold num_dims values")
+                self._keep.append(ob)
+                ext.op_blocks = ob.ctypes.data_as(C.POINTER(C.c_int))
+            check(lib().asg_plan_create_ex(C.byref(self._desc), C.byref(ext), C.byref(self._handle)))
+            if (r0, r1) != (0, self.N):
+                self.rows = (r0, r1)
+        n_out = self.N if self.rows is None else self.rows[1] - self.rows[0]
+        self.dof = n_out * self.B                      # values of y
+        self.dof_in = (n_out + len(self.halo())) * self.B  # values of f
 
     @classmethod
-    def create(cls, term_mats, idx1d, deg, **kw):
+    def create(cls, term_mats, idx1d, deg, rows=None, op_blocks=None, **kw):
+        """rows=(r0, r1): a row-slice plan (asg_plan_create_ex): y holds rows r0..r1-1, f holds
+        those rows followed by ``halo()``.  op_blocks: per dimension, the 1-D blocks to pack
+        (reserves room for ``update_elements`` with finer tables)."""
         p = cls(term_mats, idx1d, **kw)
-        p._create(deg)
+        p._create(deg, rows=rows, op_blocks=op_blocks)
         return p
+
+    def halo(self):
+        """Table ids (in the plan's index base) of the input elements after a row slice's rows,
+        in the order f holds them (empty for a whole-table plan)."""
+        n = C.c_longlong(0)
+        check(lib().asg_plan_halo(self._handle, None, 0, C.byref(n)))
+        out = np.zeros(max(1, n.value), dtype=np.int32)
+        if n.value:
+            check(lib().asg_plan_halo(self._handle, out.ctypes.data_as(C.POINTER(C.c_int)), n.value, C.byref(n)))
+        return out[:n.value]
+
+    def row_entries(self):
+        """Work entries of each output row (asg_plan_row_entries): the cost partition_rows
+        balances."""
+        out = np.zeros(max(1, self.dof // self.B), dtype=np.int64)
+        check(lib().asg_plan_row_entries(self._handle, out.ctypes.data_as(C.POINTER(C.c_longlong))))
+        return out[:self.dof // self.B]
+
+    def update_elements(self, idx1d, pairs=None):
+        """asg_plan_update_elements: a new element table (and pair list) on the plan's operators.
+        Raises AsgError(ASG_ERR_CAPACITY) when a 1-D index lies beyond the packed operators."""
+        idx = np.ascontiguousarray(np.asarray(idx1d, dtype=np.int32))
+        if idx.ndim != 2 or idx.shape[1] != self.D:
+            raise ValueError("idx1d must be [num_elems, num_dims]")
+        rp_p = cl_p = None
+        keep = [idx]
+        if pairs is not None:
+            rp = np.ascontiguousarray(np.asarray(pairs[0], dtype=np.int64))
+            cl = np.ascontiguousarray(np.asarray(pairs[1], dtype=np.int32))
+            if cl.size == 0:
+                cl = np.zeros(1, dtype=np.int32)
+            keep += [rp, cl]
+            rp_p = rp.ctypes.data_as(C.POINTER(C.c_longlong))
+            cl_p = cl.ctypes.data_as(C.POINTER(C.c_int))
+        check(lib().asg_plan_update_elements(self._handle, idx.shape[0], idx.ctypes.data_as(C.POINTER(C.c_int)),
+                                             rp_p, cl_p))
+        self.N = idx.shape[0]
+        self.dof = self.dof_in = self.N * self.B
+        self._keep[1] = idx
+        self._keep += keep
 
     # ---------------------------------------------------------------------------------
     @property
@@ -151,12 +211,12 @@ class Plan:
         """Device apply on CUDA tensors (float64 or float32); returns y."""
         import torch
 
-        if not (f.is_cuda and f.is_contiguous() and f.numel() == self.dof):
-            raise ValueError("f must be a contiguous CUDA tensor with %d values" % self.dof)
+        if not (f.is_cuda and f.is_contiguous() and f.numel() == self.dof_in):
+            raise ValueError("f must be a contiguous CUDA tensor with %d values" % self.dof_in)
         if y is None:
-            y = torch.empty_like(f)
+            y = torch.empty(self.dof, dtype=f.dtype, device=f.device)
         if y.dtype != f.dtype or not y.is_cuda or y.numel() != self.dof or not y.is_contiguous():
-            raise ValueError("y must match f")
+            raise ValueError("y must be a contiguous CUDA tensor of f's type with %d values" % self.dof)
         s = stream if stream is not None else torch.cuda.current_stream(f.device)
         sp = C.c_void_p(s.cuda_stream)
         if f.dtype == torch.float64:
@@ -224,10 +284,12 @@ class Plan:
     def apply_host(self, f, out=None):
         """Host apply (copies in/out inside the library); numpy float64 or float32."""
         f = np.ascontiguousarray(f)
-        if f.size != self.dof:
-            raise ValueError("f must hold %d values" % self.dof)
+        if f.size != self.dof_in:
+            raise ValueError("f must hold %d values" % self.dof_in)
         if out is None:
-            out = np.empty_like(f)
+            out = np.empty(self.dof, dtype=f.dtype)
+        if out.size != self.dof or out.dtype != f.dtype or not out.flags.c_contiguous:
+            raise ValueError("out must be a contiguous array of f's type with %d values" % self.dof)
         if f.dtype == np.float64:
             check(lib().asg_apply_host_f64(self._handle, f.ctypes.data, out.ctypes.data))
         elif f.dtype == np.float32:

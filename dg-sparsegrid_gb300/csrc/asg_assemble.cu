@@ -72,6 +72,7 @@ using asg::fail;
 extern "C" asg_status asg_assemble_bsr_f64(asg_plan* p, long long* row_ptr, int* cols, double* d_blocks,
                                            long long capacity, long long* num_blocks, void* stream) {
   if (!p || !num_blocks) return fail(ASG_ERR_INVALID, "assemble_bsr: NULL argument");
+  ASG_NOT_SLICE(p, "assemble_bsr");
   if (p->B > 256) return fail(ASG_ERR_UNSUPPORTED, "assemble_bsr: deg^d = %d > 256 (blocks of %d values)", p->B, p->B * p->B);
   const int N = p->N, T = p->T;
   // unique columns per row (sorted) and each block's terms, from the work list

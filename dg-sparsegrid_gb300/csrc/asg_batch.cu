@@ -337,6 +337,7 @@ extern "C" {
 asg_status asg_batch_create(asg_plan* const* plans, int count, asg_batch** out) {
   if (!plans || !out || count < 1) return fail(ASG_ERR_INVALID, "batch_create: bad arguments");
   *out = nullptr;
+  for (int k = 0; k < count; ++k) ASG_NOT_SLICE(plans[k], "batch_create");
   asg_batch* b = new (std::nothrow) asg_batch;
   if (!b) return fail(ASG_ERR_NOMEM, "batch_create: out of host memory");
   struct Cost {

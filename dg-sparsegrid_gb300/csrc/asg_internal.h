@@ -151,6 +151,12 @@ int single_tma_rows_occupancy(int es);
 // The plan object behind the opaque C handle.
 struct asg_plan {
   int D = 0, P = 0, T = 0, N = 0, B = 0;
+  // Output rows: elements [0, N_out) are the rows the kernels write (y holds N_out blocks);
+  // elements [N_out, N) are input-only (a row slice's halo, asg_plan_create_rows).  N_out == N
+  // for a plan over the whole table.
+  int N_out = 0;
+  std::vector<int> elem_global;      // row-slice plans: the table id (0-based) of each element
+  int index_base = 0;                // base of the caller's index arrays (0 or 1)
   int structure = 0;
   double drop_tol = 0.0;
   int kernel_kind = 0;
@@ -222,3 +228,10 @@ struct asg_plan {
   size_t d_io_bytes = 0;
   cudaStream_t stream = nullptr;
 };
+
+// A row-slice plan (asg_plan_create_ex with a narrower row range): forward apply only.
+inline bool asg_is_slice(const asg_plan* p) { return p && p->N_out != p->N; }
+#define ASG_NOT_SLICE(p, what)                                                                   \
+  do {                                                                                           \
+    if (asg_is_slice(p)) return ::asg::fail(ASG_ERR_UNSUPPORTED, "%s: not for a row-slice plan", what); \
+  } while (0)

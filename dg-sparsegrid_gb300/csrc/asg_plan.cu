@@ -30,8 +30,12 @@ asg_status cuda_fail(cudaError_t e, const char* what) {
 
 namespace {
 
+// Replaces *dst (freed first: finalize runs again when a plan's table changes) by a device
+// copy of src, or leaves it NULL for an empty src.
 template <typename X>
 asg_status upload(X** dst, const std::vector<X>& src) {
+  cudaFree(*dst);
+  *dst = nullptr;
   if (src.empty()) return ASG_OK;
   ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(dst), src.size() * sizeof(X)));
   ASG_CUDA(cudaMemcpy(*dst, src.data(), src.size() * sizeof(X), cudaMemcpyHostToDevice));
@@ -167,7 +171,7 @@ asg_status upload_ops(asg_plan* p) {
 // buffers), then 3 and 5 (straight into the natural tile), each group in work-list order.
 // Expects p->ed filled.
 asg_status build_streams(asg_plan* p, int nsm) {
-  const int N = p->N;
+  const int N = p->N_out;
   const int occ = stream_occupancy();
   if (occ <= 0) return fail(ASG_ERR_CUDA, "streaming apply kernel cannot be resident");
   const int G = std::max(1, std::min(N, occ * nsm));
@@ -231,10 +235,39 @@ asg_status build_streams(asg_plan* p, int nsm) {
   return ASG_OK;
 }
 
+// What a plan derives from its table on first use (the transpose, gradient targets, the fused
+// solve's partition) and the tuner's choice: dropped when the table changes.
+void drop_derived(asg_plan* p) {
+  if (p->tr) {
+    free_plan(p->tr);
+    p->tr = nullptr;
+  }
+  for (void** d : {reinterpret_cast<void**>(&p->d_g_ptr), reinterpret_cast<void**>(&p->d_g_contrib),
+                   reinterpret_cast<void**>(&p->d_g_tgt), reinterpret_cast<void**>(&p->d_ldg),
+                   reinterpret_cast<void**>(&p->d_gptrs), reinterpret_cast<void**>(&p->d_g_items),
+                   reinterpret_cast<void**>(&p->d_g_partial), reinterpret_cast<void**>(&p->d_g_counter)}) {
+    cudaFree(*d);
+    *d = nullptr;
+  }
+  p->g_ptr.clear();
+  p->g_contrib.clear();
+  p->g_tgt.clear();
+  p->g_items.clear();
+  for (int k = 0; k < 2; ++k) {
+    cudaFree(p->d_fz_int[k]);
+    cudaFree(p->d_fz_items[k]);
+    p->d_fz_int[k] = nullptr;
+    p->d_fz_items[k] = nullptr;
+    p->fz_G[k] = p->fz_max_rows[k] = p->fz_max_slots[k] = 0;
+    p->tuned_kind[k] = -1;
+  }
+}
+
 // Kernel choice, launch order, single-mode descriptors and every upload; shared by a plan
 // and its transpose.  Expects idx1d, op_nb, active, op_off, row_ptr, ent and h64 filled.
-asg_status finalize(asg_plan* p) {
-  const int D = p->D, P = p->P, T = p->T, N = p->N;
+// Output rows are elements [0, N_out); `ops` false keeps the device operator copies.
+asg_status finalize(asg_plan* p, bool ops) {
+  const int D = p->D, P = p->P, T = p->T, N = p->N, NO = p->N_out;
   const long long B = p->B;
   const bool detect = p->structure == ASG_STRUCT_DETECT;
   std::vector<int>& ent = p->ent;
@@ -256,8 +289,8 @@ asg_status finalize(asg_plan* p) {
   p->ed.clear();
   if (single) {
     // rows launch longest first so the last wave is made of short rows
-    p->row_order.resize(N);
-    for (int i = 0; i < N; ++i) p->row_order[i] = i;
+    p->row_order.resize(NO);
+    for (int i = 0; i < NO; ++i) p->row_order[i] = i;
     std::stable_sort(p->row_order.begin(), p->row_order.end(), [&](int x, int y) {
       return p->row_ptr[x + 1] - p->row_ptr[x] > p->row_ptr[y + 1] - p->row_ptr[y];
     });
@@ -283,23 +316,23 @@ asg_status finalize(asg_plan* p) {
     p->cta_rows[k].clear();
   }
   int nsm = 0;
-  if (single && P == 4 && B == 4096 && N > 0) {
+  if (single && P == 4 && B == 4096 && NO > 0) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return cuda_fail(e, "device attributes");
   }
-  if (single && P == 4 && B == 4096 && N > 0) {
+  if (single && P == 4 && B == 4096 && NO > 0) {
     for (int k = 0; k < 2; ++k) {
       const int occ = single_tma_rows_occupancy(k == 0 ? 8 : 4);
       if (occ <= 0) return fail(ASG_ERR_CUDA, "persistent single-mode kernel cannot be resident");
-      const int G = std::max(1, std::min(N, occ * nsm));
+      const int G = std::max(1, std::min(NO, occ * nsm));
       std::vector<std::vector<int>> lists(G);
       std::vector<std::pair<long long, int>> heap;  // (load, cta) min-heap
       for (int c = 0; c < G; ++c) heap.push_back({0, c});
       auto cmp = [](const std::pair<long long, int>& x, const std::pair<long long, int>& y) { return x > y; };
-      std::vector<int> by_cost(N);
-      for (int i = 0; i < N; ++i) by_cost[i] = i;
+      std::vector<int> by_cost(NO);
+      for (int i = 0; i < NO; ++i) by_cost[i] = i;
       std::stable_sort(by_cost.begin(), by_cost.end(), [&](int x, int y) {
         return p->row_ptr[x + 1] - p->row_ptr[x] > p->row_ptr[y + 1] - p->row_ptr[y];
       });
@@ -319,7 +352,7 @@ asg_status finalize(asg_plan* p) {
   }
   p->ws.clear();
   p->ws_stride = p->ws_ctas = 0;
-  if (single && P == 4 && B == 4096 && N > 0) {
+  if (single && P == 4 && B == 4096 && NO > 0) {
     asg_status sst = build_streams(p, nsm);
     if (sst) return sst;
   }
@@ -330,7 +363,7 @@ asg_status finalize(asg_plan* p) {
     if ((st = upload(&p->d_cta_rows[k], p->cta_rows[k]))) return st;
   }
   if ((st = upload(&p->d_row_order, p->row_order))) return st;
-  if ((st = upload_ops(p))) return st;
+  if (ops && (st = upload_ops(p))) return st;
   if ((st = upload(&p->d_idx1d, p->idx1d))) return st;
   if ((st = upload(&p->d_op_nb, p->op_nb))) return st;
   if ((st = upload(&p->d_active, p->active))) return st;
@@ -338,7 +371,7 @@ asg_status finalize(asg_plan* p) {
   if ((st = upload(&p->d_row_ptr, p->row_ptr))) return st;
   if ((st = upload(&p->d_ent, p->ent))) return st;
   if ((st = upload(&p->d_ed, p->ed))) return st;
-  ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_err), sizeof(int)));
+  if (!p->d_err) ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_err), sizeof(int)));
   ASG_CUDA(cudaMemset(p->d_err, 0, sizeof(int)));
   return ASG_OK;
 }
@@ -395,7 +428,8 @@ asg_status build_transpose(asg_plan* p) {
     for (int j = 0; j < N; ++j)
       std::stable_sort(t->ent.begin() + t->row_ptr[j], t->ent.begin() + t->row_ptr[j + 1],
                        [](int x, int y) { return (x & 15) < (y & 15); });
-  asg_status st = finalize(t);
+  t->N_out = t->N;
+  asg_status st = finalize(t, true);
   if (st) {
     free_plan(t);
     return st;
@@ -494,6 +528,7 @@ asg_status build_grad(asg_plan* p) {
 template <typename T>
 asg_status grad_ops(asg_plan* p, const T* f, const T* r, T* const* G, const int* ldg, void* stream) {
   if (!p || !G || !ldg) return fail(ASG_ERR_INVALID, "grad_ops: NULL argument");
+  ASG_NOT_SLICE(p, "grad_ops");
   asg_status st = check_ptr(f, "f");
   if (st) return st;
   if ((st = check_ptr(r, "r"))) return st;
@@ -552,7 +587,7 @@ ApplyArgs<T> make_args(const asg_plan* p, const T* f, T* y, const T* ops) {
   a.row_ptr = p->d_row_ptr;
   a.ent = p->d_ent;
   a.active = p->d_active;
-  a.N = p->N;
+  a.N = p->N_out;  // rows the kernels write
   a.D = p->D;
   a.B = p->B;
   a.nterms = p->T;
@@ -621,8 +656,8 @@ template <typename T>
 asg_status apply_host(asg_plan* p, const T* hf, T* hy) {
   if (!p) return fail(ASG_ERR_INVALID, "apply_host: NULL plan");
   if (!hf || !hy) return fail(ASG_ERR_INVALID, "apply_host: NULL host buffer");
-  const size_t n = static_cast<size_t>(p->N) * p->B;
-  const size_t need = 2 * n * sizeof(T) + 256;
+  const size_t n = static_cast<size_t>(p->N) * p->B, ny = static_cast<size_t>(p->N_out) * p->B;
+  const size_t need = (n + ny) * sizeof(T) + 256;
   if (!p->stream) ASG_CUDA(cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking));
   if (p->d_io_bytes < need) {
     cudaFree(p->d_io);
@@ -647,7 +682,7 @@ asg_status apply_host(asg_plan* p, const T* hf, T* hy) {
   ASG_CUDA(cudaMemcpyAsync(df, hf, n * sizeof(T), cudaMemcpyHostToDevice, p->stream));
   asg_status st = apply_dev<T>(p, df, ky, p->stream);
   if (st) return st;
-  if (ky == dy) ASG_CUDA(cudaMemcpyAsync(hy, dy, n * sizeof(T), cudaMemcpyDeviceToHost, p->stream));
+  if (ky == dy) ASG_CUDA(cudaMemcpyAsync(hy, dy, ny * sizeof(T), cudaMemcpyDeviceToHost, p->stream));
   ASG_CUDA(cudaStreamSynchronize(p->stream));
   return ASG_OK;
 }
@@ -663,6 +698,323 @@ bool small_plan_args(const asg_plan* p, ApplyArgs<T>* out) {
 }
 template bool small_plan_args<float>(const asg_plan*, ApplyArgs<float>*);
 template bool small_plan_args<double>(const asg_plan*, ApplyArgs<double>*);
+
+namespace {
+
+// Checks of a plan description shared by plan creation and the element-table update (the isok
+// checks of kron_multd.m:7-12,24-28 and the asserts of apply_A.m).
+asg_status check_desc(const asg_plan_desc* desc) {
+  const int D = desc->num_dims, P = desc->deg, T = desc->num_terms, N = desc->num_elems;
+  if (D < 1 || D > kMaxDims)
+    return fail(D < 1 ? ASG_ERR_INVALID : ASG_ERR_UNSUPPORTED, "kron_multd: invalid nkron=%d (1..%d supported)", D,
+                kMaxDims);
+  if (P < 1 || P > 8) return fail(P < 1 ? ASG_ERR_INVALID : ASG_ERR_UNSUPPORTED, "deg=%d outside 1..8", P);
+  if (T < 1 || T > kMaxTerms)
+    return fail(T < 1 ? ASG_ERR_INVALID : ASG_ERR_UNSUPPORTED, "num_terms=%d outside 1..%d", T, kMaxTerms);
+  if (N < 0 || N >= (1 << 27)) return fail(ASG_ERR_UNSUPPORTED, "num_elems=%d outside 0..2^27-1", N);
+  long long B = 1;
+  for (int k = 0; k < D; ++k) B *= P;
+  if (B > kMaxBlock) return fail(ASG_ERR_UNSUPPORTED, "deg^d=%lld exceeds %d", B, kMaxBlock);
+  if (desc->index_base != 0 && desc->index_base != 1) return fail(ASG_ERR_INVALID, "index_base must be 0 or 1");
+  if (desc->structure != ASG_STRUCT_NONE && desc->structure != ASG_STRUCT_DETECT)
+    return fail(ASG_ERR_INVALID, "unknown structure mode %d", desc->structure);
+  if (!(desc->drop_tol >= 0.0) || desc->drop_tol > 1e-3) return fail(ASG_ERR_INVALID, "drop_tol must be in [0, 1e-3]");
+  if (N > 0 && (!desc->idx1d || !desc->ops || !desc->op_ld)) return fail(ASG_ERR_INVALID, "plan_create: NULL array");
+  return ASG_OK;
+}
+
+// 0-based 1-D indices of a table; nb_dim[m] = 1 + the largest index in dimension m.
+asg_status set_table(asg_plan* p, const int* idx1d, int base, std::vector<int>& nb_dim) {
+  const int D = p->D, N = p->N;
+  p->idx1d.resize(static_cast<size_t>(N) * D);
+  nb_dim.assign(D, 0);
+  for (long long i = 0; i < static_cast<long long>(N) * D; ++i) {
+    const int v = idx1d[i] - base;
+    if (v < 0) return fail(ASG_ERR_INVALID, "idx1d[%lld]=%d below index base %d", i, idx1d[i], base);
+    p->idx1d[i] = v;
+    nb_dim[i % D] = std::max(nb_dim[i % D], v + 1);
+  }
+  return ASG_OK;
+}
+
+// The listed pairs (validated, 0-based), or all N^2 pairs when row_ptr is NULL.
+asg_status set_pairs(asg_plan* p, const long long* row_ptr, const int* cols, int base) {
+  const int N = p->N;
+  p->pr_ptr.clear();
+  p->pr_col.clear();
+  if (!row_ptr) {
+    p->all_pairs = true;
+    p->pairs = static_cast<long long>(N) * N;
+    return ASG_OK;
+  }
+  if (row_ptr[0] != 0) return fail(ASG_ERR_INVALID, "row_ptr[0] must be 0");
+  for (int i = 0; i < N; ++i)
+    if (row_ptr[i + 1] < row_ptr[i]) return fail(ASG_ERR_INVALID, "row_ptr not monotone at %d", i);
+  if (row_ptr[N] > 0 && !cols) return fail(ASG_ERR_INVALID, "cols is NULL");
+  for (long long q = 0; q < row_ptr[N]; ++q) {
+    const int j = cols[q] - base;
+    if (j < 0 || j >= N) return fail(ASG_ERR_INVALID, "cols[%lld]=%d outside the element table", q, cols[q]);
+  }
+  p->all_pairs = false;
+  p->pairs = row_ptr[N];
+  p->pr_ptr.assign(row_ptr, row_ptr + N + 1);
+  p->pr_col.resize(row_ptr[N]);
+  for (long long q = 0; q < row_ptr[N]; ++q) p->pr_col[q] = cols[q] - base;
+  return ASG_OK;
+}
+
+// Operator validation and structure analysis (identity factors, zero p x p blocks): fills
+// op_nb (the packed extent: nb_dim blocks per side), active and zero_blk.
+asg_status analyse_ops(asg_plan* p, const asg_plan_desc* desc, const std::vector<int>& nb_dim) {
+  const int D = p->D, P = p->P, T = p->T, N = p->N;
+  p->op_nb.assign(static_cast<size_t>(T) * D, 0);
+  p->op_off.assign(static_cast<size_t>(T) * D, -1);
+  p->active.assign(T, 0u);
+  std::vector<std::vector<uint8_t>>& zero_blk = p->zero_blk;
+  zero_blk.assign(static_cast<size_t>(T) * D, {});
+  const bool detect = desc->structure == ASG_STRUCT_DETECT;
+  for (int t = 0; t < T; ++t)
+    for (int m = 0; m < D; ++m) {
+      const int tm = t * D + m;
+      const int nb = nb_dim[m];
+      p->op_nb[tm] = nb;
+      if (N == 0) continue;
+      const double* op = desc->ops[tm];
+      const int ld = desc->op_ld[tm];
+      if (!op) return fail(ASG_ERR_INVALID, "operator (term %d, dim %d) is NULL", t, m);
+      if (ld < nb * P)
+        return fail(ASG_ERR_INVALID, "operator (term %d, dim %d): ld=%d < deg*max(idx1d)=%d", t, m, ld, nb * P);
+      const int n = nb * P;
+      double maxabs = 0.0;
+      for (int c = 0; c < n; ++c)
+        for (int r = 0; r < n; ++r) {
+          const double v = op[static_cast<long long>(c) * ld + r];
+          if (!std::isfinite(v))
+            return fail(ASG_ERR_INVALID, "operator (term %d, dim %d) has a non-finite entry at (%d,%d)", t, m, r, c);
+          maxabs = std::max(maxabs, std::fabs(v));
+        }
+      bool ident = false;
+      if (detect) {
+        const double thr = desc->drop_tol * maxabs;
+        ident = true;
+        for (int c = 0; c < n && ident; ++c)
+          for (int r = 0; r < n; ++r)
+            if (std::fabs(op[static_cast<long long>(c) * ld + r] - (r == c ? 1.0 : 0.0)) > thr) {
+              ident = false;
+              break;
+            }
+        if (!ident) {
+          auto& zb = zero_blk[tm];
+          zb.assign(static_cast<size_t>(nb) * nb, 1);
+          for (int c = 0; c < n; ++c)
+            for (int r = 0; r < n; ++r)
+              if (std::fabs(op[static_cast<long long>(c) * ld + r]) > thr) zb[static_cast<size_t>(r / P) * nb + c / P] = 0;
+        }
+      }
+      if (!ident) p->active[t] |= 1u << m;
+    }
+  long long off = 0;
+  for (int t = 0; t < T; ++t)
+    for (int m = 0; m < D; ++m) {
+      const int tm = t * D + m;
+      if (N == 0 || !((p->active[t] >> m) & 1u)) continue;
+      p->op_off[tm] = off;
+      off += static_cast<long long>(p->op_nb[tm]) * p->op_nb[tm] * P * P;
+    }
+  p->packed_elems = off;
+  return ASG_OK;
+}
+
+// Work entries of rows [r0, r1) (the reference work model, or the structured one under
+// ASG_STRUCT_DETECT): p->row_ptr over those rows (r1 - r0 + 1 values), p->ent with table
+// column ids.  Summation order: a row's terms in order, each term's columns in list order.
+void build_work(asg_plan* p, int r0, int r1) {
+  const int D = p->D, T = p->T, N = p->N;
+  const bool detect = p->structure == ASG_STRUCT_DETECT;
+  p->row_ptr.assign(static_cast<size_t>(r1 - r0) + 1, 0);
+  std::vector<int>& ent = p->ent;
+  ent.clear();
+  auto blk_zero = [&](int t, int m, int i, int j) {
+    const auto& zb = p->zero_blk[t * D + m];
+    return !zb.empty() && zb[static_cast<size_t>(p->idx1d[i * D + m]) * p->op_nb[t * D + m] + p->idx1d[j * D + m]];
+  };
+  auto keep = [&](int t, int i, int j) {
+    for (int m = 0; m < D; ++m) {
+      if ((p->active[t] >> m) & 1u) {
+        if (blk_zero(t, m, i, j)) return false;
+      } else if (p->idx1d[i * D + m] != p->idx1d[j * D + m]) {
+        return false;
+      }
+    }
+    return true;
+  };
+  if (!detect) {
+    for (int t = 0; t < T; ++t) p->active[t] = (1u << D) - 1u;
+    for (int i = r0; i < r1; ++i) {
+      const long long q0 = p->all_pairs ? 0 : p->pr_ptr[i];
+      const long long q1 = p->all_pairs ? N : p->pr_ptr[i + 1];
+      for (long long q = q0; q < q1; ++q) {
+        const int j = p->all_pairs ? static_cast<int>(q) : p->pr_col[q];
+        for (int t = 0; t < T; ++t) ent.push_back((j << 4) | t);
+      }
+      p->row_ptr[i - r0 + 1] = static_cast<long long>(ent.size());
+    }
+    return;
+  }
+  // group candidate columns by the 1-D indices of the term's identity dimensions
+  std::vector<std::map<std::vector<int>, std::vector<int>>> groups(T);
+  if (p->all_pairs) {
+    for (int t = 0; t < T; ++t)
+      for (int e = 0; e < N; ++e) {
+        std::vector<int> key;
+        for (int m = 0; m < D; ++m)
+          if (!((p->active[t] >> m) & 1u)) key.push_back(p->idx1d[e * D + m]);
+        groups[t][key].push_back(e);
+      }
+  }
+  for (int i = r0; i < r1; ++i) {
+    for (int t = 0; t < T; ++t) {
+      if (p->all_pairs) {
+        std::vector<int> key;
+        for (int m = 0; m < D; ++m)
+          if (!((p->active[t] >> m) & 1u)) key.push_back(p->idx1d[i * D + m]);
+        for (int j : groups[t][key])
+          if (keep(t, i, j)) ent.push_back((j << 4) | t);
+      } else {
+        for (long long q = p->pr_ptr[i]; q < p->pr_ptr[i + 1]; ++q) {
+          const int j = p->pr_col[q];
+          if (keep(t, i, j)) ent.push_back((j << 4) | t);
+        }
+      }
+    }
+    p->row_ptr[i - r0 + 1] = static_cast<long long>(ent.size());
+  }
+}
+
+// Renumbers a row slice's plan: elements become the rows r0..r1-1 (ids 0..R-1) followed by the
+// halo, every other element the rows' entries read, in table order (ids R..R+H-1; rows without
+// entries).  Expects build_work(p, r0, r1) done on the table's ids.
+void compact_slice(asg_plan* p, int r0, int r1) {
+  const int D = p->D, R = r1 - r0, Nt = p->N;
+  std::vector<int> id(Nt, -1);
+  for (int i = r0; i < r1; ++i) id[i] = i - r0;
+  std::vector<uint8_t> used(Nt, 0);
+  for (int e : p->ent) used[e >> 4] = 1;
+  p->elem_global.clear();
+  for (int i = r0; i < r1; ++i) p->elem_global.push_back(i);
+  for (int j = 0; j < Nt; ++j)
+    if (used[j] && id[j] < 0) {
+      id[j] = static_cast<int>(p->elem_global.size());
+      p->elem_global.push_back(j);
+    }
+  const int Ne = static_cast<int>(p->elem_global.size());
+  std::vector<int> idx(static_cast<size_t>(Ne) * D);
+  for (int e = 0; e < Ne; ++e)
+    for (int m = 0; m < D; ++m) idx[static_cast<size_t>(e) * D + m] = p->idx1d[static_cast<size_t>(p->elem_global[e]) * D + m];
+  p->idx1d.swap(idx);
+  for (int& e : p->ent) e = (id[e >> 4] << 4) | (e & 15);
+  p->row_ptr.resize(static_cast<size_t>(Ne) + 1, p->row_ptr[R]);  // halo elements: no entries
+  long long listed = 0;
+  for (int i = r0; i < r1; ++i) listed += p->all_pairs ? Nt : p->pr_ptr[i + 1] - p->pr_ptr[i];
+  p->pairs = listed;
+  p->all_pairs = false;  // listed pairs are not kept for a slice (no adjoint or gradients)
+  p->pr_ptr.clear();
+  p->pr_col.clear();
+  p->N = Ne;
+  p->N_out = R;
+}
+
+}  // namespace
+
+// Plan over rows [r0, r1) of the table (r0 = 0, r1 = num_elems: the whole table); op_blocks
+// (may be NULL) widens the packed operator extent per dimension.
+asg_status create_plan(const asg_plan_desc* desc, int r0, int r1, const int* op_blocks, asg_plan** out) {
+  if (!desc || !out) return fail(ASG_ERR_INVALID, "plan_create: NULL argument");
+  *out = nullptr;
+  asg_status st = check_desc(desc);
+  if (st) return st;
+  const int N = desc->num_elems;
+  if (r0 < 0 || r1 < r0 || r1 > N) return fail(ASG_ERR_INVALID, "plan_create_ex: rows [%d, %d) outside 0..%d", r0, r1, N);
+  const int base = desc->index_base;
+  asg_plan* p = new (std::nothrow) asg_plan;
+  if (!p) return fail(ASG_ERR_NOMEM, "plan_create: out of host memory");
+  p->D = desc->num_dims;
+  p->P = desc->deg;
+  p->T = desc->num_terms;
+  p->N = N;
+  p->N_out = N;
+  long long B = 1;
+  for (int k = 0; k < p->D; ++k) B *= p->P;
+  p->B = static_cast<int>(B);
+  p->structure = desc->structure;
+  p->drop_tol = desc->drop_tol;
+  p->index_base = base;
+  auto bail = [&](asg_status s) {
+    free_device(p);
+    delete p;
+    return s;
+  };
+  std::vector<int> nb_dim;
+  if ((st = set_table(p, desc->idx1d, base, nb_dim))) return bail(st);
+  if (op_blocks)
+    for (int m = 0; m < p->D; ++m) {
+      if (op_blocks[m] < 0 || op_blocks[m] > (1 << 20))
+        return bail(fail(ASG_ERR_INVALID, "plan_create_ex: op_blocks[%d]=%d", m, op_blocks[m]));
+      nb_dim[m] = std::max(nb_dim[m], op_blocks[m]);
+    }
+  if ((st = analyse_ops(p, desc, nb_dim))) return bail(st);
+  if ((st = set_pairs(p, desc->row_ptr, desc->cols, base))) return bail(st);
+  build_work(p, r0, r1);
+  const bool slice = r0 != 0 || r1 != N;
+  if (slice) compact_slice(p, r0, r1);
+  pack_host(p, desc->ops, desc->op_ld);
+  double pd1 = 1.0;
+  for (int k = 0; k <= p->D; ++k) pd1 *= p->P;
+  p->flops_dense = static_cast<double>(p->pairs) * p->T * p->D * 2.0 * pd1;
+  if ((st = finalize(p, true))) return bail(st);
+  *out = p;
+  return ASG_OK;
+}
+
+// A new element table and pair list on a plan's operators (the plan rebuild after adapt.m's
+// coarsening and refinement, adapt.m:414-437, when the operators keep their values): the
+// structure classes, packed operators and their device copies are kept; the work list, the
+// launch data and everything derived from the table are rebuilt.
+asg_status update_elements(asg_plan* p, int num_elems, const int* idx1d, const long long* row_ptr, const int* cols) {
+  if (!p) return fail(ASG_ERR_INVALID, "plan_update_elements: NULL plan");
+  if (p->N_out != p->N) return fail(ASG_ERR_UNSUPPORTED, "plan_update_elements: not for a row-slice plan");
+  if (num_elems < 0 || num_elems >= (1 << 27)) return fail(ASG_ERR_UNSUPPORTED, "num_elems=%d outside 0..2^27-1", num_elems);
+  if (num_elems > 0 && !idx1d) return fail(ASG_ERR_INVALID, "plan_update_elements: NULL idx1d");
+  const int D = p->D;
+  // validate against the packed extent before touching the plan
+  for (long long i = 0; i < static_cast<long long>(num_elems) * D; ++i) {
+    const int v = idx1d[i] - p->index_base;
+    if (v < 0) return fail(ASG_ERR_INVALID, "idx1d[%lld]=%d below index base %d", i, idx1d[i], p->index_base);
+    const int m = static_cast<int>(i % D);
+    for (int t = 0; t < p->T; ++t)
+      if (v >= p->op_nb[t * D + m])
+        return fail(ASG_ERR_CAPACITY,
+                    "plan_update_elements: 1-D index %d in dimension %d beyond the plan's operators (%d blocks); "
+                    "create a new plan", v + p->index_base, m, p->op_nb[t * D + m]);
+  }
+  asg_plan tmp;  // validated pair list first, so a failure leaves the plan unchanged
+  tmp.N = num_elems;
+  asg_status st = set_pairs(&tmp, row_ptr, cols, p->index_base);
+  if (st) return st;
+  std::vector<int> nb_dim;
+  p->N = p->N_out = num_elems;
+  set_table(p, idx1d, p->index_base, nb_dim);
+  p->all_pairs = tmp.all_pairs;
+  p->pairs = tmp.pairs;
+  p->pr_ptr.swap(tmp.pr_ptr);
+  p->pr_col.swap(tmp.pr_col);
+  build_work(p, 0, num_elems);
+  double pd1 = 1.0;
+  for (int k = 0; k <= D; ++k) pd1 *= p->P;
+  p->flops_dense = static_cast<double>(p->pairs) * p->T * D * 2.0 * pd1;
+  drop_derived(p);
+  return finalize(p, false);
+}
 
 }  // namespace asg
 
@@ -750,192 +1102,35 @@ asg_status asg_last_error(char* buf, size_t len) {
 
 asg_status asg_plan_create(const asg_plan_desc* desc, asg_plan** out) {
   if (!desc || !out) return fail(ASG_ERR_INVALID, "plan_create: NULL argument");
-  *out = nullptr;
-  const int D = desc->num_dims, P = desc->deg, T = desc->num_terms, N = desc->num_elems;
-  if (D < 1 || D > asg::kMaxDims)
-    return fail(D < 1 ? ASG_ERR_INVALID : ASG_ERR_UNSUPPORTED, "kron_multd: invalid nkron=%d (1..%d supported)", D,
-                asg::kMaxDims);
-  if (P < 1 || P > 8) return fail(P < 1 ? ASG_ERR_INVALID : ASG_ERR_UNSUPPORTED, "deg=%d outside 1..8", P);
-  if (T < 1 || T > asg::kMaxTerms)
-    return fail(T < 1 ? ASG_ERR_INVALID : ASG_ERR_UNSUPPORTED, "num_terms=%d outside 1..%d", T, asg::kMaxTerms);
-  if (N < 0 || N >= (1 << 27)) return fail(ASG_ERR_UNSUPPORTED, "num_elems=%d outside 0..2^27-1", N);
-  long long B = 1;
-  for (int k = 0; k < D; ++k) B *= P;
-  if (B > asg::kMaxBlock) return fail(ASG_ERR_UNSUPPORTED, "deg^d=%lld exceeds %d", B, asg::kMaxBlock);
-  if (desc->index_base != 0 && desc->index_base != 1) return fail(ASG_ERR_INVALID, "index_base must be 0 or 1");
-  if (desc->structure != ASG_STRUCT_NONE && desc->structure != ASG_STRUCT_DETECT)
-    return fail(ASG_ERR_INVALID, "unknown structure mode %d", desc->structure);
-  if (!(desc->drop_tol >= 0.0) || desc->drop_tol > 1e-3) return fail(ASG_ERR_INVALID, "drop_tol must be in [0, 1e-3]");
-  if (N > 0 && (!desc->idx1d || !desc->ops || !desc->op_ld)) return fail(ASG_ERR_INVALID, "plan_create: NULL array");
-  const int base = desc->index_base;
+  return asg::create_plan(desc, 0, desc->num_elems, nullptr, out);
+}
 
-  asg_plan* p = new (std::nothrow) asg_plan;
-  if (!p) return fail(ASG_ERR_NOMEM, "plan_create: out of host memory");
-  p->D = D;
-  p->P = P;
-  p->T = T;
-  p->N = N;
-  p->B = static_cast<int>(B);
-  p->structure = desc->structure;
-  p->drop_tol = desc->drop_tol;
+asg_status asg_plan_create_ex(const asg_plan_desc* desc, const asg_plan_ext* ext, asg_plan** out) {
+  if (!desc || !out) return fail(ASG_ERR_INVALID, "plan_create_ex: NULL argument");
+  if (!ext) return asg::create_plan(desc, 0, desc->num_elems, nullptr, out);
+  return asg::create_plan(desc, ext->row_begin, ext->row_end, ext->op_blocks, out);
+}
 
-  auto bail = [&](asg_status st) {
-    asg::free_device(p);
-    delete p;
-    return st;
-  };
-
-  // ---- 1-D indices ------------------------------------------------------------------
-  p->idx1d.resize(static_cast<size_t>(N) * D);
-  std::vector<int> nb_dim(D, 0);
-  for (long long i = 0; i < static_cast<long long>(N) * D; ++i) {
-    const int v = desc->idx1d[i] - base;
-    if (v < 0) return bail(fail(ASG_ERR_INVALID, "idx1d[%lld]=%d below index base %d", i, desc->idx1d[i], base));
-    p->idx1d[i] = v;
-    nb_dim[i % D] = std::max(nb_dim[i % D], v + 1);
-  }
-  // ---- operators: validate, analyse structure ----------------------------------------
-  p->op_nb.assign(static_cast<size_t>(T) * D, 0);
-  p->op_off.assign(static_cast<size_t>(T) * D, -1);
-  p->active.assign(T, 0u);
-  std::vector<std::vector<uint8_t>>& zero_blk = p->zero_blk;
-  zero_blk.assign(static_cast<size_t>(T) * D, {});
-  const bool detect = desc->structure == ASG_STRUCT_DETECT;
-  for (int t = 0; t < T; ++t)
-    for (int m = 0; m < D; ++m) {
-      const int tm = t * D + m;
-      const int nb = nb_dim[m];
-      p->op_nb[tm] = nb;
-      if (N == 0) continue;
-      const double* op = desc->ops[tm];
-      const int ld = desc->op_ld[tm];
-      if (!op) return bail(fail(ASG_ERR_INVALID, "operator (term %d, dim %d) is NULL", t, m));
-      if (ld < nb * P)
-        return bail(fail(ASG_ERR_INVALID, "operator (term %d, dim %d): ld=%d < deg*max(idx1d)=%d", t, m, ld, nb * P));
-      const int n = nb * P;
-      double maxabs = 0.0;
-      for (int c = 0; c < n; ++c)
-        for (int r = 0; r < n; ++r) {
-          const double v = op[static_cast<long long>(c) * ld + r];
-          if (!std::isfinite(v))
-            return bail(fail(ASG_ERR_INVALID, "operator (term %d, dim %d) has a non-finite entry at (%d,%d)", t, m, r, c));
-          maxabs = std::max(maxabs, std::fabs(v));
-        }
-      bool ident = false;
-      if (detect) {
-        const double thr = desc->drop_tol * maxabs;
-        ident = true;
-        for (int c = 0; c < n && ident; ++c)
-          for (int r = 0; r < n; ++r)
-            if (std::fabs(op[static_cast<long long>(c) * ld + r] - (r == c ? 1.0 : 0.0)) > thr) {
-              ident = false;
-              break;
-            }
-        if (!ident) {
-          auto& zb = zero_blk[tm];
-          zb.assign(static_cast<size_t>(nb) * nb, 1);
-          for (int c = 0; c < n; ++c)
-            for (int r = 0; r < n; ++r)
-              if (std::fabs(op[static_cast<long long>(c) * ld + r]) > thr) zb[static_cast<size_t>(r / P) * nb + c / P] = 0;
-        }
-      }
-      if (!ident) p->active[t] |= 1u << m;
-    }
-  // ---- pair list ----------------------------------------------------------------------
-  const bool all_pairs = desc->row_ptr == nullptr;
-  if (!all_pairs) {
-    if (desc->row_ptr[0] != 0) return bail(fail(ASG_ERR_INVALID, "row_ptr[0] must be 0"));
-    for (int i = 0; i < N; ++i)
-      if (desc->row_ptr[i + 1] < desc->row_ptr[i]) return bail(fail(ASG_ERR_INVALID, "row_ptr not monotone at %d", i));
-    if (desc->row_ptr[N] > 0 && !desc->cols) return bail(fail(ASG_ERR_INVALID, "cols is NULL"));
-    for (long long q = 0; q < desc->row_ptr[N]; ++q) {
-      const int j = desc->cols[q] - base;
-      if (j < 0 || j >= N) return bail(fail(ASG_ERR_INVALID, "cols[%lld]=%d outside the element table", q, desc->cols[q]));
-    }
-    p->pairs = desc->row_ptr[N];
-    p->all_pairs = false;
-    p->pr_ptr.assign(desc->row_ptr, desc->row_ptr + N + 1);
-    p->pr_col.resize(desc->row_ptr[N]);
-    for (long long q = 0; q < desc->row_ptr[N]; ++q) p->pr_col[q] = desc->cols[q] - base;
-  } else {
-    p->pairs = static_cast<long long>(N) * N;
-  }
-  // ---- work entries ---------------------------------------------------------------------
-  p->row_ptr.assign(N + 1, 0);
-  std::vector<int>& ent = p->ent;
-  auto blk_zero = [&](int t, int m, int i, int j) {
-    const auto& zb = zero_blk[t * D + m];
-    return !zb.empty() && zb[static_cast<size_t>(p->idx1d[i * D + m]) * p->op_nb[t * D + m] + p->idx1d[j * D + m]];
-  };
-  auto keep = [&](int t, int i, int j) {
-    for (int m = 0; m < D; ++m) {
-      if ((p->active[t] >> m) & 1u) {
-        if (blk_zero(t, m, i, j)) return false;
-      } else if (p->idx1d[i * D + m] != p->idx1d[j * D + m]) {
-        return false;
-      }
-    }
-    return true;
-  };
-  if (!detect) {
-    for (int t = 0; t < T; ++t) p->active[t] = (1u << D) - 1u;
-    for (int i = 0; i < N; ++i) {
-      const long long q0 = all_pairs ? 0 : desc->row_ptr[i];
-      const long long q1 = all_pairs ? N : desc->row_ptr[i + 1];
-      for (long long q = q0; q < q1; ++q) {
-        const int j = all_pairs ? static_cast<int>(q) : desc->cols[q] - base;
-        for (int t = 0; t < T; ++t) ent.push_back((j << 4) | t);
-      }
-      p->row_ptr[i + 1] = static_cast<long long>(ent.size());
-    }
-  } else {
-    // group candidate columns by the 1-D indices of the term's identity dimensions
-    std::vector<std::map<std::vector<int>, std::vector<int>>> groups(T);
-    if (all_pairs) {
-      for (int t = 0; t < T; ++t)
-        for (int e = 0; e < N; ++e) {
-          std::vector<int> key;
-          for (int m = 0; m < D; ++m)
-            if (!((p->active[t] >> m) & 1u)) key.push_back(p->idx1d[e * D + m]);
-          groups[t][key].push_back(e);
-        }
-    }
-    for (int i = 0; i < N; ++i) {
-      for (int t = 0; t < T; ++t) {
-        if (all_pairs) {
-          std::vector<int> key;
-          for (int m = 0; m < D; ++m)
-            if (!((p->active[t] >> m) & 1u)) key.push_back(p->idx1d[i * D + m]);
-          for (int j : groups[t][key])
-            if (keep(t, i, j)) ent.push_back((j << 4) | t);
-        } else {
-          for (long long q = desc->row_ptr[i]; q < desc->row_ptr[i + 1]; ++q) {
-            const int j = desc->cols[q] - base;
-            if (keep(t, i, j)) ent.push_back((j << 4) | t);
-          }
-        }
-      }
-      p->row_ptr[i + 1] = static_cast<long long>(ent.size());
-    }
-  }
-  // ---- pack operators -------------------------------------------------------------
-  long long off = 0;
-  for (int t = 0; t < T; ++t)
-    for (int m = 0; m < D; ++m) {
-      const int tm = t * D + m;
-      if (N == 0 || !((p->active[t] >> m) & 1u)) continue;
-      p->op_off[tm] = off;
-      off += static_cast<long long>(p->op_nb[tm]) * p->op_nb[tm] * P * P;
-    }
-  p->packed_elems = off;
-  asg::pack_host(p, desc->ops, desc->op_ld);
-  double pd1 = 1.0;
-  for (int k = 0; k <= D; ++k) pd1 *= P;
-  p->flops_dense = static_cast<double>(p->pairs) * T * D * 2.0 * pd1;
-  asg_status st = asg::finalize(p);
-  if (st) return bail(st);
-  *out = p;
+asg_status asg_plan_halo(const asg_plan* p, int* elems, long long capacity, long long* count) {
+  if (!p || !count) return fail(ASG_ERR_INVALID, "plan_halo: NULL argument");
+  const long long h = p->elem_global.empty() ? 0 : static_cast<long long>(p->N - p->N_out);
+  *count = h;
+  if (capacity == 0) return ASG_OK;
+  if (!elems) return fail(ASG_ERR_INVALID, "plan_halo: NULL elems");
+  if (capacity < h) return fail(ASG_ERR_CAPACITY, "plan_halo: capacity %lld < %lld halo elements", capacity, h);
+  for (long long k = 0; k < h; ++k) elems[k] = p->elem_global[p->N_out + k] + p->index_base;
   return ASG_OK;
+}
+
+asg_status asg_plan_row_entries(const asg_plan* p, long long* counts) {
+  if (!p || !counts) return fail(ASG_ERR_INVALID, "plan_row_entries: NULL argument");
+  for (int i = 0; i < p->N_out; ++i) counts[i] = p->row_ptr[i + 1] - p->row_ptr[i];
+  return ASG_OK;
+}
+
+asg_status asg_plan_update_elements(asg_plan* p, int num_elems, const int* idx1d, const long long* row_ptr,
+                                    const int* cols) {
+  return asg::update_elements(p, num_elems, idx1d, row_ptr, cols);
 }
 
 asg_status asg_plan_destroy(asg_plan* plan) {
@@ -949,7 +1144,7 @@ asg_status asg_plan_stats_get(const asg_plan* p, asg_plan_stats* s) {
   if (!p || !s) return fail(ASG_ERR_INVALID, "plan_stats_get: NULL argument");
   s->num_pairs = p->pairs;
   s->num_entries = static_cast<long long>(p->ent.size());
-  s->dof = static_cast<long long>(p->N) * p->B;
+  s->dof = static_cast<long long>(p->N_out) * p->B;  // output DOF (a row slice: its rows)
   s->flops_reference = p->flops_dense;
   s->flops_executed = p->flops_exec;
   s->op_bytes_f64 = p->packed_elems * 8;
@@ -1042,6 +1237,7 @@ asg_status asg_grad_ops_f32(asg_plan* p, const float* f, const float* r, float* 
 
 asg_status asg_apply_T_host_f64(asg_plan* p, const double* h_ybar, double* h_fbar) {
   if (!p) return fail(ASG_ERR_INVALID, "apply_T_host: NULL plan");
+  ASG_NOT_SLICE(p, "apply_T_host");
   asg_status st = asg::build_transpose(p);
   return st ? st : asg::apply_host<double>(p->tr, h_ybar, h_fbar);
 }
@@ -1049,6 +1245,7 @@ asg_status asg_apply_T_host_f64(asg_plan* p, const double* h_ybar, double* h_fba
 asg_status asg_grad_ops_host_f64(asg_plan* p, const double* h_f, const double* h_r, double* const* h_G,
                                  const int* ldg) {
   if (!p || !h_f || !h_r || !h_G || !ldg) return fail(ASG_ERR_INVALID, "grad_ops_host: NULL argument");
+  ASG_NOT_SLICE(p, "grad_ops_host");
   const int TD = p->T * p->D;
   const size_t n = static_cast<size_t>(p->N) * p->B;
   const size_t vec = ((n * sizeof(double) + 255) / 256) * 256;
@@ -1092,11 +1289,13 @@ asg_status asg_grad_ops_host_f64(asg_plan* p, const double* h_f, const double* h
 
 asg_status asg_apply_T_f64(asg_plan* p, const double* ybar, double* fbar, void* stream) {
   if (!p) return fail(ASG_ERR_INVALID, "apply_T: NULL plan");
+  ASG_NOT_SLICE(p, "apply_T");
   asg_status st = asg::build_transpose(p);
   return st ? st : asg::apply_dev<double>(p->tr, ybar, fbar, stream);
 }
 asg_status asg_apply_T_f32(asg_plan* p, const float* ybar, float* fbar, void* stream) {
   if (!p) return fail(ASG_ERR_INVALID, "apply_T: NULL plan");
+  ASG_NOT_SLICE(p, "apply_T");
   asg_status st = asg::build_transpose(p);
   return st ? st : asg::apply_dev<float>(p->tr, ybar, fbar, stream);
 }

@@ -88,6 +88,7 @@ extern "C" {
 
 asg_status asg_probe_gather_f32(asg_plan* p, const float* d_f, float* d_out, int stages, void* stream) {
   if (!p || !d_f || !d_out) return fail(ASG_ERR_INVALID, "probe_gather: NULL argument");
+  ASG_NOT_SLICE(p, "probe_gather");
   if (reinterpret_cast<uintptr_t>(d_f) & 15) return fail(ASG_ERR_INVALID, "probe_gather: f must be 16-byte aligned");
   if ((p->B * sizeof(float)) % 16 != 0) return fail(ASG_ERR_UNSUPPORTED, "probe_gather: block of %d floats", p->B);
   if (stages != 2 && stages != 4 && stages != 8) return fail(ASG_ERR_INVALID, "probe_gather: stages=%d", stages);

@@ -1252,10 +1252,12 @@ extern "C" {
 
 asg_status asg_rk3_step_f64(asg_plan* plan, double* d_f, double dt, const double* const* d_src, double* d_work,
                             size_t work_bytes, void* stream) {
+  ASG_NOT_SLICE(plan, "rk3_step");
   return rk3<double>(plan, d_f, dt, d_src, d_work, work_bytes, stream);
 }
 asg_status asg_rk3_step_f32(asg_plan* plan, float* d_f, double dt, const float* const* d_src, float* d_work,
                             size_t work_bytes, void* stream) {
+  ASG_NOT_SLICE(plan, "rk3_step");
   return rk3<float>(plan, d_f, dt, d_src, d_work, work_bytes, stream);
 }
 
@@ -1269,6 +1271,7 @@ asg_status asg_lincomb_f64(long long n, int ns, const double* d_coef, const doub
 
 asg_status asg_be_workspace(const asg_plan* plan, const asg_gmres_opts* opts, size_t* bytes) {
   if (!plan || !opts || !bytes) return fail(ASG_ERR_INVALID, "be_workspace: NULL argument");
+  ASG_NOT_SLICE(plan, "be_workspace");
   if (opts->restart < 1 || opts->restart > asg::kMaxRestart) return fail(ASG_ERR_INVALID, "be_workspace: restart=%d", opts->restart);
   asg_plan_stats ps{};
   asg_plan_stats_get(plan, &ps);
@@ -1281,6 +1284,7 @@ asg_status asg_be_workspace(const asg_plan* plan, const asg_gmres_opts* opts, si
 asg_status asg_be_solve(asg_plan* plan, double dt, const double* d_b, double* d_x, const asg_gmres_opts* opts,
                         asg_gmres_info* info, void* d_work, size_t work_bytes, void* stream) {
   if (!plan || !d_b || !d_x || !opts || !d_work) return fail(ASG_ERR_INVALID, "be_solve: NULL argument");
+  ASG_NOT_SLICE(plan, "be_solve");
   if (opts->restart < 1 || opts->restart > asg::kMaxRestart || opts->max_outer < 0 || !(opts->tol > 0) ||
       !(opts->inner_reduction > 0 && opts->inner_reduction < 1) || opts->mixed < ASG_GMRES_FP64 ||
       opts->mixed > ASG_GMRES_FP32_MATVEC)

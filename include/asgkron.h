@@ -69,7 +69,7 @@ typedef struct {
 typedef struct {
   long long num_pairs;         /* listed (row, col) pairs */
   long long num_entries;       /* (row, col, term) products the kernels execute */
-  long long dof;               /* num_elems * deg^d */
+  long long dof;               /* output values: num_elems * deg^d (a row slice: its rows') */
   double flops_reference;      /* num_pairs * T * d * 2 * deg^(d+1): the reference's work */
   double flops_executed;       /* flops of the executed work model */
   long long op_bytes_f64;      /* packed operator bytes on the device (FP64 copy) */
@@ -98,6 +98,45 @@ asg_status asg_plan_active(const asg_plan* plan, unsigned* masks);
 /* Re-upload operator values with the same sparsity class (time-dependent terms rebuilt by
  * get_coeff_mats.m with TD=1); the structure analysis is not redone. */
 asg_status asg_plan_update_ops(asg_plan* plan, const double* const* ops, const int* op_ld);
+
+/* Extended creation.  asg_plan_create(desc) is asg_plan_create_ex(desc, NULL). */
+typedef struct {
+  /* Output rows [row_begin, row_end) of the table (0 and num_elems: the whole table).  A
+   * narrower range makes a row-slice plan (no reference counterpart: the prototype applies on
+   * one node; a slice is one process's share when y = A f is split by output element): its
+   * output y holds (row_end - row_begin) blocks in row order, and its input f holds those
+   * rows' blocks followed by the halo blocks -- every other element the rows' work entries
+   * read after structure detection, in table order (asg_plan_halo lists them).  A row-slice
+   * plan runs the forward apply (device and host pointers) and the tuner; the adjoint,
+   * gradients, steppers, batches, assembly and asg_plan_update_elements return
+   * ASG_ERR_UNSUPPORTED for it. */
+  int row_begin, row_end;
+  /* NULL, or [num_dims]: pack at least op_blocks[k] deg x deg blocks per side of every operator
+   * on dimension k, however high the table's 1-D indices reach, so that a later
+   * asg_plan_update_elements can take tables with 1-D indices up to op_blocks[k] (base as the
+   * table's).  The operators must hold op_blocks[k]*deg rows and columns. */
+  const int* op_blocks;
+} asg_plan_ext;
+asg_status asg_plan_create_ex(const asg_plan_desc* desc, const asg_plan_ext* ext, asg_plan** plan);
+/* Work entries (column, term products) of each output row, counts[num rows]: the cost to
+ * balance when rows are split across processes (no reference counterpart). */
+asg_status asg_plan_row_entries(const asg_plan* plan, long long* counts);
+/* The halo of a row-slice plan: the table ids (in the creation's index base) of the input
+ * elements after the rows, in the order f holds them; capacity 0 queries the count.  A
+ * whole-table plan has none. */
+asg_status asg_plan_halo(const asg_plan* plan, int* elems, long long capacity, long long* count);
+/* A new element table and pair list (num_elems, idx1d, row_ptr, cols as in asg_plan_desc, same
+ * index base) on the plan's operators, for the rebuild adapt.m:414-437 triggers after
+ * coarsening or refinement when the operators keep their values (operators built at the
+ * maximum level: single partial terms).  The operators' structure classes, packed blocks and
+ * device copies are kept; the work list, the launch data and everything derived from the
+ * table (transpose, gradient targets, the fused solve's partition, the tuner's choice) are
+ * rebuilt or dropped.  ASG_ERR_CAPACITY when a 1-D index lies beyond the packed operator
+ * extent (create the plan with asg_plan_ext.op_blocks to reserve it); after an argument error
+ * the plan is unchanged.  Operators that change with the table (rechained LDG terms,
+ * get_coeff_mats_rechain.m) need asg_plan_update_ops afterwards, or a new plan. */
+asg_status asg_plan_update_elements(asg_plan* plan, int num_elems, const int* idx1d, const long long* row_ptr,
+                                    const int* cols);
 
 /* Force a kernel family for this plan: 0 warp chain (deg^d <= 256), 1 CTA chain,
  * 2 single-mode fiber kernel with direct loads, 3 single-mode fiber kernel with TMA bulk

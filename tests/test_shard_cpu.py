@@ -25,17 +25,57 @@ def test_partition_rows_balances_prefix_sums():
     assert p[0][0] == 0 and p[-1][1] == 3 and all(r0 <= r1 for r0, r1 in p)
 
 
-def test_row_pairs_keeps_only_the_range():
-    from asgkron.shard import row_pairs
+def structured_halo(mats, idx, rows, drop_tol=1e-13):
+    """The halo of rows [r0, r1) as the structure analysis defines it, restated in numpy: the
+    columns j outside the range such that some term's identity dimensions match row i's 1-D
+    indices and every applied factor's deg x deg block (i, j) is nonzero (0-based, ascending).
+    idx is 1-based [N, d]."""
+    T, D = len(mats), len(mats[0])
+    N = idx.shape[0]
+    deg = mats[0][0].shape[0] // int(idx.max())
+    ident, zero = [[None] * D for _ in range(T)], [[None] * D for _ in range(T)]
+    for t in range(T):
+        for m in range(D):
+            A = np.asarray(mats[t][m])
+            thr = drop_tol * np.abs(A).max()
+            ident[t][m] = bool(np.all(np.abs(A - np.eye(A.shape[0])) <= thr))
+            nb = A.shape[0] // deg
+            zero[t][m] = np.abs(A.reshape(nb, deg, nb, deg)).max(axis=(1, 3)) <= thr
+    r0, r1 = rows
+    need = set()
+    for i in range(r0, r1):
+        for j in range(N):
+            if r0 <= j < r1:
+                continue
+            for t in range(T):
+                ok = True
+                for m in range(D):
+                    a, b = idx[i, m] - 1, idx[j, m] - 1
+                    if ident[t][m]:
+                        ok = a == b
+                    else:
+                        ok = not zero[t][m][a, b]
+                    if not ok:
+                        break
+                if ok:
+                    need.add(j)
+                    break
+    return np.array(sorted(need), dtype=np.int64)
 
-    N = 6
-    rp, cl = row_pairs(N, (2, 4))
-    assert list(np.diff(rp)) == [0, 0, N, N, 0, 0] and list(cl) == list(range(N)) * 2
-    full_rp = np.array([0, 2, 3, 6, 6, 8, 9])
-    full_cl = np.array([0, 1, 2, 0, 3, 5, 1, 4, 5])
-    rp, cl = row_pairs(N, (1, 5), (full_rp, full_cl))
-    assert list(np.diff(rp)) == [0, 1, 3, 0, 2, 0]
-    assert list(cl) == [2, 0, 3, 5, 1, 4]
+
+def test_exchange_lists_route_every_halo_block():
+    from asgkron.shard import exchange_lists
+
+    ranges = [(0, 3), (3, 5), (5, 9)]
+    halos = [[3, 4, 7], [0, 8], [2, 4]]
+    s0, r0 = exchange_lists(ranges, halos, 0)
+    assert [list(x) for x in s0] == [[], [0], [2]] and r0 == [0, 2, 1]
+    s1, r1 = exchange_lists(ranges, halos, 1)
+    assert [list(x) for x in s1] == [[0, 1], [], [1]] and r1 == [1, 0, 1]
+    s2, r2 = exchange_lists(ranges, halos, 2)
+    assert [list(x) for x in s2] == [[2], [3], []] and r2 == [1, 1, 0]
+    with pytest.raises(ValueError):
+        exchange_lists([(0, 3), (3, 5)], [[7], []], 0)  # element 7 lies in no range
 
 
 def _free_port():
@@ -52,6 +92,7 @@ def _worker(rank, world, port, out_path):
     from cases import problem
     from oracle import asgard_oracle as O
     from asgkron.shard import ShardedApply, partition_rows
+    from test_shard_cpu import structured_halo
 
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
@@ -64,34 +105,39 @@ def _worker(rank, world, port, out_path):
         idx64 = idx.astype(np.int64)
         f = np.random.default_rng(0).standard_normal(N * B)
         ranges = partition_rows(np.full(N, N), world)
-
-        class OracleRows:  # the rank's plan: rows of its range, zeros elsewhere
-            def __init__(self, r0, r1):
-                self.rows = np.arange(r0, r1)
-
-            def apply(self, ft):
-                y = np.zeros(N * B)
-                if self.rows.size:
-                    vals = O.apply_A_rows(mats, idx64, deg, ft.numpy(), rows=self.rows)
-                    y.reshape(N, B)[self.rows] = vals.reshape(-1, B)
-                return torch.from_numpy(y)
-
         r0, r1 = ranges[rank]
-        sharded = ShardedApply(OracleRows(r0, r1), ranges, B)
+        halo = structured_halo(mats, idx, (r0, r1))
+
+        class OracleSlice:  # the rank's row-slice plan: f = rows + halo, y = rows
+            def apply(self, fc):
+                full = np.zeros(N * B)
+                elems = np.concatenate([np.arange(r0, r1), halo]).astype(np.int64)
+                full.reshape(N, B)[elems] = fc.numpy().reshape(-1, B)
+                if r1 == r0:
+                    return torch.zeros(0, dtype=torch.float64)
+                return torch.from_numpy(O.apply_A_rows(mats, idx64, deg, full, rows=np.arange(r0, r1)))
+
+        sharded = ShardedApply(OracleSlice(), ranges, B, halo=halo)
         f_local = torch.from_numpy(f.reshape(N, B)[r0:r1].ravel().copy())
-        # the gathered f is the full vector on every rank
-        assert torch.equal(sharded.gather_f(f_local), torch.from_numpy(f))
+        # the exchanged input is the rank's rows followed by exactly its halo blocks
+        got = sharded.gather_f(f_local).clone()
+        want_in = np.concatenate([f.reshape(N, B)[r0:r1], f.reshape(N, B)[halo]]).ravel()
+        in_ok = bool(np.array_equal(got.numpy(), want_in))
         y_local = sharded.apply(f_local)
-        parts = [torch.zeros(max(sharded.counts), dtype=torch.float64) for _ in range(world)]
-        buf = torch.zeros(max(sharded.counts), dtype=torch.float64)
+        y_again = sharded.apply(f_local)  # buffers reused: same result
+        counts = [(b - a) * B for a, b in ranges]
+        parts = [torch.zeros(max(counts), dtype=torch.float64) for _ in range(world)]
+        buf = torch.zeros(max(counts), dtype=torch.float64)
         buf[:y_local.numel()] = y_local
         dist.all_gather(parts, buf)
+        flags = [None] * world
+        dist.all_gather_object(flags, (in_ok, bool(torch.equal(y_local, y_again)), int(halo.size)))
         if rank == 0:
-            y = torch.cat([p[:c] for p, c in zip(parts, sharded.counts)]).numpy()
+            y = torch.cat([p[:c] for p, c in zip(parts, counts)]).numpy()
             want = O.apply_A_rows(mats, idx64, deg, f)
             err = np.linalg.norm(y - want) / np.linalg.norm(want)
             with open(out_path, "w") as fh:
-                fh.write("%.17g %r" % (float(err), [[int(a), int(b)] for a, b in ranges]))
+                fh.write("%.17g %r %r" % (float(err), flags, [[int(a), int(b)] for a, b in ranges]))
     finally:
         dist.destroy_process_group()
 
@@ -99,12 +145,16 @@ def _worker(rank, world, port, out_path):
 def test_sharded_apply_two_gloo_ranks(tmp_path):
     torch = pytest.importorskip("torch")
     import torch.multiprocessing as mp
+    import ast
 
     out = str(tmp_path / "res.txt")
     mp.start_processes(_worker, args=(2, _free_port(), out), nprocs=2, join=True, start_method="spawn")
-    err, ranges = open(out).read().split(" ", 1)
-    assert float(err) <= 1e-14, (err, ranges)
-    assert "[0," in ranges
+    err, rest = open(out).read().split(" ", 1)
+    flags = ast.literal_eval(rest[:rest.index("]") + 1])
+    assert float(err) <= 1e-14, (err, rest)
+    assert all(a and b for a, b, _ in flags), flags
+    # each rank receives only its halo: far less than the other rank's whole share
+    assert all(0 < h < 100 for _, _, h in flags), flags
 
 
 def test_partition_problems_covers_and_balances():
