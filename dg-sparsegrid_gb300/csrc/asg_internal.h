@@ -227,6 +227,22 @@ struct asg_plan {
   void* d_io = nullptr;
   size_t d_io_bytes = 0;
   cudaStream_t stream = nullptr;
+  // host-pointer apply in element chunks (one-CTA-per-row kernels; built on first use): f
+  // arrives in kHostChunks pieces, coarsest elements first; chunk c is elements
+  // [hc_lo[c], hc_lo[c-1]) (hc_lo[-1] = N) and its rows -- those whose blocks have all arrived
+  // with it -- are hc_rows[hc_start[c] .. hc_start[c+1]), longest first
+  static constexpr int kHostChunks = 4;
+  std::vector<int> hc_lo, hc_start;
+  int* d_hc_rows = nullptr;
+  cudaStream_t cstream[2] = {nullptr, nullptr};
+  cudaEvent_t ev_in[kHostChunks] = {};
+  cudaEvent_t ev_done[2] = {nullptr, nullptr};
+  // the chunked host apply as one CUDA graph, replayed while the caller repeats its page-locked
+  // f and y buffers (captured at the second call with the same buffers, kernel and precision)
+  cudaGraphExec_t hg_exec = nullptr;
+  const void* hg_f = nullptr;
+  const void* hg_y = nullptr;
+  int hg_kind = -1, hg_es = 0, hg_repeat = 0;
 };
 
 // A row-slice plan (asg_plan_create_ex with a narrower row range): forward apply only.

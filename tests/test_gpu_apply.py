@@ -235,12 +235,18 @@ def test_deterministic_linear_and_host_path(dev):
     assert h32.dtype == np.float32 and rel2(h32, a) <= FP32_TOL
 
 
-@pytest.mark.parametrize("name,lev,deg", [("continuity3", 4, 3), ("continuity6", 2, 4)])
-def test_host_path_pinned_output(dev, name, lev, deg):
+@pytest.mark.parametrize("name,lev,deg,kind", [("continuity3", 4, 3, None), ("continuity6", 2, 4, None),
+                                              ("continuity6", 3, 4, None), ("continuity6", 4, 4, None),
+                                              ("continuity6", 4, 4, 5), ("continuity6", 4, 4, 8)])
+def test_host_path_pinned_output(dev, name, lev, deg, kind):
     """A page-locked y is written by the apply kernel itself (no device-to-host copy); the
-    result equals the pageable copy path and the device apply bitwise, in both precisions."""
+    result equals the pageable copy path and the device apply bitwise, in both precisions.
+    continuity6 plans take the chunked host path (f in by element chunks, each chunk's ready
+    rows launched as it lands), including when the plan runs kind 5 or 8 on the device."""
     pde, table, idx, mats = problem(name, lev, deg)
     plan = _plan(mats, idx, deg)
+    if kind is not None:
+        plan.set_kernel(kind)
     f = np.random.default_rng(21).standard_normal(plan.dof)
     for dt in (torch.float64, torch.float32):
         fh = torch.from_numpy(f).to(dt).pin_memory()
@@ -249,6 +255,14 @@ def test_host_path_pinned_output(dev, name, lev, deg):
         pageable = plan.apply_host(fh.numpy().copy())
         assert np.array_equal(yh.numpy(), pageable)
         assert np.array_equal(yh.numpy(), _apply(plan, f, dev, dt).astype(yh.numpy().dtype))
+        for _ in range(4):  # repeated buffers: direct, captured into a graph, then replayed
+            yh.fill_(float("nan"))
+            plan.apply_host(fh.numpy(), yh.numpy())
+            assert np.array_equal(yh.numpy(), pageable)
+        fh.copy_(torch.from_numpy(-f).to(dt))  # new values in the same buffers
+        plan.apply_host(fh.numpy(), yh.numpy())
+        assert np.array_equal(yh.numpy(), -pageable)
+    assert plan.device_status() == 0
 
 
 def test_apply_A_matlab_mirror(dev):
