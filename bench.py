@@ -1001,21 +1001,30 @@ def main():
     value = world * dof / (apply_ms * 1e-3) / 1e9
 
     # ---- end to end through the host-pointer C ABI call ----------------------------------
+    # asg_apply_host_f32 on page-locked host f and y (the call a host caller makes; ctypes
+    # arguments prepared once), L2 flushed and the device idle before each call
+    import ctypes as C
+
+    from asgkron._lib import check, lib
+
     fh = torch.from_numpy(f64_h.astype(np.float32)).pin_memory()
     yh = torch.empty_like(fh).pin_memory()
-    fh_np, yh_np = fh.numpy(), yh.numpy()
+    host_fn, h_args = lib().asg_apply_host_f32, (plan.handle, C.c_void_p(fh.data_ptr()), C.c_void_p(yh.data_ptr()))
     for _ in range(max(3, args.warmup)):
-        plan.apply_host(fh_np, yh_np)
+        check(host_fn(*h_args))
     e2e_steps = max(1, min(args.steps, 500))
     tot = 0.0
     for _ in range(e2e_steps):
         flush()
         torch.cuda.synchronize()
         t_a = time.perf_counter()
-        plan.apply_host(fh_np, yh_np)
+        check(host_fn(*h_args))
         tot += time.perf_counter() - t_a
     e2e_ms = tot / e2e_steps * 1e3
     e2e_value = dof / (e2e_ms * 1e-3) / 1e9
+    plan.apply(f32, y32, stream)
+    torch.cuda.synchronize()
+    e2e_matches_device = bool(torch.equal(yh, y32.cpu()))
 
     # ---- variants: FP64 (same work model) and the reference work model ------------------
     variants = {}
@@ -1067,16 +1076,17 @@ def main():
         variants["tuner"] = {"fp32": plan.tune("float32"), "fp64": plan.tune("float64")}
         plan.set_kernel(st["kernel_kind"])
         # end to end through the FP64 host-pointer call (what the MATLAB gateway makes)
-        f64h = np.ascontiguousarray(f64_h)
-        y64h = np.empty_like(f64h)
+        f64h = torch.from_numpy(np.ascontiguousarray(f64_h)).pin_memory()
+        y64h = torch.empty_like(f64h).pin_memory()
+        h64 = (plan.handle, C.c_void_p(f64h.data_ptr()), C.c_void_p(y64h.data_ptr()))
         for _ in range(3):
-            plan.apply_host(f64h, y64h)
+            check(lib().asg_apply_host_f64(*h64))
         tot64 = 0.0
         for _ in range(max(5, min(args.steps, 100))):
             flush()
             torch.cuda.synchronize()
             t_a = time.perf_counter()
-            plan.apply_host(f64h, y64h)
+            check(lib().asg_apply_host_f64(*h64))
             tot64 += time.perf_counter() - t_a
         e64 = tot64 / max(5, min(args.steps, 100)) * 1e3
         variants["e2e_fp64_host"] = {"ms_per_step": e64, "value": dof / (e64 * 1e-3) / 1e9,
@@ -1117,7 +1127,8 @@ def main():
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
                          "algorithmic_bytes_per_launch": alg},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": dof * 4, "d2h_bytes_per_step": dof * 4,
-                    "ms_per_step": e2e_ms},
+                    "ms_per_step": e2e_ms, "call": "asg_apply_host_f32, page-locked f and y",
+                    "equals_device_apply": e2e_matches_device},
             "gpu_launches": args.steps,
             "clocks": clocks,
             "variants": variants,
