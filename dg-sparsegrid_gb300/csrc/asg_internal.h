@@ -242,6 +242,8 @@ struct asg_plan {
   cudaGraphExec_t hg_exec = nullptr;
   const void* hg_f = nullptr;
   const void* hg_y = nullptr;
+  const void* hg_kf = nullptr;       // the device aliases of f and y the graph was made with
+  const void* hg_ky = nullptr;
   int hg_kind = -1, hg_es = 0, hg_repeat = 0;
 };
 

@@ -247,7 +247,7 @@ asg_status build_streams(asg_plan* p, int nsm) {
 void drop_host_graph(asg_plan* p) {
   if (p->hg_exec) cudaGraphExecDestroy(p->hg_exec);
   p->hg_exec = nullptr;
-  p->hg_f = p->hg_y = nullptr;
+  p->hg_f = p->hg_y = p->hg_kf = p->hg_ky = nullptr;
   p->hg_kind = -1;
   p->hg_es = 0;
   p->hg_repeat = 0;
@@ -716,13 +716,15 @@ asg_status host_chunks(asg_plan* p) {
 }
 
 // True for page-locked host memory the runtime knows (cudaHostAlloc / cudaHostRegister).
-bool host_pinned(const void* h) {
+// The device alias of page-locked host memory the runtime knows (cudaHostAlloc /
+// cudaHostRegister), or NULL.
+const void* host_pinned(const void* h) {
   cudaPointerAttributes at{};
   if (cudaPointerGetAttributes(&at, h) != cudaSuccess) {
     cudaGetLastError();
-    return false;
+    return nullptr;
   }
-  return at.type == cudaMemoryTypeHost;
+  return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
 }
 
 // The chunked host apply on the plan's streams: f by element chunks on p->stream, each
@@ -798,8 +800,12 @@ asg_status apply_host(asg_plan* p, const T* hf, T* hy) {
     // A caller that repeats its page-locked buffers (a time loop) gets the whole pipeline as one
     // graph launch instead of ~20 runtime calls: captured at the second call with the same f, y,
     // kernel and precision, replayed from the third.
-    const bool pinned = ky != dy && host_pinned(hf);
-    const bool same = pinned && p->hg_f == hf && p->hg_y == hy && p->hg_kind == kind && p->hg_es == sizeof(T);
+    // the key holds the host pointers and their device aliases: a buffer freed and registered
+    // again at the same address must not replay a graph made for the old registration
+    const void* kf = ky != dy ? host_pinned(hf) : nullptr;
+    const bool pinned = kf != nullptr;
+    const bool same = pinned && p->hg_f == hf && p->hg_y == hy && p->hg_kf == kf && p->hg_ky == ky &&
+                      p->hg_kind == kind && p->hg_es == sizeof(T);
     if (same && p->hg_exec) {
       ASG_CUDA(cudaGraphLaunch(p->hg_exec, p->stream));
       ASG_CUDA(cudaStreamSynchronize(p->stream));
@@ -824,6 +830,8 @@ asg_status apply_host(asg_plan* p, const T* hf, T* hy) {
         p->hg_exec = ge;
         p->hg_f = hf;
         p->hg_y = hy;
+        p->hg_kf = kf;
+        p->hg_ky = ky;
         p->hg_kind = kind;
         p->hg_es = sizeof(T);
         ASG_CUDA(cudaGraphLaunch(p->hg_exec, p->stream));
@@ -838,6 +846,8 @@ asg_status apply_host(asg_plan* p, const T* hf, T* hy) {
       if (pinned) {
         p->hg_f = hf;
         p->hg_y = hy;
+        p->hg_kf = kf;
+        p->hg_ky = ky;
         p->hg_kind = kind;
         p->hg_es = sizeof(T);
       }
