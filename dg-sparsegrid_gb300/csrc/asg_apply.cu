@@ -70,14 +70,47 @@ __device__ __forceinline__ void team_copy(T* dst, const T* src, int n, int rank,
 
 // One mode product of the chain on an element block held in shared memory:
 // out[.., a, ..] = sum_b A[a][b] * in[.., b, ..] along dimension m (stride s).
+// Fibers are numbered fi = hi * s + lo (lo < s); for a power-of-two degree s is a power of two
+// and the split takes a shift and a mask instead of an integer division.  In FP32 with
+// deg <= 4 a thread takes two fibers at once (fi and fi + size) on the paired FMA; every output
+// sees the scalar loop's operations in its order (a product, then fused multiply-adds), so
+// the result is bitwise the same.
 template <typename T, int P>
 __device__ __forceinline__ void mode_pass(const T* __restrict__ in, T* __restrict__ out, const T* A, int B, int s,
                                           int rank, int size) {
   const int nf = B / P;
-  for (int fi = rank; fi < nf; fi += size) {
-    const int hi = fi / s;
-    const int lo = fi - hi * s;
-    const int base = hi * s * P + lo;
+  constexpr bool POW2 = (P & (P - 1)) == 0;
+  const int sh = POW2 ? __ffs(s) - 1 : 0;
+  auto fiber_base = [&](int fi) {
+    if constexpr (POW2) {
+      return (((fi >> sh) * P) << sh) + (fi & (s - 1));
+    } else {
+      const int hi = fi / s;
+      return hi * s * P + (fi - hi * s);
+    }
+  };
+  int fi = rank;
+  if constexpr (sizeof(T) == 4 && P <= 4) {
+    float2 A2[P * P];
+#pragma unroll
+    for (int r = 0; r < P * P; ++r) A2[r] = make_float2(A[r], A[r]);
+    for (; fi + size < nf; fi += 2 * size) {
+      const int b0 = fiber_base(fi), b1 = fiber_base(fi + size);
+      float2 x2[P];
+#pragma unroll
+      for (int b = 0; b < P; ++b) x2[b] = make_float2(in[b0 + b * s], in[b1 + b * s]);
+#pragma unroll
+      for (int a = 0; a < P; ++a) {
+        float2 sum = __fmul2_rn(A2[a * P], x2[0]);
+#pragma unroll
+        for (int b = 1; b < P; ++b) sum = __ffma2_rn(A2[a * P + b], x2[b], sum);
+        out[b0 + a * s] = sum.x;
+        out[b1 + a * s] = sum.y;
+      }
+    }
+  }
+  for (; fi < nf; fi += size) {
+    const int base = fiber_base(fi);
     T x[P];
 #pragma unroll
     for (int b = 0; b < P; ++b) x[b] = in[base + b * s];
