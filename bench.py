@@ -1104,10 +1104,21 @@ def main():
     if "fp32_forward_backward" in variants:
         fb = variants["fp32_forward_backward"]
         fb["frac_hbm"] = fb["achieved_gbs"] / peak
-    traffic = None
+    traffic = gather_ncu = None
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
-        traffic = json.load(open(tpath)).get("k_single_tma_fp32_continuity6")
+        tj = json.load(open(tpath))
+        traffic = tj.get("k_single_tma_fp32_continuity6")
+        gather_ncu = tj.get("k_single_tma_fp32_continuity6_l2_to_sm")
+    # second roofline: the L2-to-SM bytes the kernel moves (ncu) over the rate the same kind of
+    # gather reaches when streamed alone (asg_probe_gather_f32, measured in this run)
+    gather_roof = None
+    if gather_ncu and "gather_stream" in variants:
+        g_ach = gather_ncu / (apply_ms * 1e-3) / 1e9
+        g_peak = variants["gather_stream"]["gbs"]
+        gather_roof = {"achieved": g_ach, "peak": g_peak, "unit": "GB/s", "frac": g_ach / g_peak,
+                       "bytes_per_launch": gather_ncu,
+                       "peak_source": "measured in this run: the plan's gather pattern streamed alone"}
 
     cpu = None
     if rank == 0 and world == 1:
@@ -1125,7 +1136,7 @@ def main():
                         "parallelism": "replicas" if world > 1 else "single GPU"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
-                         "algorithmic_bytes_per_launch": alg},
+                         "algorithmic_bytes_per_launch": alg, "gather": gather_roof},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": dof * 4, "d2h_bytes_per_step": dof * 4,
                     "ms_per_step": e2e_ms, "call": "asg_apply_host_f32, page-locked f and y",
                     "equals_device_apply": e2e_matches_device},

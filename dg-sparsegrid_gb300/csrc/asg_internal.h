@@ -227,13 +227,14 @@ struct asg_plan {
   void* d_io = nullptr;
   size_t d_io_bytes = 0;
   cudaStream_t stream = nullptr;
-  // host-pointer apply in element chunks (one-CTA-per-row kernels; built on first use): f
-  // arrives in kHostChunks pieces, coarsest elements first; chunk c is elements
-  // [hc_lo[c], hc_lo[c-1]) (hc_lo[-1] = N) and its rows -- those whose blocks have all arrived
-  // with it -- are hc_rows[hc_start[c] .. hc_start[c+1]), longest first
+  // host-pointer apply in element chunks (one-CTA-per-row kernels; built on first use, per
+  // precision k = 0 FP64, 1 FP32): f arrives in kHostChunks pieces, coarsest elements first;
+  // chunk c is elements [hc_lo[k][c], hc_lo[k][c-1]) (hc_lo[k][-1] = N) and its rows -- those
+  // whose blocks have all arrived with it -- are hc_rows[k][hc_start[k][c] .. hc_start[k][c+1]),
+  // longest first
   static constexpr int kHostChunks = 4;
-  std::vector<int> hc_lo, hc_start;
-  int* d_hc_rows = nullptr;
+  std::vector<int> hc_lo[2], hc_start[2];
+  int* d_hc_rows[2] = {nullptr, nullptr};
   cudaStream_t cstream[2] = {nullptr, nullptr};
   cudaEvent_t ev_in[kHostChunks] = {};
   cudaEvent_t ev_done[2] = {nullptr, nullptr};

@@ -88,7 +88,7 @@ void free_device(asg_plan* p) {
   cudaFree(p->d_io);
   if (p->stream) cudaStreamDestroy(p->stream);
   if (p->hg_exec) cudaGraphExecDestroy(p->hg_exec);
-  cudaFree(p->d_hc_rows);
+  for (int k = 0; k < 2; ++k) cudaFree(p->d_hc_rows[k]);
   for (int k = 0; k < 2; ++k) {
     if (p->cstream[k]) cudaStreamDestroy(p->cstream[k]);
     if (p->ev_done[k]) cudaEventDestroy(p->ev_done[k]);
@@ -279,10 +279,12 @@ void drop_derived(asg_plan* p) {
     p->fz_G[k] = p->fz_max_rows[k] = p->fz_max_slots[k] = 0;
     p->tuned_kind[k] = -1;
   }
-  cudaFree(p->d_hc_rows);
-  p->d_hc_rows = nullptr;
-  p->hc_lo.clear();
-  p->hc_start.clear();
+  for (int k = 0; k < 2; ++k) {
+    cudaFree(p->d_hc_rows[k]);
+    p->d_hc_rows[k] = nullptr;
+    p->hc_lo[k].clear();
+    p->hc_start[k].clear();
+  }
   drop_host_graph(p);
 }
 
@@ -675,14 +677,17 @@ asg_status apply_dev(asg_plan* p, const T* f, T* y, void* stream) {
   return ASG_OK;
 }
 
-// Element chunks of the host-pointer apply (see asg_plan::hc_lo): pieces of N/2, N/4, 3N/20
-// and N/10 elements, taken from the end of the table (its coarsest elements, which rows of
-// every level read) towards its start; a row is ready with the chunk that brings the
-// lowest-numbered element it reads (itself or a column).
-asg_status host_chunks(asg_plan* p) {
-  if (!p->hc_start.empty()) return ASG_OK;
+// Element chunks of the host-pointer apply (see asg_plan::hc_lo), taken from the end of the
+// table (its coarsest elements, which rows of every level read) towards its start; a row is
+// ready with the chunk that brings the lowest-numbered element it reads (itself or a column).
+// FP32 pieces of N/2, N/4, 3N/20, N/10 elements; FP64, whose apply takes longer than the
+// copy, starts computing earlier: 2N/5, 3N/10, N/5, N/10 (each the fastest of five splits
+// measured on the continuity6 workload).
+asg_status host_chunks(asg_plan* p, int prec) {
+  if (!p->hc_start[prec].empty()) return ASG_OK;
   const int N = p->N, K = asg_plan::kHostChunks;
-  static const double kFrac[K] = {0.5, 0.75, 0.9, 1.0};
+  static const double kFracs[2][K] = {{0.4, 0.7, 0.9, 1.0}, {0.5, 0.75, 0.9, 1.0}};
+  const double* kFrac = kFracs[prec];
   std::vector<int> lo(K);
   for (int c = 0; c < K; ++c) lo[c] = std::max(0, N - static_cast<int>(std::lround(N * kFrac[c])));
   lo[K - 1] = 0;
@@ -702,7 +707,7 @@ asg_status host_chunks(asg_plan* p) {
     all.insert(all.end(), rows[c].begin(), rows[c].end());
     start.push_back(static_cast<int>(all.size()));
   }
-  asg_status st = upload(&p->d_hc_rows, all);
+  asg_status st = upload(&p->d_hc_rows[prec], all);
   if (st) return st;
   for (int k = 0; k < 2; ++k) {
     if (!p->cstream[k]) ASG_CUDA(cudaStreamCreateWithFlags(&p->cstream[k], cudaStreamNonBlocking));
@@ -710,8 +715,8 @@ asg_status host_chunks(asg_plan* p) {
   }
   for (int c = 0; c < K; ++c)
     if (!p->ev_in[c]) ASG_CUDA(cudaEventCreateWithFlags(&p->ev_in[c], cudaEventDisableTiming));
-  p->hc_lo = lo;
-  p->hc_start = start;
+  p->hc_lo[prec] = lo;
+  p->hc_start[prec] = start;
   return ASG_OK;
 }
 
@@ -732,9 +737,11 @@ const void* host_pinned(const void* h) {
 // mapped) one copy of y back; joined on p->stream.  No synchronisation (capturable).
 template <typename T>
 asg_status host_pipeline(asg_plan* p, int kind, const T* hf, T* df, T* hy, T* ky, T* dy, size_t ny) {
-  const int K = asg_plan::kHostChunks, N = p->N;
+  const int K = asg_plan::kHostChunks, N = p->N, pk = sizeof(T) == 4 ? 1 : 0;
+  const std::vector<int>& lo = p->hc_lo[pk];
+  const std::vector<int>& start = p->hc_start[pk];
   for (int c = 0; c < K; ++c) {
-    const size_t e0 = static_cast<size_t>(p->hc_lo[c]) * p->B, e1 = static_cast<size_t>(c ? p->hc_lo[c - 1] : N) * p->B;
+    const size_t e0 = static_cast<size_t>(lo[c]) * p->B, e1 = static_cast<size_t>(c ? lo[c - 1] : N) * p->B;
     if (e1 > e0) ASG_CUDA(cudaMemcpyAsync(df + e0, hf + e0, (e1 - e0) * sizeof(T), cudaMemcpyHostToDevice, p->stream));
     ASG_CUDA(cudaEventRecord(p->ev_in[c], p->stream));
   }
@@ -742,11 +749,11 @@ asg_status host_pipeline(asg_plan* p, int kind, const T* hf, T* df, T* hy, T* ky
   for (int c = 0; c < K; ++c) {
     cudaStream_t cs = p->cstream[c & 1];
     ASG_CUDA(cudaStreamWaitEvent(cs, p->ev_in[c], 0));
-    const int r0 = p->hc_start[c], r1 = p->hc_start[c + 1];
+    const int r0 = start[c], r1 = start[c + 1];
     if (r1 > r0) {
       ApplyArgs<T> a = make_args<T>(p, df, ky, ops);
       a.N = r1 - r0;  // one CTA per listed row
-      a.row_order = p->d_hc_rows + r0;
+      a.row_order = p->d_hc_rows[pk] + r0;
       cudaError_t e = launch_apply<T>(a, p->P, kind, cs);
       if (e != cudaSuccess) return cuda_fail(e, "apply kernel launch");
     }
@@ -795,7 +802,7 @@ asg_status apply_host(asg_plan* p, const T* hf, T* hy) {
   if (kind == KK_SINGLE_TMA_ROWS) kind = KK_SINGLE_TMA;
   if ((kind == KK_SINGLE_TMA || kind == KK_SINGLE_TMA3 || kind == KK_SINGLE_TMA_X2) && p->N_out == p->N &&
       p->N >= 4 * asg_plan::kHostChunks) {
-    asg_status st = host_chunks(p);
+    asg_status st = host_chunks(p, sizeof(T) == 4 ? 1 : 0);
     if (st) return st;
     // A caller that repeats its page-locked buffers (a time loop) gets the whole pipeline as one
     // graph launch instead of ~20 runtime calls: captured at the second call with the same f, y,
