@@ -328,21 +328,26 @@ def implicit_steps(dev, nsteps=10):
     finals = {}
     # matvec32: FP32 operator inside FP64 Arnoldi (dot products, norms, updates): the
     # configuration's mixed mode; inner32: the whole inner cycle in FP32; fp64: everything FP64
+    # each mode runs the ten steps twice from f0 (identical work, bitwise identical results);
+    # the faster pass is reported, so one host-side stall does not stand for the mode
     for mode, mixed in (("mixed", "matvec32"), ("mixed_fp32_inner", "inner32"), ("fp64", "fp64")):
-        f = torch.from_numpy(f0).to(dev)
-        be_step(plan, f.clone(), dt, mixed=mixed)  # warm-up (workspace, first launches)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        outer = inner = 0
-        worst = 0.0
-        for _ in range(nsteps):
-            f, info = be_step(plan, f, dt, mixed=mixed)
-            outer += info["outer_iters"]
-            inner += info["inner_iters"]
-            worst = max(worst, info["rel_residual"])
-        torch.cuda.synchronize()
-        ms = (time.perf_counter() - t0) / nsteps * 1e3
-        out[mode] = {"ms_per_step": ms, "outer_iters": outer, "inner_iters": inner, "max_rel_residual": worst}
+        be_step(plan, torch.from_numpy(f0).to(dev), dt, mixed=mixed)  # warm-up (workspace, first launches)
+        passes = []
+        for _ in range(2):
+            f = torch.from_numpy(f0).to(dev)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            outer = inner = 0
+            worst = 0.0
+            for _ in range(nsteps):
+                f, info = be_step(plan, f, dt, mixed=mixed)
+                outer += info["outer_iters"]
+                inner += info["inner_iters"]
+                worst = max(worst, info["rel_residual"])
+            torch.cuda.synchronize()
+            passes.append((time.perf_counter() - t0) / nsteps * 1e3)
+        out[mode] = {"ms_per_step": min(passes), "passes_ms_per_step": passes, "outer_iters": outer,
+                     "inner_iters": inner, "max_rel_residual": worst}
         finals[mode] = f
     out["mixed_speedup"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
     out["mixed_fp32_inner_speedup"] = out["fp64"]["ms_per_step"] / out["mixed_fp32_inner"]["ms_per_step"]
