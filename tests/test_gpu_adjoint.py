@@ -98,8 +98,9 @@ def _single_factor_grad_numpy(mats, idx0, f, r, deg):
 
 @pytest.mark.parametrize("lev", [2, 3])
 def test_single_factor_gradients_chunked_kernel(dev, lev):
-    """continuity6 deg 4 (one applied factor per term): the chunked gradient kernel against
-    the mode-unfolding contraction in numpy, FP64 and FP32, and bitwise repeatable."""
+    """continuity6 deg 4 (one applied factor per term): the chunked gradient kernel, on all
+    pairs and on the same pairs given as an explicit list, against the mode-unfolding
+    contraction in numpy, FP64 and FP32, and bitwise repeatable."""
     import asgkron
 
     _, _, idx, mats = problem("continuity6", lev, 4)
@@ -107,13 +108,16 @@ def test_single_factor_gradients_chunked_kernel(dev, lev):
     rng = np.random.default_rng(40 + lev)
     f, r = rng.standard_normal(N * 4096), rng.standard_normal(N * 4096)
     plan = asgkron.Plan.create(mats, idx, 4)
+    listed = asgkron.Plan.create(mats, idx, 4, pairs=(np.arange(N + 1) * N, np.tile(np.arange(N) + 1, N)))
     want = _single_factor_grad_numpy(mats, idx.astype(np.int64) - 1, f, r, 4)
     G = plan.grad_ops(_t(f, dev), _t(r, dev))
     G2 = plan.grad_ops(_t(f, dev), _t(r, dev))
+    Gl = listed.grad_ops(_t(f, dev), _t(r, dev))
     torch.cuda.synchronize()
     for t in range(6):
         got = G[t][t].cpu().numpy()
         assert np.abs(got - want[t]).max() <= 1e-12 * np.abs(want[t]).max(), t
+        assert np.abs(Gl[t][t].cpu().numpy() - want[t]).max() <= 1e-12 * np.abs(want[t]).max(), t
         assert torch.equal(G[t][t], G2[t][t])
     G32 = plan.grad_ops(_t(f, dev, torch.float32), _t(r, dev, torch.float32))
     torch.cuda.synchronize()
