@@ -720,7 +720,6 @@ asg_status host_chunks(asg_plan* p, int prec) {
   return ASG_OK;
 }
 
-// True for page-locked host memory the runtime knows (cudaHostAlloc / cudaHostRegister).
 // The device alias of page-locked host memory the runtime knows (cudaHostAlloc /
 // cudaHostRegister), or NULL.
 const void* host_pinned(const void* h) {
@@ -806,9 +805,9 @@ asg_status apply_host(asg_plan* p, const T* hf, T* hy) {
     if (st) return st;
     // A caller that repeats its page-locked buffers (a time loop) gets the whole pipeline as one
     // graph launch instead of ~20 runtime calls: captured at the second call with the same f, y,
-    // kernel and precision, replayed from the third.
-    // the key holds the host pointers and their device aliases: a buffer freed and registered
-    // again at the same address must not replay a graph made for the old registration
+    // kernel and precision, replayed from the third.  The key holds the host pointers and their
+    // device aliases: a buffer freed and registered again at the same address must not replay
+    // a graph made for the old registration.
     const void* kf = ky != dy ? host_pinned(hf) : nullptr;
     const bool pinned = kf != nullptr;
     const bool same = pinned && p->hg_f == hf && p->hg_y == hy && p->hg_kf == kf && p->hg_ky == ky &&
