@@ -57,6 +57,32 @@ def test_update_elements_equals_a_fresh_plan(structure):
     assert torch.equal(y1, p1.apply(f32))
 
 
+def test_update_elements_with_pair_lists_and_base0():
+    """A connectivity-list plan (0-based indices) takes a new table with its own connect_nD
+    pairs in place: equal to a fresh plan on that table and pair list, bitwise, both work
+    models."""
+    _need_gpu()
+    import asgkron
+    from asgkron import pdes
+
+    pde = pdes.continuity2(3)
+    deg = 2
+    mats = pde.term_mats(deg, construction_level=5)
+    t1 = asgkron.hash_table_sparse_nD([3, 3], 5)
+    t2 = asgkron.hash_table_sparse_nD([4, 4], 5)
+    for structure in ("detect", "none"):
+        rp1, cl1 = asgkron.connect_nD(t1, 3, 3)
+        rp2, cl2 = asgkron.connect_nD(t2, 4, 4)
+        plan = asgkron.Plan.create(mats, t1.idx1d() - 1, deg, pairs=(rp1, cl1), index_base=0,
+                                   structure=structure, op_blocks=[32, 32])
+        plan.update_elements(t2.idx1d() - 1, (rp2, cl2))
+        fresh = asgkron.Plan.create(mats, t2.idx1d() - 1, deg, pairs=(rp2, cl2), index_base=0, structure=structure)
+        assert plan.stats()["num_pairs"] == fresh.stats()["num_pairs"] == rp2[-1]
+        f = torch.from_numpy(np.random.default_rng(5).standard_normal(fresh.dof)).cuda()
+        assert torch.equal(plan.apply(f), fresh.apply(f))
+        assert torch.equal(plan.apply(f.float()), fresh.apply(f.float()))
+
+
 def test_update_elements_capacity_and_argument_errors():
     _need_gpu()
     import asgkron
