@@ -1105,6 +1105,7 @@ def main():
             t64.append(time.perf_counter() - t_a)
         e64 = statistics.median(t64) * 1e3
         variants["e2e_fp64_host"] = {"ms_per_step": e64, "mean_ms": sum(t64) / len(t64) * 1e3,
+                                     "max_ms": max(t64) * 1e3, "slowest_call": int(max(range(len(t64)), key=t64.__getitem__)),
                                      "value": dof / (e64 * 1e-3) / 1e9, "statistic": "median of host-timed calls",
                                      "h2d_bytes_per_step": 8 * dof, "d2h_bytes_per_step": 8 * dof}
 
@@ -1154,7 +1155,8 @@ def main():
                          "frac": achieved / peak, "traffic": traffic, "peak_source": peak_src,
                          "algorithmic_bytes_per_launch": alg, "gather": gather_roof},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": dof * 4, "d2h_bytes_per_step": dof * 4,
-                    "ms_per_step": e2e_ms, "mean_ms": e2e_mean_ms, "statistic": "median of host-timed calls",
+                    "ms_per_step": e2e_ms, "mean_ms": e2e_mean_ms, "max_ms": max(e2e_t) * 1e3,
+                    "statistic": "median of host-timed calls",
                     "call": "asg_apply_host_f32, page-locked f and y",
                     "equals_device_apply": e2e_matches_device},
             "gpu_launches": args.steps,
