@@ -837,6 +837,29 @@ def small_config_graph(dev):
     us = graph_replay(plan, f, y, stream)
     out = {"dof": plan.dof, "us_per_apply": us, "value": plan.dof / (us * 1e-6) / 1e9,
            "kernel": asgkron._lib.KERNEL_NAMES[plan.stats()["kernel_kind"]]}
+    # the configuration's five explicit RK3 steps at CFL 0.01 (sources included), one step
+    # captured in a CUDA graph and replayed five times per timed pass
+    from asgkron.steppers import RK3Stepper
+
+    dt = pde.dt(0.01)
+    x = f.clone()
+    stepper = RK3Stepper(plan, pde, idx)
+    stepper.capture(x, dt)
+    for i in range(5):
+        stepper.replay(i * dt)
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(20):
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        for i in range(5):
+            stepper.replay(i * dt)
+        t1.record()
+        torch.cuda.synchronize()
+        ts.append(t0.elapsed_time(t1) * 1e3 / 5)
+    out["rk3_step_us"] = statistics.median(ts)
+    out["rk3_launches_per_step"] = 9  # 3 source combinations, 3 applies, 3 stage updates; one graph
     plan.close()
     return out
 

@@ -33,7 +33,11 @@ class RK3Stepper:
         self.vecs = [torch.from_numpy(np.asarray(v, dtype=np.float64)).to(dev) for v in (source_parts or [])]
         self.vec_ptrs = torch.tensor([v.data_ptr() for v in self.vecs] or [0], dtype=torch.int64, device=dev)
         self.coef = torch.zeros(3 * max(ns, 1), dtype=torch.float64, device=dev)
-        self.coef_host = torch.zeros(3 * max(ns, 1), dtype=torch.float64).pin_memory()
+        # a ring of page-locked sources for the time factors: a replay queued while an earlier
+        # one's copy has not run yet must not overwrite that copy's source
+        self.coef_ring = [torch.zeros(3 * max(ns, 1), dtype=torch.float64).pin_memory() for _ in range(4)]
+        self.coef_done = [None] * 4
+        self._slot = 0
         self.src64 = [torch.zeros(self.n, dtype=torch.float64, device=dev) for _ in range(3)]
         self.src = self.src64 if self.torch_dtype == torch.float64 else [
             torch.zeros(self.n, dtype=torch.float32, device=dev) for _ in range(3)]
@@ -61,8 +65,15 @@ class RK3Stepper:
         if self.ns == 0:
             return
         vals = [fn(tt) for tt in (t, t + 0.5 * dt, t + dt) for fn in self.tfac]
-        self.coef_host.copy_(torch.tensor(vals, dtype=torch.float64))
-        self.coef.copy_(self.coef_host, non_blocking=True)
+        k = self._slot
+        if self.coef_done[k] is not None:
+            self.coef_done[k].synchronize()
+        self.coef_ring[k].copy_(torch.tensor(vals, dtype=torch.float64))
+        self.coef.copy_(self.coef_ring[k], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record()
+        self.coef_done[k] = ev
+        self._slot = (k + 1) % len(self.coef_ring)
 
     def _launch(self, f, dt, stream):
         src = self._sources(stream)
