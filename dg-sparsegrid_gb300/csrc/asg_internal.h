@@ -228,13 +228,16 @@ struct asg_plan {
   size_t d_io_bytes = 0;
   cudaStream_t stream = nullptr;
   // host-pointer apply in element chunks (one-CTA-per-row kernels; built on first use, per
-  // precision k = 0 FP64, 1 FP32): f arrives in kHostChunks pieces, coarsest elements first;
-  // chunk c is elements [hc_lo[k][c], hc_lo[k][c-1]) (hc_lo[k][-1] = N) and its rows -- those
-  // whose blocks have all arrived with it -- are hc_rows[k][hc_start[k][c] .. hc_start[k][c+1]),
-  // longest first
+  // schedule s = 2 * g + k, k = 0 FP64, 1 FP32): f arrives in kHostChunks pieces of an element
+  // order -- g = 0: the table reversed (coarsest elements first), one copy per chunk; g = 1
+  // (page-locked f): the columns of the longest rows first, gathered by a kernel from the
+  // mapped buffer, order d_hc_order[s]. Chunk c is positions [hc_estart[s][c],
+  // hc_estart[s][c+1]) of the order, and its rows -- those whose blocks have all arrived with
+  // it -- are hc_rows[s][hc_start[s][c] .. hc_start[s][c+1]), longest first
   static constexpr int kHostChunks = 4;
-  std::vector<int> hc_lo[2], hc_start[2];
-  int* d_hc_rows[2] = {nullptr, nullptr};
+  std::vector<int> hc_estart[4], hc_start[4];
+  int* d_hc_rows[4] = {};
+  int* d_hc_order[4] = {};
   cudaStream_t cstream[2] = {nullptr, nullptr};
   cudaEvent_t ev_in[kHostChunks] = {};
   cudaEvent_t ev_done[2] = {nullptr, nullptr};

@@ -242,7 +242,9 @@ def test_host_path_pinned_output(dev, name, lev, deg, kind):
     """A page-locked y is written by the apply kernel itself (no device-to-host copy); the
     result equals the pageable copy path and the device apply bitwise, in both precisions.
     continuity6 plans take the chunked host path (f in by element chunks, each chunk's ready
-    rows launched as it lands), including when the plan runs kind 5 or 8 on the device."""
+    rows launched as it lands), including when the plan runs kind 5 or 8 on the device; a
+    page-locked f arrives in the gathered order (longest rows' columns first), a pageable one
+    by contiguous chunks, with the same result."""
     pde, table, idx, mats = problem(name, lev, deg)
     plan = _plan(mats, idx, deg)
     if kind is not None:
@@ -254,6 +256,7 @@ def test_host_path_pinned_output(dev, name, lev, deg, kind):
         plan.apply_host(fh.numpy(), yh.numpy())
         pageable = plan.apply_host(fh.numpy().copy())
         assert np.array_equal(yh.numpy(), pageable)
+        assert np.array_equal(plan.apply_host(fh.numpy()), pageable)  # page-locked f (gathered), pageable y
         assert np.array_equal(yh.numpy(), _apply(plan, f, dev, dt).astype(yh.numpy().dtype))
         for _ in range(4):  # repeated buffers: direct, captured into a graph, then replayed
             yh.fill_(float("nan"))
