@@ -8,6 +8,7 @@
 #include <cstring>
 #include <map>
 #include <new>
+#include <queue>
 #include <vector>
 
 #include "asg_internal.h"
@@ -684,36 +685,58 @@ asg_status apply_dev(asg_plan* p, const T* f, T* y, void* stream) {
 // Element chunks of the host-pointer apply (see asg_plan::hc_estart), per precision and
 // arrival order.  Contiguous (g = 0): the table from its end (its coarsest elements, which
 // rows of every level read) towards its start, one copy per chunk.  Gathered (g = 1, f
-// page-locked): rows by length, longest first, each bringing the elements it reads that have
-// not come yet, so the rows that become ready with the last chunk -- those that start only
-// once all of f is in -- are short ones.  A row is ready with the chunk that brings the last
-// of its elements (itself and its columns).  FP32 pieces of N/2, N/4, 3N/20, N/10 elements;
-// FP64, whose apply takes longer than the copy, starts computing earlier: 2N/5, 3N/10, N/5,
-// N/10 (each the fastest of five splits measured on the continuity6 workload).
+// page-locked): the row with the fewest elements still to come next, bringing them, so that
+// rows become ready -- and their y starts over the link -- while f is still arriving.  A row
+// is ready with the chunk that brings the last of its elements (itself and its columns).
+// Chunk sizes, each the fastest of the splits measured on the continuity6 workload: FP32
+// contiguous N/2, N/4, 3N/20, N/10; FP32 gathered 3N/10, N/4, N/4, N/5; FP64 in both orders,
+// its apply taking longer than the copy and so starting earlier, 2N/5, 3N/10, N/5, N/10.
 asg_status host_chunks(asg_plan* p, int prec, bool gathered) {
   const int sch = 2 * gathered + prec;
   if (!p->hc_start[sch].empty()) return ASG_OK;
   const int N = p->N, K = asg_plan::kHostChunks;
-  static const double kFracs[2][K] = {{0.4, 0.7, 0.9, 1.0}, {0.5, 0.75, 0.9, 1.0}};
-  const double* kFrac = kFracs[prec];
+  static const double kFracs[4][K] = {
+      {0.4, 0.7, 0.9, 1.0}, {0.5, 0.75, 0.9, 1.0}, {0.4, 0.7, 0.9, 1.0}, {0.3, 0.55, 0.8, 1.0}};
+  const double* kFrac = kFracs[sch];
   auto len = [&](int i) { return p->row_ptr[i + 1] - p->row_ptr[i]; };
   std::vector<int> order;
   order.reserve(N);
   if (!gathered) {
     for (int i = N - 1; i >= 0; --i) order.push_back(i);
   } else {
-    std::vector<int> by_len(N), cols;
-    for (int i = 0; i < N; ++i) by_len[i] = i;
-    std::stable_sort(by_len.begin(), by_len.end(), [&](int x, int y) { return len(x) > len(y); });
-    std::vector<char> in(N, 0);
-    for (int i : by_len) {
-      cols.assign(1, i);
-      for (long long q = p->row_ptr[i]; q < p->row_ptr[i + 1]; ++q) cols.push_back(p->ent[q] >> 4);
-      std::sort(cols.begin(), cols.end(), [](int x, int y) { return x > y; });
-      for (int j : cols)
+    // next, the row with the fewest elements still to come (ties: the lowest row), which
+    // brings those elements, highest-numbered first
+    std::vector<std::vector<int>> elems(N), users(N);
+    for (int i = 0; i < N; ++i) {
+      elems[i].push_back(i);
+      for (long long q = p->row_ptr[i]; q < p->row_ptr[i + 1]; ++q) elems[i].push_back(p->ent[q] >> 4);
+      std::sort(elems[i].begin(), elems[i].end(), [](int x, int y) { return x > y; });
+      elems[i].erase(std::unique(elems[i].begin(), elems[i].end()), elems[i].end());
+      for (int j : elems[i]) users[j].push_back(i);
+    }
+    std::vector<int> miss(N);
+    std::vector<char> in(N, 0), done(N, 0);
+    using Key = std::pair<int, int>;
+    std::priority_queue<Key, std::vector<Key>, std::greater<Key>> heap;
+    for (int i = 0; i < N; ++i) {
+      miss[i] = static_cast<int>(elems[i].size());
+      heap.push({miss[i], i});
+    }
+    while (!heap.empty()) {
+      const Key top = heap.top();
+      heap.pop();
+      const int i = top.second;
+      if (done[i] || top.first != miss[i]) continue;  // finished, or a stale key
+      done[i] = 1;
+      for (int j : elems[i])
         if (!in[j]) {
           in[j] = 1;
           order.push_back(j);
+          for (int u : users[j])
+            if (!done[u]) {
+              --miss[u];
+              heap.push({miss[u], u});
+            }
         }
     }
   }
@@ -863,14 +886,11 @@ asg_status apply_host(asg_plan* p, const T* hf, T* hy) {
   if (kind == KK_SINGLE_TMA_ROWS) kind = KK_SINGLE_TMA;
   if ((kind == KK_SINGLE_TMA || kind == KK_SINGLE_TMA3 || kind == KK_SINGLE_TMA_X2) && p->N_out == p->N &&
       p->N >= 4 * asg_plan::kHostChunks) {
-    // An FP32 page-locked f with a 16-byte aligned alias arrives in the gathered order (read by
-    // a kernel from the mapped buffer); any other f by copies of contiguous chunks.  FP64 keeps
-    // the contiguous order with a page-locked f too: its apply outlasts the copy, and the
-    // contiguous order makes the most rows ready early (continuity6: 347 us against 374 us
-    // gathered; FP32 100 us against 104 us contiguous).
+    // A page-locked f with a 16-byte aligned alias arrives in the gathered order (read by a
+    // kernel from the mapped buffer); any other f by copies of contiguous chunks (continuity6:
+    // FP32 96 us gathered against 104 us contiguous, FP64 343 us against 346 us).
     const void* kf = host_pinned(hf);
-    const T* gf = sizeof(T) == 4 && kf && (reinterpret_cast<uintptr_t>(kf) & 15) == 0 &&
-                          (p->B * sizeof(T)) % 16 == 0
+    const T* gf = kf && (reinterpret_cast<uintptr_t>(kf) & 15) == 0 && (p->B * sizeof(T)) % 16 == 0
                       ? static_cast<const T*>(kf)
                       : nullptr;
     asg_status st = host_chunks(p, sizeof(T) == 4 ? 1 : 0, gf != nullptr);
