@@ -688,15 +688,15 @@ asg_status apply_dev(asg_plan* p, const T* f, T* y, void* stream) {
 // page-locked): the row with the fewest elements still to come next, bringing them, so that
 // rows become ready -- and their y starts over the link -- while f is still arriving.  A row
 // is ready with the chunk that brings the last of its elements (itself and its columns).
-// Chunk sizes, each the fastest of the splits measured on the continuity6 workload: FP32
-// contiguous N/2, N/4, 3N/20, N/10; FP32 gathered 3N/10, N/4, N/4, N/5; FP64 in both orders,
-// its apply taking longer than the copy and so starting earlier, 2N/5, 3N/10, N/5, N/10.
+// Chunk sizes, each the fastest of the splits measured on the continuity6 workload:
+// contiguous FP32 N/2, N/4, 3N/20, N/10, FP64 (whose apply outlasts the copy, so it gains
+// from starting earlier) 2N/5, 3N/10, N/5, N/10; gathered 3N/10, N/4, N/4, N/5 in both.
 asg_status host_chunks(asg_plan* p, int prec, bool gathered) {
   const int sch = 2 * gathered + prec;
   if (!p->hc_start[sch].empty()) return ASG_OK;
   const int N = p->N, K = asg_plan::kHostChunks;
   static const double kFracs[4][K] = {
-      {0.4, 0.7, 0.9, 1.0}, {0.5, 0.75, 0.9, 1.0}, {0.4, 0.7, 0.9, 1.0}, {0.3, 0.55, 0.8, 1.0}};
+      {0.4, 0.7, 0.9, 1.0}, {0.5, 0.75, 0.9, 1.0}, {0.3, 0.55, 0.8, 1.0}, {0.3, 0.55, 0.8, 1.0}};
   const double* kFrac = kFracs[sch];
   auto len = [&](int i) { return p->row_ptr[i + 1] - p->row_ptr[i]; };
   std::vector<int> order;
@@ -888,7 +888,7 @@ asg_status apply_host(asg_plan* p, const T* hf, T* hy) {
       p->N >= 4 * asg_plan::kHostChunks) {
     // A page-locked f with a 16-byte aligned alias arrives in the gathered order (read by a
     // kernel from the mapped buffer); any other f by copies of contiguous chunks (continuity6:
-    // FP32 96 us gathered against 104 us contiguous, FP64 343 us against 346 us).
+    // FP32 97 us gathered against 104 us contiguous, FP64 312 us against 346 us).
     const void* kf = host_pinned(hf);
     const T* gf = kf && (reinterpret_cast<uintptr_t>(kf) & 15) == 0 && (p->B * sizeof(T)) % 16 == 0
                       ? static_cast<const T*>(kf)
