@@ -227,6 +227,29 @@ class Plan:
             raise TypeError("f must be float64 or float32")
         return y
 
+    def apply_residual(self, f, ystar, r=None, stream=None):
+        """r = A f - ystar (CUDA tensors of one type, three distinct buffers)."""
+        import torch
+
+        if not (f.is_cuda and f.is_contiguous() and f.numel() == self.dof_in):
+            raise ValueError("f must be a contiguous CUDA tensor with %d values" % self.dof_in)
+        if not (ystar.is_cuda and ystar.is_contiguous() and ystar.numel() == self.dof and ystar.dtype == f.dtype):
+            raise ValueError("ystar must be a contiguous CUDA tensor of f's type with %d values" % self.dof)
+        if r is None:
+            r = torch.empty_like(ystar)
+        if r.dtype != f.dtype or not r.is_cuda or r.numel() != self.dof or not r.is_contiguous():
+            raise ValueError("r must be a contiguous CUDA tensor of f's type with %d values" % self.dof)
+        s = stream if stream is not None else torch.cuda.current_stream(f.device)
+        if f.dtype == torch.float64:
+            fn = lib().asg_apply_residual_f64
+        elif f.dtype == torch.float32:
+            fn = lib().asg_apply_residual_f32
+        else:
+            raise TypeError("apply_residual supports float32 and float64")
+        check(fn(self._handle, C.c_void_p(f.data_ptr()), C.c_void_p(ystar.data_ptr()), C.c_void_p(r.data_ptr()),
+                 C.c_void_p(s.cuda_stream)))
+        return r
+
     def apply_T(self, ybar, fbar=None, stream=None):
         """Adjoint on CUDA tensors: fbar = A^T ybar."""
         import torch

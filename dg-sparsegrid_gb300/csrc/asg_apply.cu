@@ -410,12 +410,13 @@ __global__ void __launch_bounds__(256) k_single_mode(ApplyArgs<T> a) {
         }
     }
   }
-  T* yr = a.y + static_cast<size_t>(row) * B + tid * P * P;
+  const size_t y0 = static_cast<size_t>(row) * B + tid * P * P;
+  T* yr = a.y + y0;
 #pragma unroll
   for (int r = 0; r < P; ++r) {
     Row<T, P> rr;
 #pragma unroll
-    for (int c = 0; c < P; ++c) rr.v[c] = nat[r][c];
+    for (int c = 0; c < P; ++c) rr.v[c] = minus_sub(nat[r][c], a.ysub, y0 + r * P + c);
     rr.store(yr + r * P);
   }
 }
@@ -735,16 +736,18 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma(ApplyArgs<T> a) {
     pend = st;
   }
   if (*abort_flag) return;  // y is undefined; the plan's status word reports the timeout
-  T* yr = a.y + static_cast<size_t>(row) * B + nat_base;
+  const size_t y0 = static_cast<size_t>(row) * B + nat_base;
+  T* yr = a.y + y0;
 #pragma unroll
   for (int r = 0; r < P; ++r) {
     if constexpr (F32) {
       *reinterpret_cast<float4*>(reinterpret_cast<float*>(yr) + r * nat_s) =
-          make_float4(n32.v[r][0].x, n32.v[r][0].y, n32.v[r][1].x, n32.v[r][1].y);
+          minus_sub4(make_float4(n32.v[r][0].x, n32.v[r][0].y, n32.v[r][1].x, n32.v[r][1].y),
+                     reinterpret_cast<const float*>(a.ysub), y0 + r * nat_s);
     } else {
       Row<T, P> rr;
 #pragma unroll
-      for (int c = 0; c < P; ++c) rr.v[c] = nat[r][c];
+      for (int c = 0; c < P; ++c) rr.v[c] = minus_sub(nat[r][c], a.ysub, y0 + r * nat_s + c);
       rr.store(yr + r * nat_s);
     }
   }
@@ -948,11 +951,13 @@ __global__ void __launch_bounds__(160, MINB) k_single_tma_x2(ApplyArgs<float> a)
   if (*abort_flag) return;  // y is undefined; the plan's status word reports the timeout
 #pragma unroll
   for (int q = 0; q < NT; ++q) {
-    float* yr = a.y + static_cast<size_t>(row) * B + nat_base[q];
+    const size_t y0 = static_cast<size_t>(row) * B + nat_base[q];
+    float* yr = a.y + y0;
 #pragma unroll
     for (int r = 0; r < P; ++r)
       *reinterpret_cast<float4*>(yr + r * nat_s) =
-          make_float4(n32[q].v[r][0].x, n32[q].v[r][0].y, n32[q].v[r][1].x, n32[q].v[r][1].y);
+          minus_sub4(make_float4(n32[q].v[r][0].x, n32[q].v[r][0].y, n32[q].v[r][1].x, n32[q].v[r][1].y),
+                     a.ysub, y0 + r * nat_s);
   }
 }
 
@@ -1172,16 +1177,18 @@ __global__ void __launch_bounds__(288, MINB) k_single_tma_rows(ApplyArgs<T> a) {
       ++g;
     }
     if (*abort_flag) continue;  // y is undefined; the plan's status word reports the timeout
-    T* yr = a.y + static_cast<size_t>(row) * B + nat_base;
+    const size_t y0 = static_cast<size_t>(row) * B + nat_base;
+    T* yr = a.y + y0;
 #pragma unroll
     for (int r = 0; r < P; ++r) {
       if constexpr (F32) {
         *reinterpret_cast<float4*>(reinterpret_cast<float*>(yr) + r * nat_s) =
-            make_float4(n32.v[r][0].x, n32.v[r][0].y, n32.v[r][1].x, n32.v[r][1].y);
+            minus_sub4(make_float4(n32.v[r][0].x, n32.v[r][0].y, n32.v[r][1].x, n32.v[r][1].y),
+                       reinterpret_cast<const float*>(a.ysub), y0 + r * nat_s);
       } else {
         Row<T, P> rr;
 #pragma unroll
-        for (int c = 0; c < P; ++c) rr.v[c] = nat[r][c];
+        for (int c = 0; c < P; ++c) rr.v[c] = minus_sub(nat[r][c], a.ysub, y0 + r * nat_s + c);
         rr.store(yr + r * nat_s);
       }
     }

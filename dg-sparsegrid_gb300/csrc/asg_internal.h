@@ -65,6 +65,7 @@ struct ApplyArgs {
   const int* cta_ptr;        // [nctas+1] persistent single-mode kernel: rows of CTA c are
   const int* cta_rows;       //   cta_rows[cta_ptr[c] .. cta_ptr[c+1]) (static LPT assignment)
   int nctas;
+  const T* ysub;             // NULL, or a vector laid out like y: the kernels store A f - ysub
 };
 
 template <typename T>
@@ -131,6 +132,7 @@ struct StreamArgs {
   int ws_stride;          // int4 per CTA: 1 + entries rounded up to 32
   int nctas;
   int* err;
+  const float* ysub;      // NULL, or a vector laid out like y: the kernel stores A f - ysub
 };
 // Dynamic shared memory and resident CTAs per SM of the streaming kernel (0 on error).
 size_t stream_smem();

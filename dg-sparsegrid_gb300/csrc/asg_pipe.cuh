@@ -9,6 +9,23 @@
 
 namespace asg {
 
+// The value a kernel stores for y: v, or v - s[i] for a residual apply (s = ApplyArgs::ysub,
+// i the value's index in y).
+template <typename T>
+__device__ __forceinline__ T minus_sub(T v, const T* s, size_t i) {
+  return s ? v - s[i] : v;
+}
+__device__ __forceinline__ float4 minus_sub4(float4 v, const float* s, size_t i) {
+  if (s) {
+    const float4 q = *reinterpret_cast<const float4*>(s + i);
+    v.x -= q.x;
+    v.y -= q.y;
+    v.z -= q.z;
+    v.w -= q.w;
+  }
+  return v;
+}
+
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }

@@ -653,8 +653,20 @@ int effective_kind(const asg_plan* p) {
   return ((k == KK_STREAM || k == KK_SINGLE_TMA_X2) && sizeof(T) == 8) ? KK_SINGLE_TMA : k;
 }
 
+// y -= s over n values: the residual step of the kernel families that store A f only.
 template <typename T>
-asg_status apply_dev(asg_plan* p, const T* f, T* y, void* stream) {
+__global__ void k_sub_inplace(T* __restrict__ y, const T* __restrict__ s, long long n) {
+  for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
+       i += static_cast<long long>(gridDim.x) * blockDim.x)
+    y[i] -= s[i];
+}
+
+// y = A f, or with ysub (laid out like y, not aliasing it) the residual y = A f - ysub: in the
+// apply's own stores for the single-mode bulk-copy, fiber and streaming kinds (2, 3, 4, 5, 7,
+// 8), by a second launch for the chain and small-block kinds (0, 1, 6), whose register
+// budgets the extra operand would change.  Either way y = (A f) - ysub, rounded once.
+template <typename T>
+asg_status apply_dev(asg_plan* p, const T* f, T* y, void* stream, const T* ysub = nullptr) {
   if (!p) return fail(ASG_ERR_INVALID, "apply: NULL plan");
   asg_status st = check_ptr(f, "f");
   if (st) return st;
@@ -666,6 +678,7 @@ asg_status apply_dev(asg_plan* p, const T* f, T* y, void* stream) {
     StreamArgs sa{};
     sa.f = reinterpret_cast<const float*>(f);
     sa.y = reinterpret_cast<float*>(y);
+    sa.ysub = reinterpret_cast<const float*>(ysub);
     sa.ops_cols = p->d_ops_cols;
     sa.ws = reinterpret_cast<const int4*>(p->d_ws);
     sa.ws_stride = p->ws_stride;
@@ -677,9 +690,26 @@ asg_status apply_dev(asg_plan* p, const T* f, T* y, void* stream) {
   }
   const T* ops = sizeof(T) == 8 ? reinterpret_cast<const T*>(p->d_ops64) : reinterpret_cast<const T*>(p->d_ops32);
   ApplyArgs<T> a = make_args<T>(p, f, y, ops);
+  const bool second = ysub && (kind == KK_CHAIN_WARP || kind == KK_CHAIN_CTA || kind == KK_SINGLE_SMALL);
+  a.ysub = second ? nullptr : ysub;
   cudaError_t e = launch_apply<T>(a, p->P, kind, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "apply kernel launch");
+  if (second) {
+    const long long n = static_cast<long long>(p->N_out) * p->B;
+    const int grid = static_cast<int>(std::min<long long>((n + 255) / 256, 152 * 8));
+    if (n > 0) k_sub_inplace<T><<<grid, 256, 0, static_cast<cudaStream_t>(stream)>>>(y, ysub, n);
+    if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "residual kernel launch");
+  }
   return ASG_OK;
+}
+
+template <typename T>
+asg_status apply_residual(asg_plan* p, const T* f, const T* ystar, T* r, void* stream) {
+  if (!p) return fail(ASG_ERR_INVALID, "apply_residual: NULL plan");
+  asg_status st = check_ptr(ystar, "ystar");
+  if (st) return st;
+  if (ystar == f || ystar == r) return fail(ASG_ERR_INVALID, "apply_residual: ystar must alias neither f nor r");
+  return apply_dev<T>(p, f, r, stream, ystar);
 }
 
 // Element chunks of the host-pointer apply (see asg_plan::hc_estart), per precision and
@@ -1576,6 +1606,12 @@ asg_status asg_apply_T_f32(asg_plan* p, const float* ybar, float* fbar, void* st
 
 asg_status asg_apply_f64(asg_plan* p, const double* f, double* y, void* stream) { return asg::apply_dev<double>(p, f, y, stream); }
 asg_status asg_apply_f32(asg_plan* p, const float* f, float* y, void* stream) { return asg::apply_dev<float>(p, f, y, stream); }
+asg_status asg_apply_residual_f64(asg_plan* p, const double* f, const double* ystar, double* r, void* stream) {
+  return asg::apply_residual<double>(p, f, ystar, r, stream);
+}
+asg_status asg_apply_residual_f32(asg_plan* p, const float* f, const float* ystar, float* r, void* stream) {
+  return asg::apply_residual<float>(p, f, ystar, r, stream);
+}
 asg_status asg_apply_host_f64(asg_plan* p, const double* f, double* y) { return asg::apply_host<double>(p, f, y); }
 asg_status asg_apply_host_f32(asg_plan* p, const float* f, float* y) { return asg::apply_host<float>(p, f, y); }
 

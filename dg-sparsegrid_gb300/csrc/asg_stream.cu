@@ -166,9 +166,11 @@ __global__ void __launch_bounds__(288, 1) k_stream(StreamArgs a) {
     const int4 e = desc(k);
     const int fl = e.w;
     if (fl & SF_ZERO) {
-      float* yr = a.y + static_cast<size_t>(e.y) * kB + nat_base;
+      const size_t y0 = static_cast<size_t>(e.y) * kB + nat_base;
+      float* yr = a.y + y0;
 #pragma unroll
-      for (int r = 0; r < 4; ++r) *reinterpret_cast<float4*>(yr + r * nat_s) = make_float4(0.f, 0.f, 0.f, 0.f);
+      for (int r = 0; r < 4; ++r)
+        *reinterpret_cast<float4*>(yr + r * nat_s) = minus_sub4(make_float4(0.f, 0.f, 0.f, 0.f), a.ysub, y0 + r * nat_s);
       continue;
     }
     if (fl & SF_GRP0) {
@@ -227,11 +229,12 @@ __global__ void __launch_bounds__(288, 1) k_stream(StreamArgs a) {
     }
     if (fl & SF_ROW1) {
       if (live) {
-        float* yr = a.y + static_cast<size_t>(e.y) * kB + nat_base;
+        const size_t y0 = static_cast<size_t>(e.y) * kB + nat_base;
+        float* yr = a.y + y0;
 #pragma unroll
         for (int r = 0; r < 4; ++r)
           *reinterpret_cast<float4*>(yr + r * nat_s) =
-              make_float4(n.v[r][0].x, n.v[r][0].y, n.v[r][1].x, n.v[r][1].y);
+              minus_sub4(make_float4(n.v[r][0].x, n.v[r][0].y, n.v[r][1].x, n.v[r][1].y), a.ysub, y0 + r * nat_s);
         __syncwarp();
         if (lane == 0) mbar_arrive(&rempty[rows & 1]);
       }

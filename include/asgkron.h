@@ -171,6 +171,15 @@ asg_status asg_plan_device_status(asg_plan* plan, int* status);
  * accumulation across the column reduction. */
 asg_status asg_apply_f64(asg_plan* plan, const double* d_f, double* d_y, void* stream);
 asg_status asg_apply_f32(asg_plan* plan, const float* d_f, float* d_y, void* stream);
+/* Residual: r = A*f - ystar (device pointers, ystar laid out like y; the three buffers
+ * distinct).  Bitwise the apply followed by an elementwise subtraction in the same
+ * precision; one launch for the single-mode deg-3/4 kernels (subtracted as y is stored),
+ * two for the others.  The first step of the gradient of L = 1/2 ||A f - ystar||^2 (r is then
+ * the cotangent of asg_apply_T_* and asg_grad_ops_*).  No reference counterpart. */
+asg_status asg_apply_residual_f64(asg_plan* plan, const double* d_f, const double* d_ystar, double* d_r,
+                                  void* stream);
+asg_status asg_apply_residual_f32(asg_plan* plan, const float* d_f, const float* d_ystar, float* d_r,
+                                  void* stream);
 /* Adjoint: fbar = A^T * ybar (device pointers).  No reference counterpart (the prototype has
  * no adjoint); built from the transposed operator blocks and the transposed work list. */
 asg_status asg_apply_T_f64(asg_plan* plan, const double* d_ybar, double* d_fbar, void* stream);

@@ -148,6 +148,31 @@ def test_continuity6_lev4_deg4_kernels_agree(dev):
     assert rel2(y_none, y_single) <= FP64_TOL
 
 
+@pytest.mark.parametrize("name,lev,deg,kinds", [("continuity6", 3, 4, [3, 4, 5, 7, 8, 2, 1]),
+                                               ("continuity2", 4, 2, [6, 0, 1]), ("continuity3", 4, 3, [6, 0, 1])])
+def test_apply_residual_equals_apply_minus_ystar(dev, name, lev, deg, kinds):
+    """asg_apply_residual_*: r = A f - y* equals the apply followed by a subtraction in the same
+    precision, bitwise, for every kernel family the plan can run (subtracted in the apply's
+    own stores for kinds 2-5, 7, 8; a second launch for kinds 0, 1, 6), in both precisions."""
+    import asgkron
+
+    pde, table, idx, mats = problem(name, lev, deg)
+    p = _plan(mats, idx, deg)
+    rng = np.random.default_rng(5)
+    f, ys = rng.standard_normal(p.dof), rng.standard_normal(p.dof)
+    for kind in kinds:
+        p.set_kernel(kind)
+        for dt in (torch.float64, torch.float32):
+            ft, yst = torch.from_numpy(f).to(dev, dt), torch.from_numpy(ys).to(dev, dt)
+            want = p.apply(ft) - yst
+            r = p.apply_residual(ft, yst)
+            torch.cuda.synchronize()
+            assert torch.equal(r, want), (kind, dt)
+    assert p.device_status() == 0
+    with pytest.raises(asgkron.AsgError):
+        p.apply_residual(ft, yst, yst)  # r must not alias ystar
+
+
 @pytest.mark.parametrize("name,lev,deg", [("continuity2", 4, 2), ("continuity2", 3, 4), ("continuity3", 4, 3),
                                           ("continuity3", 3, 4), ("diffusion2", 5, 4), ("continuity6", 2, 2),
                                           ("continuity3", 2, 6)])
