@@ -944,6 +944,15 @@ def run_sharded(args, rank, world, local):
     e2e_ms = float(t.item())
     halo = torch.tensor([float(sh.halo.size)], device=dev)
     dist.all_reduce(halo)
+    # roofline as on one GPU: the job's compulsory bytes (f read, y written, operators, pair
+    # list) over the slowest rank's step, against the ranks' summed measured HBM bandwidth
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peak, peak_src = float(json.load(open(peaks_path))["hbm_gbs"]) * world, "of measured (x %d GPUs)" % world
+    else:
+        peak, peak_src = FALLBACK_HBM_GBS * world, "of fallback (x %d GPUs)" % world
+    alg = algorithmic_bytes(4, dof, len(mats), D, np.asarray(mats[0][0]).shape[0], N, N * N)
+    achieved = alg / (step_ms * 1e-3) / 1e9
     if rank == 0:
         print(json.dumps({
             "metric": METRIC, "value": dof / (step_ms * 1e-3) / 1e9, "unit": UNIT, "n_gpus": world,
@@ -953,6 +962,8 @@ def run_sharded(args, rank, world, local):
                                        "step" % world,
                         "ranges": [[int(a), int(b)] for a, b in ranges],
                         "halo_blocks_total": int(halo.item()), "all_gather_blocks_would_be": (world - 1) * N},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": None, "peak_source": peak_src, "algorithmic_bytes_per_launch": alg},
             "e2e": {"value": dof / (e2e_ms * 1e-3) / 1e9, "unit": UNIT, "h2d_bytes_per_step": 4 * dof,
                     "d2h_bytes_per_step": 4 * dof, "ms_per_step": e2e_ms},
             "gpu_launches": args.steps * world,
