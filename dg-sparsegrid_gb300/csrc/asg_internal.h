@@ -240,9 +240,9 @@ struct asg_plan {
   std::vector<int> hc_estart[4], hc_start[4];
   int* d_hc_rows[4] = {};
   int* d_hc_order[4] = {};
-  cudaStream_t cstream[2] = {nullptr, nullptr};
+  cudaStream_t cstream[kHostChunks] = {};  // one compute stream per chunk
   cudaEvent_t ev_in[kHostChunks] = {};
-  cudaEvent_t ev_done[2] = {nullptr, nullptr};
+  cudaEvent_t ev_done[kHostChunks] = {};
   // the chunked host apply as one CUDA graph, replayed while the caller repeats its page-locked
   // f and y buffers (captured at the second call with the same buffers, kernel and precision)
   cudaGraphExec_t hg_exec = nullptr;

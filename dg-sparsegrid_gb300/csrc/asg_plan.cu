@@ -93,7 +93,7 @@ void free_device(asg_plan* p) {
     cudaFree(p->d_hc_rows[k]);
     cudaFree(p->d_hc_order[k]);
   }
-  for (int k = 0; k < 2; ++k) {
+  for (int k = 0; k < asg_plan::kHostChunks; ++k) {
     if (p->cstream[k]) cudaStreamDestroy(p->cstream[k]);
     if (p->ev_done[k]) cudaEventDestroy(p->ev_done[k]);
   }
@@ -791,7 +791,7 @@ asg_status host_chunks(asg_plan* p, int prec, bool gathered) {
   asg_status st = upload(&p->d_hc_rows[sch], all);
   if (!st && gathered) st = upload(&p->d_hc_order[sch], order);
   if (st) return st;
-  for (int k = 0; k < 2; ++k) {
+  for (int k = 0; k < asg_plan::kHostChunks; ++k) {
     if (!p->cstream[k]) ASG_CUDA(cudaStreamCreateWithFlags(&p->cstream[k], cudaStreamNonBlocking));
     if (!p->ev_done[k]) ASG_CUDA(cudaEventCreateWithFlags(&p->ev_done[k], cudaEventDisableTiming));
   }
@@ -836,9 +836,10 @@ const void* host_pinned(const void* h) {
 }
 
 // The chunked host apply on the plan's streams: f by element chunks on p->stream (copies,
-// or with kf -- f's device alias -- the gather kernel), each chunk's ready rows on one of two
-// compute streams once the chunk has landed, then (y not mapped) one copy of y back; joined
-// on p->stream.  No synchronisation (capturable).
+// or with kf -- f's device alias -- the gather kernel), each chunk's ready rows on the
+// chunk's own compute stream once the chunk has landed (so no chunk's rows wait for an
+// earlier chunk's last rows), then (y not mapped) one copy of y back; joined on p->stream.
+// No synchronisation (capturable).
 template <typename T>
 asg_status host_pipeline(asg_plan* p, int kind, const T* hf, const T* kf, T* df, T* hy, T* ky, T* dy, size_t ny) {
   const int K = asg_plan::kHostChunks, N = p->N, pk = sizeof(T) == 4 ? 1 : 0, sch = 2 * (kf != nullptr) + pk;
@@ -861,7 +862,7 @@ asg_status host_pipeline(asg_plan* p, int kind, const T* hf, const T* kf, T* df,
   }
   const T* ops = sizeof(T) == 8 ? reinterpret_cast<const T*>(p->d_ops64) : reinterpret_cast<const T*>(p->d_ops32);
   for (int c = 0; c < K; ++c) {
-    cudaStream_t cs = p->cstream[c & 1];
+    cudaStream_t cs = p->cstream[c];
     ASG_CUDA(cudaStreamWaitEvent(cs, p->ev_in[c], 0));
     const int r0 = start[c], r1 = start[c + 1];
     if (r1 > r0) {
@@ -872,7 +873,7 @@ asg_status host_pipeline(asg_plan* p, int kind, const T* hf, const T* kf, T* df,
       if (e != cudaSuccess) return cuda_fail(e, "apply kernel launch");
     }
   }
-  for (int k = 0; k < 2; ++k) {
+  for (int k = 0; k < K; ++k) {
     ASG_CUDA(cudaEventRecord(p->ev_done[k], p->cstream[k]));
     ASG_CUDA(cudaStreamWaitEvent(p->stream, p->ev_done[k], 0));
   }
@@ -909,7 +910,7 @@ asg_status apply_host(asg_plan* p, const T* hf, T* hy) {
     cudaGetLastError();  // clear a query error for host memory the runtime does not know
   // The one-CTA-per-row bulk-copy kernels (kinds 3, 4, 8; kind 5 runs kind 3's arithmetic)
   // take a row list, so the copy of f can overlap the apply: f comes in by element chunks
-  // on the plan's stream, and each chunk's ready rows launch on one of two compute streams as
+  // on the plan's stream, and each chunk's ready rows launch on the chunk's compute stream as
   // soon as their last block has landed, writing y (over the host link when y is mapped)
   // while later chunks are still arriving.  Same kernel per row, same result.
   int kind = effective_kind<T>(p);
