@@ -838,7 +838,8 @@ def small_config_graph(dev):
     out = {"dof": plan.dof, "us_per_apply": us, "value": plan.dof / (us * 1e-6) / 1e9,
            "kernel": asgkron._lib.KERNEL_NAMES[plan.stats()["kernel_kind"]]}
     # the configuration's five explicit RK3 steps at CFL 0.01 (sources included), one step
-    # captured in a CUDA graph and replayed five times per timed pass
+    # captured in a CUDA graph and replayed five times per timed pass, each replay after the
+    # upload of its stage times' source factors
     from asgkron.steppers import RK3Stepper
 
     dt = pde.dt(0.01)
@@ -859,7 +860,7 @@ def small_config_graph(dev):
         torch.cuda.synchronize()
         ts.append(t0.elapsed_time(t1) * 1e3 / 5)
     out["rk3_step_us"] = statistics.median(ts)
-    out["rk3_launches_per_step"] = 9  # 3 source combinations, 3 applies, 3 stage updates; one graph
+    out["rk3_launches_per_step"] = 1  # sources, three applies and the stage updates in one cooperative launch
     plan.close()
     return out
 

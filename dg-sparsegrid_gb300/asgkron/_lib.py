@@ -173,6 +173,8 @@ SIGNATURES = {
     "asg_batch_info": (C.c_int, [C.c_void_p, _I, _I, C.POINTER(C.c_double)]),
     "asg_rk3_step_f64": (C.c_int, [C.c_void_p, _P, C.c_double, C.POINTER(C.c_void_p), _P, C.c_size_t, _P]),
     "asg_rk3_step_f32": (C.c_int, [C.c_void_p, _P, C.c_double, C.POINTER(C.c_void_p), _P, C.c_size_t, _P]),
+    "asg_rk3_step_sources_f64": (C.c_int, [C.c_void_p, _P, C.c_double, C.c_int, _P, _P, _P, C.c_size_t, _P]),
+    "asg_rk3_step_sources_f32": (C.c_int, [C.c_void_p, _P, C.c_double, C.c_int, _P, _P, _P, C.c_size_t, _P]),
     "asg_lincomb_f64": (C.c_int, [C.c_longlong, C.c_int, _P, _P, _P, _P]),
     "asg_be_workspace": (C.c_int, [C.c_void_p, C.POINTER(GmresOpts), C.POINTER(C.c_size_t)]),
     "asg_be_solve": (C.c_int, [C.c_void_p, C.c_double, _P, _P, C.POINTER(GmresOpts), C.POINTER(GmresInfo), _P,

@@ -36,49 +36,33 @@ class RK3Stepper:
         # a ring of page-locked sources for the time factors: a replay queued while an earlier
         # one's copy has not run yet must not overwrite that copy's source
         self.coef_ring = [torch.zeros(3 * max(ns, 1), dtype=torch.float64).pin_memory() for _ in range(4)]
-        self.coef_done = [None] * 4
+        self.coef_np = [r.numpy() for r in self.coef_ring]  # written in place, no tensor per step
+        self.coef_done = [torch.cuda.Event() for _ in range(4)]
+        self.coef_used = [False] * 4
         self._slot = 0
-        self.src64 = [torch.zeros(self.n, dtype=torch.float64, device=dev) for _ in range(3)]
-        self.src = self.src64 if self.torch_dtype == torch.float64 else [
-            torch.zeros(self.n, dtype=torch.float32, device=dev) for _ in range(3)]
         per = 16 // (8 if self.torch_dtype == torch.float64 else 4)  # values per 16 bytes
         self.work = torch.empty(4 * ((self.n + per - 1) // per * per), dtype=self.torch_dtype, device=dev)
         self.graph = None
         self._f_static = None
 
-    def _sources(self, stream):
-        import torch
-
-        if self.ns == 0:
-            return None
-        for k in range(3):
-            check(lib().asg_lincomb_f64(self.n, self.ns, C.c_void_p(self.coef.data_ptr() + 8 * k * self.ns),
-                                        C.c_void_p(self.vec_ptrs.data_ptr()), C.c_void_p(self.src64[k].data_ptr()),
-                                        C.c_void_p(stream.cuda_stream)))
-            if self.torch_dtype != torch.float64:
-                self.src[k].copy_(self.src64[k])
-        return (C.c_void_p * 3)(*[x.data_ptr() for x in self.src])
-
     def _set_time(self, t, dt):
-        import torch
-
         if self.ns == 0:
             return
-        vals = [fn(tt) for tt in (t, t + 0.5 * dt, t + dt) for fn in self.tfac]
         k = self._slot
-        if self.coef_done[k] is not None:
+        if self.coef_used[k]:
             self.coef_done[k].synchronize()
-        self.coef_ring[k].copy_(torch.tensor(vals, dtype=torch.float64))
+        self.coef_np[k][:] = [fn(tt) for tt in (t, t + 0.5 * dt, t + dt) for fn in self.tfac]
         self.coef.copy_(self.coef_ring[k], non_blocking=True)
-        ev = torch.cuda.Event()
-        ev.record()
-        self.coef_done[k] = ev
+        self.coef_done[k].record()
+        self.coef_used[k] = True
         self._slot = (k + 1) % len(self.coef_ring)
 
     def _launch(self, f, dt, stream):
-        src = self._sources(stream)
-        fn = lib().asg_rk3_step_f64 if self.torch_dtype.itemsize == 8 else lib().asg_rk3_step_f32
-        check(fn(self.plan.handle, C.c_void_p(f.data_ptr()), float(dt), src, C.c_void_p(self.work.data_ptr()),
+        # the stage sources (sum of the spatial parts times their time factors, read from the
+        # device) are formed inside the step
+        fn = lib().asg_rk3_step_sources_f64 if self.torch_dtype.itemsize == 8 else lib().asg_rk3_step_sources_f32
+        check(fn(self.plan.handle, C.c_void_p(f.data_ptr()), float(dt), self.ns, C.c_void_p(self.coef.data_ptr()),
+                 C.c_void_p(self.vec_ptrs.data_ptr()), C.c_void_p(self.work.data_ptr()),
                  self.work.numel() * self.work.element_size(), C.c_void_p(stream.cuda_stream)))
 
     def step(self, f, t, dt):

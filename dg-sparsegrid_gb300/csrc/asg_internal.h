@@ -223,6 +223,7 @@ struct asg_plan {
   int* d_fz_int[2] = {nullptr, nullptr};  // blk_row[G+1], blk_slot[G+1], row_slot[N+1], warp_item[G*W+1]
   asg::FzItem* d_fz_items[2] = {nullptr, nullptr};
   int* d_err = nullptr;
+  unsigned* d_bar = nullptr;  // grid barrier words of the fused RK3 step (zeroed per launch)
   double* d_ops64 = nullptr;
   float* d_ops32 = nullptr;
   // host-pointer apply path (staging owned by the plan)

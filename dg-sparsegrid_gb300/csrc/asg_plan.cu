@@ -86,6 +86,7 @@ void free_device(asg_plan* p) {
     cudaFree(p->d_fz_items[k]);
   }
   cudaFree(p->d_err);
+  cudaFree(p->d_bar);
   cudaFree(p->d_io);
   if (p->stream) cudaStreamDestroy(p->stream);
   if (p->hg_exec) cudaGraphExecDestroy(p->hg_exec);
@@ -402,6 +403,7 @@ asg_status finalize(asg_plan* p, bool ops) {
   if ((st = upload(&p->d_ent, p->ent))) return st;
   if ((st = upload(&p->d_ed, p->ed))) return st;
   if (!p->d_err) ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_err), sizeof(int)));
+  if (!p->d_bar) ASG_CUDA(cudaMalloc(reinterpret_cast<void**>(&p->d_bar), 4 * sizeof(unsigned)));
   ASG_CUDA(cudaMemset(p->d_err, 0, sizeof(int)));
   return ASG_OK;
 }

@@ -39,25 +39,51 @@ __device__ __forceinline__ double warp_sum_partials(const double* __restrict__ p
 //   stage 2: k2 = A y + s2;             y = f + dt (-k1 + 2 k2)
 //   stage 3: k3 = A y + s3;             f = f + dt (k1/6 + 2 k2/3 + k3/6)
 // ---------------------------------------------------------------------------------------
+// The stage sources of an RK3 step: three precomputed vectors (or NULL), or ns device vectors
+// combined with the stage's ns device coefficients (coef[3*ns]: t, t + dt/2, t + dt), summed
+// in FP64 as asg_lincomb_f64 sums them and rounded once to the step's type.
+template <typename T>
+struct Rk3Src {
+  const T* src[3];
+  int ns;
+  const double* coef;
+  const double* const* vecs;
+};
+template <typename T>
+__device__ __forceinline__ T rk3_source(const Rk3Src<T>& S, int k, long long i) {
+  if (S.ns > 0) {
+    double acc = 0.0;
+    for (int q = 0; q < S.ns; ++q) acc = fma(S.coef[k * S.ns + q], S.vecs[q][i], acc);
+    return static_cast<T>(acc);
+  }
+  return S.src[k] ? S.src[k][i] : T(0);
+}
+
+// One value's update after a stage's operator application v (= (A x)_i) with the stage's
+// source si: the stage kernel and the fused step both call it, so the two paths round alike.
+template <typename T>
+__device__ __forceinline__ void rk3_update(int stage, long long i, T v, T dt, T si, T* f, T* y, T* k1, T* k2) {
+  if (stage == 1) {
+    const T a = v + si;
+    k1[i] = a;
+    y[i] = f[i] + dt * T(0.5) * a;
+  } else if (stage == 2) {
+    const T b = v + si;
+    k2[i] = b;
+    y[i] = f[i] + dt * (T(-1) * k1[i] + T(2) * b);
+  } else {
+    const T c = v + si;
+    f[i] = f[i] + dt * (k1[i] / T(6) + T(2) / T(3) * k2[i] + c / T(6));
+  }
+}
+
 template <typename T>
 __global__ void k_rk3_stage(int stage, long long n, T dt, T* __restrict__ f, T* __restrict__ y, T* __restrict__ k1,
-                            T* __restrict__ k2, T* __restrict__ k3, const T* __restrict__ s) {
+                            T* __restrict__ k2, T* __restrict__ k3, Rk3Src<T> S) {
+  const T* kv = stage == 1 ? k1 : (stage == 2 ? k2 : k3);
   for (long long i = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; i < n;
-       i += static_cast<long long>(gridDim.x) * blockDim.x) {
-    const T si = s ? s[i] : T(0);
-    if (stage == 1) {
-      const T a = k1[i] + si;
-      k1[i] = a;
-      y[i] = f[i] + dt * T(0.5) * a;
-    } else if (stage == 2) {
-      const T b = k2[i] + si;
-      k2[i] = b;
-      y[i] = f[i] + dt * (T(-1) * k1[i] + T(2) * b);
-    } else {
-      const T c = k3[i] + si;
-      f[i] = f[i] + dt * (k1[i] / T(6) + T(2) / T(3) * k2[i] + c / T(6));
-    }
-  }
+       i += static_cast<long long>(gridDim.x) * blockDim.x)
+    rk3_update(stage, i, kv[i], dt, rk3_source(S, stage - 1, i), f, y, k1, k2);
 }
 
 // out = sum_s c[s] * v[s]  (sources s(t) = sum_s c_s(t) v_s, c on the device)
@@ -380,6 +406,106 @@ __device__ bool grid_sync(unsigned* bar, unsigned& target, bool withhold = false
   }
   __syncthreads();
   return s_ok != 0;
+}
+
+// ---------------------------------------------------------------------------------------
+// One RK3 step in one cooperative launch, for plans whose apply is the split fiber kernel
+// (small blocks, one applied factor per term).  Each stage applies the operator to its input
+// row by row exactly as k_single_fiber_split does (same warps per row, same partial order) and
+// updates the row's values at once with rk3_update; two grid barriers separate the stages.
+// The stage-2 input (y1) and output (y2) are distinct vectors, so a stage never writes what
+// another CTA may still be reading.  Results equal the nine-launch step bitwise.
+// ---------------------------------------------------------------------------------------
+template <typename T>
+struct Rk3Args {
+  ApplyArgs<T> a;      // the plan's apply arguments (f and y unused)
+  T* f;                // the state, advanced in place
+  Rk3Src<T> S;         // the stage sources
+  T* k1;
+  T* k2;
+  T* y1;               // stage-1 output, stage-2 input
+  T* y2;               // stage-2 output, stage-3 input
+  T dt;
+  unsigned* bar;       // grid barrier words, zeroed before the launch
+};
+
+template <typename T, int P, int MAXF, bool KAHAN, int WR>
+__global__ void __launch_bounds__(32 * WR) k_rk3_fused(Rk3Args<T> r) {
+  __shared__ __align__(16) T part[WR][256];
+  const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
+  const ApplyArgs<T>& a = r.a;
+  const int B = a.B;
+  const FiberLane<MAXF> fl = fiber_lane<T, P, MAXF>(a, lane);
+  unsigned target = 0;
+  for (int stage = 1; stage <= 3; ++stage) {
+    const T* x = stage == 1 ? r.f : (stage == 2 ? r.y1 : r.y2);
+    T* yout = stage == 1 ? r.y1 : r.y2;
+    for (int row = blockIdx.x; row < a.N; row += gridDim.x) {
+      fiber_chunk<T, P, MAXF, KAHAN>(a, x, a.row_ptr[row], a.row_ptr[row + 1], fl, part[warp], warp * fl.Gf,
+                                     WR * fl.Gf);
+      __syncthreads();
+      for (int e = threadIdx.x; e < B; e += 32 * WR) {
+        T v = part[0][e];
+#pragma unroll
+        for (int w = 1; w < WR; ++w) v += part[w][e];
+        const long long i = static_cast<long long>(row) * B + e;
+        rk3_update(stage, i, v, r.dt, rk3_source(r.S, stage - 1, i), r.f, yout, r.k1, r.k2);
+      }
+      __syncthreads();
+    }
+    if (stage < 3 && !grid_sync(r.bar, target)) {
+      if (threadIdx.x == 0) atomicExch(a.err, static_cast<int>(ASG_ERR_TIMEOUT));
+      return;
+    }
+  }
+}
+
+template <typename T, int P>
+cudaError_t launch_rk3_fused_p(const Rk3Args<T>& r, cudaStream_t s) {
+  constexpr int WR = sizeof(T) == 4 ? 4 : 2;  // the split fiber kernel's warps per row
+  constexpr bool K = sizeof(T) == 4;
+  const int Lf = r.a.B / P;
+  auto go = [&](auto maxf) -> cudaError_t {
+    constexpr int MF = decltype(maxf)::value;
+    auto kern = k_rk3_fused<T, P, MF, K, WR>;
+    static long long resident = -1;  // co-resident CTAs, queried once per instantiation
+    if (resident < 0) {
+      int dev = 0, nsm = 0, coop = 0, per_sm = 0;
+      cudaError_t e;
+      if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+      if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+      if ((e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev)) != cudaSuccess) return e;
+      if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * WR, 0)) != cudaSuccess) return e;
+      resident = coop ? static_cast<long long>(per_sm) * nsm : 0;
+    }
+    const int G = static_cast<int>(std::min<long long>(r.a.N, std::min<long long>(resident, 152 * 16)));
+    if (G <= 0) return cudaErrorNotSupported;
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(G);
+    cfg.blockDim = dim3(32 * WR);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kern, r);
+  };
+  if (Lf <= 32) return go(std::integral_constant<int, 1>{});
+  if (Lf <= 64) return go(std::integral_constant<int, 2>{});
+  return go(std::integral_constant<int, 4>{});
+}
+
+template <typename T>
+cudaError_t launch_rk3_fused(const Rk3Args<T>& r, int P, cudaStream_t s) {
+  switch (P) {
+    case 1: return launch_rk3_fused_p<T, 1>(r, s);
+    case 2: return launch_rk3_fused_p<T, 2>(r, s);
+    case 3: return launch_rk3_fused_p<T, 3>(r, s);
+    case 4: return launch_rk3_fused_p<T, 4>(r, s);
+    default: return cudaErrorNotSupported;
+  }
 }
 
 // Sum over the CTA of one value per thread, fixed order; the result goes to every thread.
@@ -1211,7 +1337,7 @@ asg_status be_solve(asg_plan* p, double dt, const double* b, double* x, const as
 }
 
 template <typename T>
-asg_status rk3(asg_plan* p, T* f, double dt, const T* const* src, T* work, size_t work_bytes, void* stream) {
+asg_status rk3(asg_plan* p, T* f, double dt, const asg::Rk3Src<T>& S, T* work, size_t work_bytes, void* stream) {
   if (!p || !f || !work) return fail(ASG_ERR_INVALID, "rk3_step: NULL argument");
   asg_plan_stats st{};
   asg_plan_stats_get(p, &st);
@@ -1231,16 +1357,32 @@ asg_status rk3(asg_plan* p, T* f, double dt, const T* const* src, T* work, size_
                           : asg_apply_f32(p, reinterpret_cast<const float*>(in), reinterpret_cast<float*>(out), s);
   };
   const int gr = asg::grid_for(n);
-  const T* s1 = src ? src[0] : nullptr;
-  const T* s2 = src ? src[1] : nullptr;
-  const T* s3 = src ? src[2] : nullptr;
+  // plans applied by the split fiber kernel: the whole step in one cooperative launch
+  int kind = -1;
+  asg_plan_kernel_for(p, sizeof(T) == 4 ? 1 : 0, &kind);
+  asg::Rk3Args<T> r{};
+  if (kind == asg::KK_SINGLE_SMALL && p->P <= 4 && p->d_bar && asg::small_plan_args<T>(p, &r.a)) {
+    r.f = f;
+    r.S = S;
+    r.k1 = k1;
+    r.k2 = k2;
+    r.y1 = k3;
+    r.y2 = y;
+    r.dt = static_cast<T>(dt);
+    r.bar = p->d_bar;
+    cudaError_t e = cudaMemsetAsync(p->d_bar, 0, 4 * sizeof(unsigned), s);
+    if (e != cudaSuccess) return asg::cuda_fail(e, "rk3 barrier reset");
+    e = asg::launch_rk3_fused<T>(r, p->P, s);
+    if (e == cudaSuccess) return ASG_OK;
+    if (e != cudaErrorNotSupported) return asg::cuda_fail(e, "fused rk3 launch");
+  }
   asg_status a;
   if ((a = apply(f, k1))) return a;
-  asg::k_rk3_stage<T><<<gr, 256, 0, s>>>(1, n, static_cast<T>(dt), f, y, k1, k2, k3, s1);
+  asg::k_rk3_stage<T><<<gr, 256, 0, s>>>(1, n, static_cast<T>(dt), f, y, k1, k2, k3, S);
   if ((a = apply(y, k2))) return a;
-  asg::k_rk3_stage<T><<<gr, 256, 0, s>>>(2, n, static_cast<T>(dt), f, y, k1, k2, k3, s2);
+  asg::k_rk3_stage<T><<<gr, 256, 0, s>>>(2, n, static_cast<T>(dt), f, y, k1, k2, k3, S);
   if ((a = apply(y, k3))) return a;
-  asg::k_rk3_stage<T><<<gr, 256, 0, s>>>(3, n, static_cast<T>(dt), f, y, k1, k2, k3, s3);
+  asg::k_rk3_stage<T><<<gr, 256, 0, s>>>(3, n, static_cast<T>(dt), f, y, k1, k2, k3, S);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return asg::cuda_fail(e, "rk3 stage launch");
   return ASG_OK;
@@ -1253,12 +1395,37 @@ extern "C" {
 asg_status asg_rk3_step_f64(asg_plan* plan, double* d_f, double dt, const double* const* d_src, double* d_work,
                             size_t work_bytes, void* stream) {
   ASG_NOT_SLICE(plan, "rk3_step");
-  return rk3<double>(plan, d_f, dt, d_src, d_work, work_bytes, stream);
+  asg::Rk3Src<double> S{};
+  for (int k = 0; k < 3; ++k) S.src[k] = d_src ? d_src[k] : nullptr;
+  return rk3<double>(plan, d_f, dt, S, d_work, work_bytes, stream);
 }
 asg_status asg_rk3_step_f32(asg_plan* plan, float* d_f, double dt, const float* const* d_src, float* d_work,
                             size_t work_bytes, void* stream) {
   ASG_NOT_SLICE(plan, "rk3_step");
-  return rk3<float>(plan, d_f, dt, d_src, d_work, work_bytes, stream);
+  asg::Rk3Src<float> S{};
+  for (int k = 0; k < 3; ++k) S.src[k] = d_src ? d_src[k] : nullptr;
+  return rk3<float>(plan, d_f, dt, S, d_work, work_bytes, stream);
+}
+
+asg_status asg_rk3_step_sources_f64(asg_plan* plan, double* d_f, double dt, int ns, const double* d_coef,
+                                    const double* const* d_vecs, double* d_work, size_t work_bytes, void* stream) {
+  ASG_NOT_SLICE(plan, "rk3_step_sources");
+  if (ns < 0 || (ns > 0 && (!d_coef || !d_vecs))) return fail(ASG_ERR_INVALID, "rk3_step_sources: bad sources");
+  asg::Rk3Src<double> S{};
+  S.ns = ns;
+  S.coef = d_coef;
+  S.vecs = d_vecs;
+  return rk3<double>(plan, d_f, dt, S, d_work, work_bytes, stream);
+}
+asg_status asg_rk3_step_sources_f32(asg_plan* plan, float* d_f, double dt, int ns, const double* d_coef,
+                                    const double* const* d_vecs, float* d_work, size_t work_bytes, void* stream) {
+  ASG_NOT_SLICE(plan, "rk3_step_sources");
+  if (ns < 0 || (ns > 0 && (!d_coef || !d_vecs))) return fail(ASG_ERR_INVALID, "rk3_step_sources: bad sources");
+  asg::Rk3Src<float> S{};
+  S.ns = ns;
+  S.coef = d_coef;
+  S.vecs = d_vecs;
+  return rk3<float>(plan, d_f, dt, S, d_work, work_bytes, stream);
 }
 
 asg_status asg_lincomb_f64(long long n, int ns, const double* d_coef, const double* const* d_vecs, double* d_out,

@@ -317,11 +317,24 @@ asg_status asg_batch_info(const asg_batch* batch, int* warps_per_cta, int* rows_
  * three device source vectors at t, t+dt/2, t+dt (NULL array or entries = zero sources).
  * d_work: 16-byte aligned device workspace of 4 * round_up(dof, 16 / sizeof(value)) values
  * (four vectors, each on a 16-byte boundary).  Asynchronous, allocation-free, capturable into
- * a CUDA graph. */
+ * a CUDA graph.  For plans applied by the small-block kernel the step is one cooperative
+ * launch (three applies separated by grid barriers), otherwise three applies and three
+ * stage updates; the results are the same. */
 asg_status asg_rk3_step_f64(asg_plan* plan, double* d_f, double dt, const double* const* d_src, double* d_work,
                             size_t work_bytes, void* stream);
 asg_status asg_rk3_step_f32(asg_plan* plan, float* d_f, double dt, const float* const* d_src, float* d_work,
                             size_t work_bytes, void* stream);
+/* The same step with the stage sources formed inside it: source_k = sum_q d_coef[k*ns + q] *
+ * d_vecs[q] for the stage times k = 0, 1, 2 (t, t+dt/2, t+dt) -- the separable sources of
+ * source_vector.m, spatial parts times time factors -- summed in FP64 as asg_lincomb_f64 does
+ * and rounded once to the step's type.  d_coef (3*ns values) and d_vecs (ns device pointers to
+ * FP64 vectors) live on the device, so a captured step reads new time factors on replay.
+ * Equal to asg_lincomb_f64 per stage followed by asg_rk3_step_*; for plans applied by the
+ * small-block kernel the whole step is one cooperative launch. */
+asg_status asg_rk3_step_sources_f64(asg_plan* plan, double* d_f, double dt, int ns, const double* d_coef,
+                                    const double* const* d_vecs, double* d_work, size_t work_bytes, void* stream);
+asg_status asg_rk3_step_sources_f32(asg_plan* plan, float* d_f, double dt, int ns, const double* d_coef,
+                                    const double* const* d_vecs, float* d_work, size_t work_bytes, void* stream);
 /* d_out = sum_s d_coef[s] * d_vecs[s] (the separable sources of source_vector.m: spatial parts
  * times time factors); d_coef and d_vecs (an array of device pointers) live on the device. */
 asg_status asg_lincomb_f64(long long n, int ns, const double* d_coef, const double* const* d_vecs, double* d_out,

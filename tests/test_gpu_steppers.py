@@ -60,6 +60,40 @@ def test_rk3_matches_gold_trajectory(dev, name, pdename, lev, deg, graph):
         assert rel2(f.cpu().numpy(), g) <= 1e-13, i
 
 
+@pytest.mark.parametrize("pdename,lev,deg", [("continuity2", 4, 2), ("continuity3", 4, 3), ("continuity2", 3, 4)])
+@pytest.mark.parametrize("dtype", ["float64", "float32"])
+def test_rk3_step_equals_composed_step(dev, pdename, lev, deg, dtype):
+    """One RK3 step with its sources formed inside it (for small-block plans one cooperative
+    launch: three applies, two grid barriers) equals the step composed from three separate
+    applies, the stage formulas of time_advance.m:177-204 and the sources summed on the host,
+    to round-off."""
+    import asgkron
+    from asgkron import pdes
+    from asgkron.steppers import RK3Stepper
+
+    pde = getattr(pdes, pdename)(lev, 0.0)
+    idx = asgkron.hash_table_sparse_nD(pde.levels, 8).idx1d()
+    plan = asgkron.Plan.create(pde.term_mats(deg, construction_level=8), idx, deg)
+    tdt = torch.float64 if dtype == "float64" else torch.float32
+    st = RK3Stepper(plan, pde, idx, dtype=dtype)
+    f0 = torch.from_numpy(np.random.default_rng(8).standard_normal(plan.dof)).to(dev, tdt)
+    dt, t = pde.dt(0.01), 0.3
+    x = f0.clone()
+    st.step(x, t, dt)
+    torch.cuda.synchronize()
+    parts = [v.cpu().numpy() for v in st.vecs]
+    s1, s2, s3 = [torch.from_numpy(sum((fn(tt) * v for fn, v in zip(st.tfac, parts)), np.zeros(plan.dof))).to(dev, tdt)
+                  for tt in (t, t + 0.5 * dt, t + dt)]
+    k1 = plan.apply(f0) + s1
+    y = f0 + dt * 0.5 * k1
+    k2 = plan.apply(y) + s2
+    y = f0 + dt * (-k1 + 2 * k2)
+    k3 = plan.apply(y) + s3
+    want = f0 + dt * (k1 / 6 + 2 * k2 / 3 + k3 / 6)
+    assert rel2(x.double().cpu().numpy(), want.double().cpu().numpy()) <= (1e-14 if dtype == "float64" else 1e-6)
+    assert plan.device_status() == 0
+
+
 @pytest.mark.parametrize("name,lev,deg,grid", [("continuity2_implicit_l2_d2", 2, 2, "SG"),
                                                ("continuity2_implicit_l4_d3", 4, 3, "SG"),
                                                ("continuity2_implicit_fg_l3_4_d3", [3, 4], 3, "FG")])
