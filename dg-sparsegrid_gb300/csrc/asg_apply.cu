@@ -1331,6 +1331,7 @@ __global__ void __launch_bounds__(256) k_grad_items(GradArgs<T> a) {
       const int s = a.stride[e.k];
       if (s == 1) {
         // fibers are 4 contiguous values: G[x][y] += r[x] z[y]
+#pragma unroll 8
         for (int fb = lane; fb < B / P; fb += 32) {
           T rv[4], zv[4];
           load4(ri + fb * P, rv);
@@ -1343,6 +1344,7 @@ __global__ void __launch_bounds__(256) k_grad_items(GradArgs<T> a) {
       } else {
         // 4 fibers with consecutive fastest-dimension offsets per lane: one 16-byte load per
         // (fiber position x) holds the 4 fibers' values
+#pragma unroll 8
         for (int grp = lane; grp < B / (P * 4); grp += 32) {
           const int o = grp * 4;            // first of the 4 fibers (o = hi * s + lo)
           const int hi = o / s, lo = o - hi * s;
