@@ -461,6 +461,20 @@ __global__ void __launch_bounds__(32 * WR) k_rk3_fused(Rk3Args<T> r) {
   }
 }
 
+// CTAs of `kern` (threads per CTA, no dynamic shared memory) a cooperative launch can hold on
+// the current device; 0 when cooperative launches are unavailable or a query fails.
+template <typename K>
+long long coop_resident(K kern, int threads) {
+  int dev = 0, nsm = 0, coop = 0, per_sm = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess ||
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return coop ? static_cast<long long>(per_sm) * nsm : 0;
+}
+
 template <typename T, int P>
 cudaError_t launch_rk3_fused_p(const Rk3Args<T>& r, cudaStream_t s) {
   constexpr int WR = sizeof(T) == 4 ? 4 : 2;  // the split fiber kernel's warps per row
@@ -469,16 +483,9 @@ cudaError_t launch_rk3_fused_p(const Rk3Args<T>& r, cudaStream_t s) {
   auto go = [&](auto maxf) -> cudaError_t {
     constexpr int MF = decltype(maxf)::value;
     auto kern = k_rk3_fused<T, P, MF, K, WR>;
-    static long long resident = -1;  // co-resident CTAs, queried once per instantiation
-    if (resident < 0) {
-      int dev = 0, nsm = 0, coop = 0, per_sm = 0;
-      cudaError_t e;
-      if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-      if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-      if ((e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev)) != cudaSuccess) return e;
-      if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * WR, 0)) != cudaSuccess) return e;
-      resident = coop ? static_cast<long long>(per_sm) * nsm : 0;
-    }
+    // co-resident CTAs, queried once per instantiation (a thread-safe static); a failed query
+    // gives 0, and the step then runs as separate launches
+    static const long long resident = coop_resident(kern, 32 * WR);
     const int G = static_cast<int>(std::min<long long>(r.a.N, std::min<long long>(resident, 152 * 16)));
     if (G <= 0) return cudaErrorNotSupported;
     cudaLaunchConfig_t cfg{};
