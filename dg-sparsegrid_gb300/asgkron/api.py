@@ -370,17 +370,28 @@ def _get(obj, name, default=None):
     return getattr(obj, name, default)
 
 
-def apply_A(pde, opts, A_data, f, deg, Vmax=None, Emax=None, imex_flag="N"):
-    """Mirror of apply_A.m:1-252 (explicit path): returns ftmp = A*f as float64 numpy.
+def _cached_plan(mats, idx, deg, pairs):
+    key = (tuple((id(m), m.shape) for row in mats for m in row), idx.tobytes(), int(deg),
+           None if pairs is None else (pairs[0].tobytes(), pairs[1].tobytes()))
+    plan = _PLAN_CACHE.get(key)
+    if plan is None:
+        plan = Plan.create(mats, idx, deg, pairs=pairs, structure="detect", index_base=1)
+        _PLAN_CACHE[key] = plan
+    return plan
+
+
+def apply_A(pde, opts, A_data, f, deg, Vmax=None, Emax=None, imex_flag="N", nargout=1):
+    """Mirror of apply_A.m:1-252: returns ftmp = A*f as float64 numpy, or with nargout 2 or 3
+    the tuple (ftmp, A, ALHS) of the reference's build_A branch.
 
     pde.terms[t].terms_1D[d].mat and pde.terms[t].imex select the terms (apply_A.m:19-28);
     opts.use_connectivity selects pde.connectivity (1-based lists) over all pairs
-    (apply_A.m:44-52).  Plans are cached per operator/index set like a MEX persistent
-    handle; call clear_plan_cache() after mutating operators in place."""
-    terms = [t for t in _get(pde, "terms") if _get(t, "imex", "N") == imex_flag]
-    if not terms:
-        return np.zeros(np.asarray(f).size)
-    mats = [[_get(sd, "mat") for sd in _get(t, "terms_1D")] for t in terms]
+    (apply_A.m:44-52).  A is the operator of those terms over those pairs, assembled on the
+    GPU (apply_A.m:170-180), a scipy sparse matrix when opts.use_sparse_A and a dense array
+    otherwise; ALHS is the same assembly of pde.termsLHS, the non-identity LHS mass terms
+    (apply_A.m:209-221), or 0 when there are none (apply_A.m:55).  Plans are cached per
+    operator/index set like a MEX persistent handle; call clear_plan_cache() after mutating
+    operators in place."""
     idx = np.stack([np.asarray(v).reshape(-1) for v in _get(A_data, "element_local_index_D")], axis=1)
     pairs = None
     if _get(opts, "use_connectivity", False):
@@ -389,13 +400,31 @@ def apply_A(pde, opts, A_data, f, deg, Vmax=None, Emax=None, imex_flag="N"):
         rp = np.concatenate([[0], np.cumsum(lens)]).astype(np.int64)
         cl = np.concatenate([np.asarray(c, dtype=np.int64).reshape(-1) for c in conn]).astype(np.int32)
         pairs = (rp, cl)
-    key = (tuple((id(m), m.shape) for row in mats for m in row), idx.tobytes(), int(deg),
-           None if pairs is None else (pairs[0].tobytes(), pairs[1].tobytes()))
-    plan = _PLAN_CACHE.get(key)
-    if plan is None:
-        plan = Plan.create(mats, idx, deg, pairs=pairs, structure="detect", index_base=1)
-        _PLAN_CACHE[key] = plan
-    return plan.apply_host(np.asarray(f, dtype=np.float64).reshape(-1))
+    sparse = bool(_get(opts, "use_sparse_A", False))
+
+    def assembled(terms):
+        mats = [[_get(sd, "mat") for sd in _get(t, "terms_1D")] for t in terms]
+        A = _cached_plan(mats, idx, deg, pairs).assemble_bsr()
+        return A.tocsr() if sparse else A.toarray()
+
+    terms = [t for t in _get(pde, "terms") if _get(t, "imex", "N") == imex_flag]
+    n = np.asarray(f).size
+    if terms:
+        mats = [[_get(sd, "mat") for sd in _get(t, "terms_1D")] for t in terms]
+        ftmp = _cached_plan(mats, idx, deg, pairs).apply_host(np.asarray(f, dtype=np.float64).reshape(-1))
+    else:
+        ftmp = np.zeros(n)
+    if nargout <= 1:
+        return ftmp
+    if terms:
+        A = assembled(terms)
+    else:
+        import scipy.sparse as sp
+
+        A = sp.csr_matrix((n, n)) if sparse else np.zeros((n, n))
+    lhs = _get(pde, "termsLHS") or []
+    ALHS = assembled(lhs) if len(lhs) > 0 else 0
+    return ftmp, A, ALHS
 
 
 # -------------------------------------------------------------------------------------

@@ -315,6 +315,40 @@ def test_apply_A_matlab_mirror(dev):
     asgkron.clear_plan_cache()
 
 
+def test_apply_A_matlab_mirror_build_A(dev):
+    """[ftmp, A, ALHS] = apply_A(...): A and ALHS (a non-identity LHS mass term) equal the
+    oracle's krond assembly (apply_A.m:170-180,209-221), dense and sparse, over all pairs and
+    over pde.connectivity; ALHS is 0 without LHS terms (apply_A.m:55)."""
+    import asgkron
+
+    pde, table, idx, mats = problem("continuity2", 3, 2)
+    A_data = asgkron.global_matrix(table)
+    rng = np.random.default_rng(3)
+    lhs = [[np.eye(m.shape[0]) + 0.1 * rng.standard_normal(m.shape) for m in mats[0]]]
+    rp, cols = asgkron.connect_nD(table, 3, 3)
+    pde_obj = {"terms": [{"terms_1D": [{"mat": m} for m in row], "imex": "N"} for row in mats],
+               "termsLHS": [{"terms_1D": [{"mat": m} for m in lhs[0]]}],
+               "connectivity": asgkron.connectivity_cells(rp, cols)}
+    f = rng.standard_normal(idx.shape[0] * 4)
+    for conn in (False, True):
+        cc = pde_obj["connectivity"] if conn else None
+        want_y = O.apply_A_loop(mats, idx.astype(np.int64), 2, f, conn=cc)
+        _, want_A = O.apply_A_loop(mats, idx.astype(np.int64), 2, f, conn=cc, build_A=True)
+        _, want_L = O.apply_A_loop(lhs, idx.astype(np.int64), 2, f, conn=cc, build_A=True)
+        for sparse in (False, True):
+            y, A, AL = asgkron.apply_A(pde_obj, {"use_connectivity": conn, "use_sparse_A": sparse}, A_data, f, 2,
+                                       nargout=3)
+            Ad, ALd = (A.toarray(), AL.toarray()) if sparse else (A, AL)
+            assert rel2(y, want_y) <= FP64_TOL
+            assert rel2(Ad @ f, y) <= FP64_TOL
+            assert np.abs(Ad - want_A).max() <= 1e-12 * np.abs(want_A).max()
+            assert np.abs(ALd - want_L).max() <= 1e-12 * np.abs(want_L).max()
+    no_lhs = {"terms": pde_obj["terms"]}
+    y, A, AL = asgkron.apply_A(no_lhs, {}, A_data, f, 2, nargout=3)
+    assert isinstance(AL, int) and AL == 0
+    asgkron.clear_plan_cache()
+
+
 def test_argument_errors(dev):
     import asgkron
     from asgkron._lib import AsgError
