@@ -237,7 +237,7 @@ struct asg_plan {
   // mapped buffer, order d_hc_order[s]. Chunk c is positions [hc_estart[s][c],
   // hc_estart[s][c+1]) of the order, and its rows -- those whose blocks have all arrived with
   // it -- are hc_rows[s][hc_start[s][c] .. hc_start[s][c+1]), longest first
-  static constexpr int kHostChunks = 4;
+  static constexpr int kHostChunks = 5;
   std::vector<int> hc_estart[4], hc_start[4];
   int* d_hc_rows[4] = {};
   int* d_hc_order[4] = {};

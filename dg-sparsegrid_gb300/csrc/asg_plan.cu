@@ -720,15 +720,17 @@ asg_status apply_residual(asg_plan* p, const T* f, const T* ystar, T* r, void* s
 // page-locked): the row with the fewest elements still to come next, bringing them, so that
 // rows become ready -- and their y starts over the link -- while f is still arriving.  A row
 // is ready with the chunk that brings the last of its elements (itself and its columns).
-// Chunk sizes, each the fastest of the splits measured on the continuity6 workload:
-// contiguous FP32 N/2, N/4, 3N/20, N/10, FP64 (whose apply outlasts the copy, so it gains
-// from starting earlier) 2N/5, 3N/10, N/5, N/10; gathered 3N/10, N/4, N/4, N/5 in both.
+// Chunk sizes, each the fastest of the splits measured on the continuity6 workload (a
+// repeated 1.0 leaves the last chunk empty: no copy, no rows): contiguous FP32 N/2, N/4,
+// 3N/20, N/10, FP64 (whose apply outlasts the copy, so it gains from starting earlier) 2N/5,
+// 3N/10, N/5, N/10; gathered FP32 3N/10, N/4, N/5, 3N/20, N/10 (98 us with four chunks,
+// 92 us with these five), FP64 3N/10, N/4, N/4, N/5 (311 us; 339 us with FP32's five).
 asg_status host_chunks(asg_plan* p, int prec, bool gathered) {
   const int sch = 2 * gathered + prec;
   if (!p->hc_start[sch].empty()) return ASG_OK;
   const int N = p->N, K = asg_plan::kHostChunks;
   static const double kFracs[4][K] = {
-      {0.4, 0.7, 0.9, 1.0}, {0.5, 0.75, 0.9, 1.0}, {0.3, 0.55, 0.8, 1.0}, {0.3, 0.55, 0.8, 1.0}};
+      {0.4, 0.7, 0.9, 1.0, 1.0}, {0.5, 0.75, 0.9, 1.0, 1.0}, {0.3, 0.55, 0.8, 1.0, 1.0}, {0.3, 0.55, 0.75, 0.9, 1.0}};
   const double* kFrac = kFracs[sch];
   auto len = [&](int i) { return p->row_ptr[i + 1] - p->row_ptr[i]; };
   std::vector<int> order;
