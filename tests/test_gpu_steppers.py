@@ -60,6 +60,30 @@ def test_rk3_matches_gold_trajectory(dev, name, pdename, lev, deg, graph):
         assert rel2(f.cpu().numpy(), g) <= 1e-13, i
 
 
+def test_lincomb_matches_host_sum(dev):
+    """asg_lincomb_f64: sum_s coef[s] * vecs[s] (the separable sources of source_vector.m)
+    against the same sum on the host, to round-off; ns = 0 gives zeros."""
+    import ctypes as C
+
+    from asgkron._lib import check, lib
+
+    rng = np.random.default_rng(11)
+    n, ns = 1000, 3
+    vecs = [torch.from_numpy(rng.standard_normal(n)).to(dev) for _ in range(ns)]
+    ptrs = torch.tensor([v.data_ptr() for v in vecs], dtype=torch.int64, device=dev)
+    coef = torch.from_numpy(rng.standard_normal(ns)).to(dev)
+    out = torch.full((n,), float("nan"), dtype=torch.float64, device=dev)
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    check(lib().asg_lincomb_f64(n, ns, C.c_void_p(coef.data_ptr()), C.c_void_p(ptrs.data_ptr()),
+                                C.c_void_p(out.data_ptr()), s))
+    torch.cuda.synchronize()
+    want = sum(c * v for c, v in zip(coef.cpu().numpy(), [v.cpu().numpy() for v in vecs]))
+    assert rel2(out.cpu().numpy(), want) <= 1e-15
+    check(lib().asg_lincomb_f64(n, 0, None, None, C.c_void_p(out.data_ptr()), s))
+    torch.cuda.synchronize()
+    assert not out.any()
+
+
 @pytest.mark.parametrize("pdename,lev,deg", [("continuity2", 4, 2), ("continuity3", 4, 3), ("continuity2", 3, 4)])
 @pytest.mark.parametrize("dtype", ["float64", "float32"])
 def test_rk3_step_equals_composed_step(dev, pdename, lev, deg, dtype):
